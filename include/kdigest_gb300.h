@@ -1,0 +1,128 @@
+/*
+ * kdigest_gb300.h — C-ABI of the GB300 (sm_103a) t-digest engine.
+ *
+ * Plain pointers and sizes only.  Every entry point returns an int status
+ * (KD_OK on success) and leaves a message readable through kd_last_error().
+ * Digest state, centroid arithmetic, decay factors and scale evaluations are
+ * FP64 throughout.
+ *
+ * Each declaration cites the reference interface it replaces (paths inside the
+ * kdigest project, src/kdigest/...).  The reference's GPU backend is Mojo/MAX;
+ * its host code would bind these symbols with external_call.
+ */
+#ifndef KDIGEST_GB300_H
+#define KDIGEST_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define KD_API __attribute__((visibility("default")))
+#else
+#define KD_API
+#endif
+
+/* Status codes.  The reference raises Error(String); each raise site maps to one
+ * code (tdigest.mojo:317-322, grouped.mojo:74-97, tdigest.mojo:492-498,545-546,
+ * tdigest.mojo:661-662, gpu/primitives.mojo:260-268). */
+#define KD_OK 0
+#define KD_EINVAL 1     /* non-finite value, weight <= 0, key out of range, q outside [0,1] */
+#define KD_EEMPTY 2     /* quantile / cdf of an empty digest */
+#define KD_ERANGE 3     /* output capacity too small (needed size returned), truncated bytes */
+#define KD_ECONVERGE 4  /* P-path pass could not shrink a key (the reference loops forever) */
+#define KD_ENOMEM 5     /* over the session's device-memory budget / allocation failure */
+#define KD_ECUDA 6      /* CUDA runtime error */
+#define KD_ETIMEOUT 7   /* a bounded device wait gave up (serving loop) */
+
+/* Scale functions — src/kdigest/scale.mojo:78-200 (ScaleK0..ScaleK3). */
+#define KD_K0 0
+#define KD_K1 1
+#define KD_K2 2
+#define KD_K3 3
+
+/* Clock modes of an ingest: count clock (add_batch, tdigest.mojo:177-296) or
+ * time clock (add_at semantics with one timestamp per batch, :163-175). */
+#define KD_CLOCK_COUNT 0
+#define KD_CLOCK_TIME 1
+
+/* Pointer flag: inputs/outputs of the call are device pointers (no H2D/D2H). */
+#define KD_PTR_DEVICE 1
+
+/* Session options (kd_session_set_option). */
+#define KD_OPT_FORCE_EXACT_K 1 /* evaluate every bucket id in FP64 (no FP32 filter) */
+#define KD_OPT_MAX_LEVELS 2    /* levels of the tile hierarchy run per ingest (default 8) */
+
+typedef struct kd_session kd_session;
+typedef struct kd_store kd_store;
+
+KD_API int kd_version(void);
+KD_API const char* kd_status_string(int status);
+
+/* GpuSession (gpu/session.mojo:19-27): device context + reusable workspaces.
+ * mem_budget = 0 means no limit.  Not thread-safe (as the reference). */
+KD_API int kd_session_create(int device, size_t mem_budget, kd_session** out);
+KD_API void kd_session_destroy(kd_session* s);
+KD_API const char* kd_last_error(kd_session* s);
+KD_API int kd_session_sync(kd_session* s);
+KD_API int kd_session_set_option(kd_session* s, int option, int value);
+/* The CUDA stream (cudaStream_t) all work of this session is ordered on. */
+KD_API void* kd_session_stream(kd_session* s);
+
+/* gpu_compress_batch[S] (gpu/add_batch.mojo:629-663): P-path compress of an
+ * arbitrary (mean, weight) set -> mean-sorted centroids.  out arrays hold cap
+ * entries; KD_ERANGE with *out_n = needed when cap is too small. */
+KD_API int kd_compress(kd_session* s, int scale, double compression, const double* means,
+                       const double* weights, int64_t n, int flags, double* out_means,
+                       double* out_weights, int64_t cap, int64_t* out_n);
+
+/* Resident per-key digests (GroupedTDigest, grouped.mojo:30-58; one key is a
+ * TDigest, tdigest.mojo:135-151): num_keys dense ids, shared scale, compression
+ * and decay rate (Decay.rate / half_life, decay.mojo:24-47; 0 = none). */
+KD_API int kd_store_create(kd_session* s, int64_t num_keys, int scale, double compression,
+                           double decay_lambda, kd_store** out);
+KD_API void kd_store_destroy(kd_store* st);
+
+/* GroupedTDigest.add_batch (grouped.mojo:60-162) / TDigest.add_batch on the GPU
+ * route (tdigest.mojo:223-315): unit-weight samples; keys may be NULL (all key 0).
+ * The whole batch is validated before any digest changes. */
+KD_API int kd_store_ingest(kd_store* st, const uint32_t* keys, const double* values, int64_t n,
+                           int clock_mode, double timestamp, int flags);
+
+/* TDigest.quantile / cdf per (key, q|x) (tdigest.mojo:485-587); keys may be
+ * NULL (all key 0).  Errors fill NaN and return the first failing status. */
+KD_API int kd_store_quantile(kd_store* st, const uint32_t* keys, const double* qs, int64_t nq,
+                             double* out, int flags);
+KD_API int kd_store_cdf(kd_store* st, const uint32_t* keys, const double* xs, int64_t nx,
+                        double* out, int flags);
+
+/* gpu_merge_digests (gpu/query.mojo:348-369) with merge_into's rebasing
+ * (tdigest.mojo:589-623), batched: dst key g becomes the P-path compress of the
+ * concatenated centroids of src keys parts[group_offsets[g] .. group_offsets[g+1])
+ * in order.  Host pointers. */
+KD_API int kd_store_merge(kd_store* dst, kd_store* src, const int64_t* group_offsets,
+                          const uint32_t* parts, int64_t ngroups);
+
+/* One key's state.  header8 = compression, decay lambda, log_scale, clock,
+ * stored_total, min, max, count (the to_bytes header, tdigest.mojo:634-648). */
+KD_API int kd_store_get_digest(kd_store* st, uint32_t key, double* header8, double* means,
+                               double* weights, int64_t cap, int64_t* out_count);
+KD_API int kd_store_set_digest(kd_store* st, uint32_t key, const double* header8,
+                               const double* means, const double* weights, int64_t count);
+
+/* to_bytes / from_bytes wire format (tdigest.mojo:627-698). */
+KD_API int kd_store_to_bytes(kd_store* st, uint32_t key, uint8_t* buf, int64_t cap,
+                             int64_t* out_len);
+KD_API int kd_store_from_bytes(kd_store* st, uint32_t key, const uint8_t* buf, int64_t len);
+
+KD_API int kd_store_stats(kd_store* st, int64_t* num_keys, int64_t* total_centroids,
+                          size_t* device_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KDIGEST_GB300_H */

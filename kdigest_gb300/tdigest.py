@@ -1,0 +1,454 @@
+"""Host mirror of the reference kdigest API over the GB300 engine.
+
+Names, argument meaning and error behaviour follow the reference
+(src/kdigest/tdigest.mojo, grouped.mojo, decay.mojo, gpu/session.mojo):
+
+  * ``Decay.none / rate / half_life``           (decay.mojo:24-51)
+  * ``TDigest(compression, scale, decay)``       (tdigest.mojo:135-151)
+      add_batch / add_batch_at / add / add_at, quantile, cdf, merge_into,
+      to_bytes / from_bytes, total_weight, min, max, len
+  * ``GroupedTDigest(num_keys, compression, decay)`` (grouped.mojo:30-190)
+  * ``GpuSession``                                (gpu/session.mojo:19-27)
+
+Every batch takes the reference's GPU route (the P-path: parallel
+k-bucketing over 1024-element tiles), in FP64.  Errors the reference raises
+surface as ``ValueError`` (invalid input), ``IndexError`` (key out of range)
+or ``KdError`` (engine status), and a rejected batch leaves every digest
+unchanged.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _native as N
+from ._native import KdError
+
+K0, K1, K2, K3 = N.KD_K0, N.KD_K1, N.KD_K2, N.KD_K3
+SCALES = {"K0": K0, "K1": K1, "K2": K2, "K3": K3}
+
+
+def _check(sess_handle, rc: int):
+    if rc == N.KD_OK:
+        return
+    msg = N.load().kd_last_error(sess_handle).decode(errors="replace")
+    if rc == N.KD_EINVAL:
+        raise ValueError(msg)
+    if rc == N.KD_EEMPTY:
+        raise ValueError(msg)
+    raise KdError(rc, msg)
+
+
+class Decay:
+    """Exponential decay rate lambda per unit of the digest's clock."""
+
+    def __init__(self, rate_lambda: float = 0.0):
+        self.rate_lambda = float(rate_lambda)
+
+    @staticmethod
+    def none() -> "Decay":
+        return Decay(0.0)
+
+    @staticmethod
+    def rate(lambda_: float) -> "Decay":
+        return Decay(lambda_)
+
+    @staticmethod
+    def half_life(h: float) -> "Decay":
+        if not h > 0.0:
+            raise ValueError("half_life must be positive")
+        return Decay(math.log(2.0) / h)
+
+    def is_active(self) -> bool:
+        return self.rate_lambda > 0.0
+
+    def __repr__(self):
+        return f"Decay(lambda={self.rate_lambda})"
+
+
+class GpuSession:
+    """One device, one CUDA stream, reusable workspaces (gpu/session.mojo)."""
+
+    def __init__(self, device: int = 0, mem_budget: int = 0):
+        L = N.load()
+        h = ctypes.c_void_p()
+        rc = L.kd_session_create(device, mem_budget, ctypes.byref(h))
+        if rc != N.KD_OK:
+            raise KdError(rc, f"kd_session_create failed ({L.kd_status_string(rc).decode()})")
+        self._h = h.value
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_option(self, option: int, value: int):
+        _check(self._h, N.load().kd_session_set_option(self._h, option, value))
+
+    def sync(self):
+        _check(self._h, N.load().kd_session_sync(self._h))
+
+    @property
+    def stream(self) -> int:
+        return N.load().kd_session_stream(self._h) or 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().kd_session_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_session = None
+
+
+def default_session() -> GpuSession:
+    global _default_session
+    if _default_session is None:
+        _default_session = GpuSession()
+    return _default_session
+
+
+def compress(means, weights, compression: float = 100.0, scale: int = K1,
+             session: GpuSession | None = None):
+    """gpu_compress_batch (gpu/add_batch.mojo:629-663): P-path compress of an
+    arbitrary (mean, weight) set.  Returns (means, weights) as float64 arrays."""
+    s = session or default_session()
+    m = np.ascontiguousarray(means, dtype=np.float64)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    if m.shape != w.shape:
+        raise ValueError("means and weights must have equal length")
+    n = len(m)
+    cap = min(max(n, 1), 1024)
+    om = np.empty(cap)
+    ow = np.empty(cap)
+    out_n = ctypes.c_int64(0)
+    rc = N.load().kd_compress(s.handle, scale, compression, N.ptr(m), N.ptr(w), n, 0, N.ptr(om),
+                              N.ptr(ow), cap, ctypes.byref(out_n))
+    _check(s.handle, rc)
+    return om[:out_n.value].copy(), ow[:out_n.value].copy()
+
+
+class _Store:
+    """A resident store of num_keys digests on the device."""
+
+    def __init__(self, num_keys: int, compression: float, scale: int, decay: Decay,
+                 session: GpuSession | None):
+        self.session = session or default_session()
+        self.num_keys = int(num_keys)
+        self.compression = float(compression)
+        self.scale = int(scale)
+        self.decay = decay if decay is not None else Decay.none()
+        h = ctypes.c_void_p()
+        rc = N.load().kd_store_create(self.session.handle, self.num_keys, self.scale,
+                                      self.compression, self.decay.rate_lambda, ctypes.byref(h))
+        _check(self.session.handle, rc)
+        self._h = h.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                N.load().kd_store_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        _check(self.session.handle, rc)
+
+    def ingest(self, keys, values, clock_mode=N.KD_CLOCK_COUNT, timestamp=0.0):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        k = None
+        if keys is not None:
+            k = np.asarray(keys)
+            if len(k) != len(v):
+                raise ValueError("keys and values must have equal length")
+            if k.dtype.kind == "i" and len(k) and (k.min() < 0):
+                raise IndexError("key out of range [0, num_keys)")
+            k = np.ascontiguousarray(k, dtype=np.uint32)
+        rc = N.load().kd_store_ingest(self._h, N.ptr(k), N.ptr(v), len(v), clock_mode, timestamp, 0)
+        if rc == N.KD_EINVAL and k is not None and len(k) and int(k.max()) >= self.num_keys:
+            raise IndexError("key out of range [0, num_keys)")
+        self._chk(rc)
+
+    def query(self, keys, xs, is_cdf: bool):
+        x = np.ascontiguousarray(xs, dtype=np.float64)
+        k = None if keys is None else np.ascontiguousarray(keys, dtype=np.uint32)
+        out = np.empty(len(x))
+        fn = N.load().kd_store_cdf if is_cdf else N.load().kd_store_quantile
+        self._chk(fn(self._h, N.ptr(k), N.ptr(x), len(x), N.ptr(out), 0))
+        return out
+
+    def digest(self, key: int):
+        hdr = np.empty(8)
+        cnt = ctypes.c_int64(0)
+        self._chk(N.load().kd_store_get_digest(self._h, key, N.ptr(hdr), None, None, 0,
+                                               ctypes.byref(cnt)))
+        m = np.empty(max(cnt.value, 1))
+        w = np.empty(max(cnt.value, 1))
+        self._chk(N.load().kd_store_get_digest(self._h, key, N.ptr(hdr), N.ptr(m), N.ptr(w),
+                                               cnt.value, ctypes.byref(cnt)))
+        return hdr, m[:cnt.value].copy(), w[:cnt.value].copy()
+
+    def set_digest(self, key: int, hdr, means, weights):
+        hdr = np.ascontiguousarray(hdr, dtype=np.float64)
+        m = np.ascontiguousarray(means, dtype=np.float64)
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        self._chk(N.load().kd_store_set_digest(self._h, key, N.ptr(hdr), N.ptr(m), N.ptr(w), len(m)))
+
+    def to_bytes(self, key: int) -> bytes:
+        n = ctypes.c_int64(0)
+        self._chk(N.load().kd_store_to_bytes(self._h, key, None, 0, ctypes.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        self._chk(N.load().kd_store_to_bytes(self._h, key, N.ptr(buf), n.value, ctypes.byref(n)))
+        return buf.tobytes()
+
+    def from_bytes(self, key: int, data: bytes):
+        buf = np.frombuffer(bytes(data), np.uint8).copy() if len(data) else np.zeros(1, np.uint8)
+        rc = N.load().kd_store_from_bytes(self._h, key, N.ptr(buf), len(data))
+        self._chk(rc)
+
+    def merge_from(self, src: "_Store", group_offsets, parts):
+        go = np.ascontiguousarray(group_offsets, dtype=np.int64)
+        pa = np.ascontiguousarray(parts, dtype=np.uint32)
+        self._chk(N.load().kd_store_merge(self._h, src._h, N.ptr(go), N.ptr(pa), len(go) - 1))
+
+
+def _validate_values(values) -> np.ndarray:
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    if v.size and not np.all(np.isfinite(v)):
+        raise ValueError("value must be finite (got NaN or inf)")
+    return v
+
+
+class TDigest:
+    """One t-digest on the device (tdigest.mojo:97-726) — a one-key store."""
+
+    def __init__(self, compression: float = 100.0, scale: int = K1, decay: Decay | None = None,
+                 session: GpuSession | None = None, _store: _Store | None = None):
+        self.compression = float(compression)
+        self.scale = scale
+        self._decay = decay if decay is not None else Decay.none()
+        self._store = _store or _Store(1, compression, scale, self._decay, session)
+
+    @property
+    def session(self) -> GpuSession:
+        return self._store.session
+
+    # -- ingest ---------------------------------------------------------------
+    def add_batch(self, values, session: GpuSession | None = None):
+        """Fold a batch of unit-weight samples in (tdigest.mojo:177-234); the
+        clock advances by len(values) ticks."""
+        v = _validate_values(values)
+        if v.size == 0:
+            return
+        self._store.ingest(None, v, N.KD_CLOCK_COUNT, 0.0)
+
+    def add_batch_at(self, values, timestamp: float):
+        """Batch form of add_at (tdigest.mojo:163-175): the clock moves to
+        `timestamp` once when later, then every sample is inserted."""
+        v = _validate_values(values)
+        if v.size == 0:
+            return
+        self._store.ingest(None, v, N.KD_CLOCK_TIME, float(timestamp))
+
+    def add(self, value: float, weight: float = 1.0):
+        """One unit-weight sample as a batch of one (P-path)."""
+        if weight != 1.0:
+            if not (weight > 0.0) or not math.isfinite(weight):
+                raise ValueError("weight must be positive and finite")
+            raise ValueError("weighted samples are not part of the GPU batch path")
+        self.add_batch([value])
+
+    def add_at(self, value: float, timestamp: float, weight: float = 1.0):
+        if weight != 1.0:
+            if not (weight > 0.0) or not math.isfinite(weight):
+                raise ValueError("weight must be positive and finite")
+            raise ValueError("weighted samples are not part of the GPU batch path")
+        self.add_batch_at([value], timestamp)
+
+    def merge(self):
+        """Every batch is already compressed; nothing is buffered."""
+
+    # -- queries --------------------------------------------------------------
+    def quantile(self, q: float) -> float:
+        if not (0.0 <= q <= 1.0):
+            raise ValueError("quantile q must be in [0, 1]")
+        return float(self._store.query(None, [q], False)[0])
+
+    def cdf(self, x: float) -> float:
+        return float(self._store.query(None, [x], True)[0])
+
+    def quantiles(self, qs) -> np.ndarray:
+        return self._store.query(None, qs, False)
+
+    def cdfs(self, xs) -> np.ndarray:
+        return self._store.query(None, xs, True)
+
+    # -- state ----------------------------------------------------------------
+    def _state(self):
+        return self._store.digest(0)
+
+    def centroids(self):
+        _, m, w = self._state()
+        return m, w
+
+    def __len__(self) -> int:
+        return int(self._state()[0][7])
+
+    def total_weight(self) -> float:
+        hdr = self._state()[0]
+        if self._decay.is_active():
+            return float(hdr[4] * math.exp(-hdr[2]))
+        return float(hdr[4])
+
+    def min(self) -> float:
+        return float(self._state()[0][5])
+
+    def max(self) -> float:
+        return float(self._state()[0][6])
+
+    def state(self) -> dict:
+        hdr = self._state()[0]
+        keys = ("compression", "lambda", "log_scale", "clock", "stored_total", "min", "max", "count")
+        return dict(zip(keys, hdr.tolist()))
+
+    # -- merge / serde --------------------------------------------------------
+    def merge_into(self, other: "TDigest"):
+        """Fold `other` into this digest: both rebased to effective weights,
+        centroids concatenated (self first) and compressed once with the
+        P-path (gpu/query.mojo:348-369, tdigest.mojo:589-623)."""
+        merge_digests(self, [self, other])
+
+    def to_bytes(self) -> bytes:
+        return self._store.to_bytes(0)
+
+    @staticmethod
+    def from_bytes(data: bytes, scale: int = K1, session: GpuSession | None = None) -> "TDigest":
+        if len(data) == 0 or data[0] != 1:
+            raise ValueError("unrecognized digest serialization version")
+        if len(data) < 65:
+            raise ValueError("truncated digest: not enough bytes for a Float64")
+        hdr = np.frombuffer(bytes(data[1:65]), dtype="<f8")
+        d = TDigest(compression=float(hdr[0]), scale=scale, decay=Decay.rate(float(hdr[1])),
+                    session=session)
+        try:
+            d._store.from_bytes(0, data)
+        except KdError as e:
+            if e.code == N.KD_ERANGE:
+                raise ValueError(e.message) from None
+            raise
+        return d
+
+
+def merge_digests(dst: TDigest, parts) -> None:
+    """Replace `dst` by the P-path merge of `parts` (gpu_merge_digests)."""
+    sess = dst.session
+    tmp = _Store(len(parts), parts[0].compression, parts[0].scale, parts[0]._decay, sess)
+    for i, p in enumerate(parts):
+        hdr, m, w = p._state()
+        tmp.set_digest(i, hdr, m, w)
+    dst._store.merge_from(tmp, [0, len(parts)], np.arange(len(parts), dtype=np.uint32))
+
+
+class GroupedTDigest:
+    """num_keys independent digests updated together (grouped.mojo:30-190)."""
+
+    def __init__(self, num_keys: int, compression: float = 100.0, decay: Decay | None = None,
+                 scale: int = K2, session: GpuSession | None = None):
+        self.num_keys = int(num_keys)
+        self.compression = float(compression)
+        self.decay = decay if decay is not None else Decay.none()
+        self.scale = scale
+        self._store = _Store(num_keys, compression, scale, self.decay, session)
+
+    @property
+    def session(self) -> GpuSession:
+        return self._store.session
+
+    def _check_keys(self, keys) -> np.ndarray:
+        k = np.asarray(keys)
+        if k.size and (k.min() < 0 or k.max() >= self.num_keys):
+            raise IndexError("key out of range [0, num_keys)")
+        return np.ascontiguousarray(k, dtype=np.uint32)
+
+    def add_batch(self, keys, values):
+        """Fold (key, value) samples into their per-key digests; every key's
+        clock advances by its own sample count.  Validated before mutation."""
+        k = np.asarray(keys)
+        v = np.asarray(values)
+        if len(k) != len(v):
+            raise ValueError("keys and values must have equal length")
+        if len(v) == 0:
+            return
+        k = self._check_keys(k)
+        v = _validate_values(v)
+        self._store.ingest(k, v, N.KD_CLOCK_COUNT, 0.0)
+
+    def add_batch_at(self, keys, values, timestamp: float):
+        k = np.asarray(keys)
+        v = np.asarray(values)
+        if len(k) != len(v):
+            raise ValueError("keys and values must have equal length")
+        if len(v) == 0:
+            return
+        k = self._check_keys(k)
+        v = _validate_values(v)
+        self._store.ingest(k, v, N.KD_CLOCK_TIME, float(timestamp))
+
+    def _key(self, key: int) -> int:
+        if key < 0 or key >= self.num_keys:
+            raise IndexError("key out of range [0, num_keys)")
+        return int(key)
+
+    def quantile(self, key: int, q: float) -> float:
+        self._key(key)
+        if not (0.0 <= q <= 1.0):
+            raise ValueError("quantile q must be in [0, 1]")
+        return float(self._store.query([key], [q], False)[0])
+
+    def cdf(self, key: int, x: float) -> float:
+        self._key(key)
+        return float(self._store.query([key], [x], True)[0])
+
+    def quantiles(self, keys, qs) -> np.ndarray:
+        return self._store.query(self._check_keys(keys), qs, False)
+
+    def cdfs(self, keys, xs) -> np.ndarray:
+        return self._store.query(self._check_keys(keys), xs, True)
+
+    def to_bytes(self, key: int) -> bytes:
+        return self._store.to_bytes(self._key(key))
+
+    def from_bytes(self, key: int, data: bytes):
+        self._store.from_bytes(self._key(key), data)
+
+    def centroid_count(self, key: int) -> int:
+        return int(self._store.digest(self._key(key))[0][7])
+
+    def centroids(self, key: int):
+        _, m, w = self._store.digest(self._key(key))
+        return m, w
+
+    def state(self, key: int) -> dict:
+        hdr = self._store.digest(self._key(key))[0]
+        keys = ("compression", "lambda", "log_scale", "clock", "stored_total", "min", "max", "count")
+        return dict(zip(keys, hdr.tolist()))
+
+    def total_weight(self, key: int) -> float:
+        hdr = self._store.digest(self._key(key))[0]
+        if self.decay.is_active():
+            return float(hdr[4] * math.exp(-hdr[2]))
+        return float(hdr[4])
+
+    def merge_groups(self, src: "GroupedTDigest", group_offsets, parts):
+        """Batched merge_into: key g of this store becomes the P-path merge of
+        src keys parts[group_offsets[g]:group_offsets[g+1]] (in order)."""
+        self._store.merge_from(src._store, group_offsets, parts)
