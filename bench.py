@@ -1,0 +1,461 @@
+#!/usr/bin/env python3
+"""Grouped-ingest benchmark on one GB300 (and the CPU reference arm).
+
+Workload (the grouped per-key configuration): 65,536 keys with Zipf(s=1.1)
+frequencies (rank -> key id permuted by seed), 2^27 (uint32 key, FP64 value)
+pairs; per key 95% N(mu_k, 1) and 5% mu_k + Pareto(alpha=1.5, scale 1), with
+mu_k ~ U(-100, 100); TDigest[ScaleK3], compression 100, no decay; ingested in
+batches of 2^22, then 7 tail and median quantiles for every key.  Inputs are
+seeded synthetic data generated on the host (numpy) and copied once to HBM.
+
+A step is the ingest of one 2^22 batch into the resident 65,536-key store (the
+default 3 warm-up + 29 timed steps ingest the whole 2^27-sample stream).  Each
+step reads a fresh 48 MiB slice of a 1.5 GiB device-resident stream and the L2
+is flushed (a 256 MiB write) between timed steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NUM_KEYS = 65536
+ZIPF_S = 1.1
+TOTAL = 1 << 27
+BATCH = 1 << 22
+COMPRESSION = 100.0
+QUANTILES = (0.001, 0.01, 0.1, 0.5, 0.9, 0.99, 0.999)
+SEED = 2026
+METRIC = "grouped ingest samples/s (65,536 Zipf keys, K3 d100)"
+WORKLOAD = "grouped-ingest 2^27 Zipf(1.1)-keyed FP64 samples into 65,536 TDigest[K3] (compression 100) in 2^22 batches, then 7 quantiles per key"
+
+
+# ----------------------------------------------------------------------------
+# Workload
+# ----------------------------------------------------------------------------
+def make_workload(seed: int = SEED, num_keys: int = NUM_KEYS, total: int = TOTAL,
+                  batch: int = BATCH):
+    rng = np.random.default_rng(seed)
+    p = 1.0 / np.arange(1, num_keys + 1, dtype=np.float64) ** ZIPF_S
+    cdf = np.cumsum(p)
+    cdf /= cdf[-1]
+    perm = rng.permutation(num_keys).astype(np.uint32)
+    mu = rng.uniform(-100.0, 100.0, num_keys)
+    nb = total // batch
+    keys = np.empty(total, np.uint32)
+    vals = np.empty(total, np.float64)
+    seeds = np.random.SeedSequence(seed + 1).spawn(nb)
+
+    def fill(b):
+        r = np.random.default_rng(seeds[b])
+        lo = b * batch
+        u = r.random(batch)
+        rank = np.minimum(np.searchsorted(cdf, u, side="right"), num_keys - 1)
+        k = perm[rank]
+        v = r.standard_normal(batch) + mu[k]
+        tail = r.random(batch) < 0.05
+        v[tail] = mu[k[tail]] + (r.pareto(1.5, int(tail.sum())) + 1.0)
+        keys[lo:lo + batch] = k
+        vals[lo:lo + batch] = v
+
+    threads = [threading.Thread(target=lambda bs=bs: [fill(b) for b in bs])
+               for bs in np.array_split(np.arange(nb), min(nb, os.cpu_count() or 1))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    return keys, vals
+
+
+# ----------------------------------------------------------------------------
+# Clock sampling during the timed region
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+# ----------------------------------------------------------------------------
+# CPU arms (oracle = CPU restatement of the reference path)
+# ----------------------------------------------------------------------------
+def cpu_ingest_rate(keys, vals, threads: int, target_s: float = 12.0):
+    """Time the oracle's grouped P-path ingest on whole batches of the stream
+    until about target_s seconds of CPU work; returns samples/s and the sample."""
+    from oracle import pyoracle as o
+
+    digests = [o.Digest(o.K3, COMPRESSION, 0.0) for _ in range(NUM_KEYS)]
+    done = 0
+    t_total = 0.0
+    nb = len(vals) // BATCH
+    for b in range(nb):
+        sl = slice(b * BATCH, (b + 1) * BATCH)
+        t0 = time.perf_counter()
+        o.grouped_add_batch(digests, keys[sl], vals[sl], threads=threads)
+        t_total += time.perf_counter() - t0
+        done += 1
+        if t_total >= target_s:
+            break
+    return done * BATCH / t_total, done, t_total, digests
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    keys, vals = make_workload(total=TOTAL)
+    threads = os.cpu_count() or 1
+    per_step = []
+    digests = None
+    from oracle import pyoracle as o
+
+    digests = [o.Digest(o.K3, COMPRESSION, 0.0) for _ in range(NUM_KEYS)]
+    # bounded sample per step: one 2^22 batch of the stream per step
+    nb = len(vals) // BATCH
+    for i in range(args.warmup + args.steps):
+        b = i % nb
+        sl = slice(b * BATCH, (b + 1) * BATCH)
+        t0 = time.perf_counter()
+        o.grouped_add_batch(digests, keys[sl], vals[sl], threads=threads)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            per_step.append(dt)
+        if sum(per_step) > 90.0:
+            break
+    k = len(per_step)
+    v = k * BATCH / sum(per_step)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "samples/s",
+        "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(per_step) / k, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy, host)",
+        "config": {"workload": WORKLOAD, "keys": NUM_KEYS, "batch": BATCH, "scale": "K3",
+                   "compression": COMPRESSION},
+        "cpu_baseline": {"value": v, "unit": "samples/s", "cores": threads, "kind": "port",
+                         "sample": f"{k} batches of 2^22 pairs of the stream (C oracle, P-path, key-partitioned threads)"},
+        "e2e": {"value": v, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+
+    import kdigest_gb300 as kd
+    from kdigest_gb300 import _native as N
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+
+    keys, vals = make_workload(total=TOTAL)
+    nb = TOTAL // BATCH
+    d_keys = torch.from_numpy(keys).to(dev)
+    d_vals = torch.from_numpy(vals).to(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    sess = kd.GpuSession(local_rank)
+    sess.set_option(N.KD_OPT_STAGE_TIMING, 1)
+    ext = torch.cuda.ExternalStream(sess.stream, device=dev)
+    store = kd.GroupedTDigest(NUM_KEYS, COMPRESSION, scale=kd.K3, session=sess)
+    L = N.load()
+    h = store._store._h
+
+    def ingest_dev(b):
+        kp = d_keys.data_ptr() + b * BATCH * 4
+        vp = d_vals.data_ptr() + b * BATCH * 8
+        rc = L.kd_store_ingest(h, kp, vp, BATCH, N.KD_CLOCK_COUNT, 0.0, N.KD_PTR_DEVICE)
+        if rc:
+            raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+
+    for i in range(args.warmup):
+        ingest_dev(i % nb)
+    torch.cuda.synchronize()
+    sess.reset_stats()
+
+    times = []
+    compulsory = []
+    counts_before = store.centroid_counts()
+    sampler = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    for i in range(args.steps):
+        b = (args.warmup + i) % nb
+        flush.fill_(i & 0xFF)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        ingest_dev(b)
+        e1.record(ext)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        # compulsory bytes of this step (outside the timed region): 12 B per
+        # sample, 16 B per prior and per output centroid of every touched key,
+        # 2 x 48 B of per-key header
+        counts_after = store.centroid_counts()
+        touched = np.bincount(keys[b * BATCH:(b + 1) * BATCH], minlength=NUM_KEYS) > 0
+        compulsory.append(12 * BATCH + int(16 * (counts_before[touched].sum() + counts_after[touched].sum()))
+                          + 96 * int(touched.sum()))
+        counts_before = counts_after
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    if dist:
+        dist.barrier()
+    st = sess.stats()
+    step_ms = sum(times) / len(times)
+    local_total_ms = sum(times)
+    total_ms = local_total_ms
+    if dist:
+        t = torch.tensor([local_total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps * BATCH / (total_ms / 1e3)
+
+    # Queries: 7 quantiles for every key, one launch, device pointers.
+    qk = torch.arange(NUM_KEYS, dtype=torch.int32, device=dev).repeat_interleave(len(QUANTILES)).contiguous()
+    qq = torch.tensor(QUANTILES, dtype=torch.float64, device=dev).repeat(NUM_KEYS).contiguous()
+    qo = torch.empty_like(qq)
+    torch.cuda.synchronize()
+    q_times = []
+    for r in range(6):
+        flush.fill_(r)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        rc = L.kd_store_quantile(h, qk.data_ptr(), qq.data_ptr(), qq.numel(), qo.data_ptr(), N.KD_PTR_DEVICE)
+        e1.record(ext)
+        e1.synchronize()
+        if rc:
+            raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+        if r >= 3:
+            q_times.append(e0.elapsed_time(e1))
+    qps = qq.numel() / (statistics.median(q_times) / 1e3)
+
+    comp_bytes = sum(compulsory) / len(compulsory)
+    peaks = measured_peaks()
+    step_gbs = sum(compulsory) / (sum(times) / 1e3) / 1e9
+    touched_avg = np.mean([(np.bincount(keys[b * BATCH:(b + 1) * BATCH], minlength=NUM_KEYS) > 0).sum()
+                           for b in range(min(nb, 4))])
+    prior_avg = float(counts_before.sum()) / NUM_KEYS
+
+    # Dominant stage (kernel group) from the stage events on the launching stream.
+    stage_ms = {k: v / max(1, st["ingests"]) for k, v in st["stage_ms"].items()}
+    dom = max(stage_ms, key=stage_ms.get)
+    passes = 8 + 2  # 64 value bits + 16 key bits, 8-bit digits
+    alg = {
+        # radix passes: histogram read of the digit source + scatter read/write of 12 B pairs
+        "sort": passes * BATCH * (8 + 24) - 2 * BATCH * 4,
+        "level0": 8 * BATCH + touched_avg * 16 * 2 * prior_avg,
+        "prep": 12 * BATCH + 12 * BATCH,
+    }
+    dom_bytes = alg.get(dom, comp_bytes)
+    achieved = dom_bytes / (stage_ms[dom] / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                "peak_source": peaks["source"], "algorithmic_bytes": int(dom_bytes),
+                "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()}}
+
+    # End to end through the public C-ABI with pinned host buffers: H2D of the
+    # step's keys and values and D2H of the step's status word inside the step.
+    e2e = None
+    if rank == 0 or True:
+        store2 = kd.GroupedTDigest(NUM_KEYS, COMPRESSION, scale=kd.K3, session=sess)
+        h2 = store2._store._h
+        pk = torch.from_numpy(keys).pin_memory()
+        pv = torch.from_numpy(vals).pin_memory()
+        for i in range(args.warmup):
+            b = i % nb
+            L.kd_store_ingest(h2, pk.data_ptr() + b * BATCH * 4, pv.data_ptr() + b * BATCH * 8,
+                              BATCH, N.KD_CLOCK_COUNT, 0.0, 0)
+        e2e_t = []
+        for i in range(args.steps):
+            b = (args.warmup + i) % nb
+            flush.fill_(i & 0xFF)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc = L.kd_store_ingest(h2, pk.data_ptr() + b * BATCH * 4, pv.data_ptr() + b * BATCH * 8,
+                                   BATCH, N.KD_CLOCK_COUNT, 0.0, 0)
+            e2e_t.append(time.perf_counter() - t0)
+            if rc:
+                raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+        e2e = {"value": args.steps * BATCH / sum(e2e_t), "unit": "samples/s",
+               "h2d_bytes_per_step": 12 * BATCH, "d2h_bytes_per_step": 16,
+               "timing": "host wall clock around kd_store_ingest (pinned host inputs)"}
+        del store2
+
+    # Plain per-digest form: one digest per call, no graph (one batch).
+    plain = None
+    if not args.no_plain and rank == 0 and world == 1:
+        b = 0
+        kb = keys[b * BATCH:(b + 1) * BATCH]
+        vb = vals[b * BATCH:(b + 1) * BATCH]
+        order = np.argsort(kb, kind="stable")
+        ks = kb[order]
+        vs = np.ascontiguousarray(vb[order])
+        bounds = np.flatnonzero(np.diff(ks)) + 1
+        starts = np.concatenate([[0], bounds])
+        ends = np.concatenate([bounds, [len(ks)]])
+        d_vs = torch.from_numpy(vs).to(dev)
+        d_ks = torch.from_numpy(np.ascontiguousarray(ks)).to(dev)
+        store3 = kd.GroupedTDigest(NUM_KEYS, COMPRESSION, scale=kd.K3, session=sess)
+        h3 = store3._store._h
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        done = 0
+        for s_, e_ in zip(starts, ends):
+            rc = L.kd_store_ingest(h3, d_ks.data_ptr() + int(s_) * 4, d_vs.data_ptr() + int(s_) * 8,
+                                   int(e_ - s_), N.KD_CLOCK_COUNT, 0.0, N.KD_PTR_DEVICE)
+            if rc:
+                raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+            done += int(e_ - s_)
+            if time.perf_counter() - t0 > args.plain_seconds:
+                break
+        dt = time.perf_counter() - t0
+        plain = {"value": done / dt, "unit": "samples/s", "digests": int(np.searchsorted(ends, done, side="right")),
+                 "sample": f"batch 0, one key per call in key order, {done} samples in {dt:.1f} s"}
+        del store3
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, done, t, _ = cpu_ingest_rate(keys, vals, threads)
+        cpu = {"value": v, "unit": "samples/s", "cores": threads, "kind": "port",
+               "sample": f"first {done} batches of 2^22 pairs ({t:.1f} s, C oracle P-path, key-partitioned threads)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded numpy, host-generated, copied to HBM once)",
+        "config": {"workload": WORKLOAD, "keys": NUM_KEYS, "batch": BATCH, "total": TOTAL,
+                   "scale": "K3", "compression": COMPRESSION, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed (256 MiB write) between timed steps; each step reads a fresh 48 MiB slice"},
+        "queries_per_s": qps,
+        "step_roofline": {"compulsory_bytes": int(comp_bytes), "achieved": round(step_gbs, 1),
+                          "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                          "frac": round(step_gbs / peaks["hbm_gbs"], 4)},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "plain_form": plain,
+        "e2e": e2e,
+        "gpu_launches": st["launches"],
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    global TOTAL
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=29)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--plain-seconds", type=float, default=30.0)
+    ap.add_argument("--total", type=int, default=TOTAL,
+                    help="stream length (samples); smaller values are for profiling only")
+    args = ap.parse_args()
+    TOTAL = args.total
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    if not os.path.exists(os.path.join(ROOT, "kdigest_gb300", "libkdigest_gb300.so")):
+        from kdigest_gb300 import build as kb
+
+        kb.build()
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

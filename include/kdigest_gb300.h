@@ -54,7 +54,8 @@ extern "C" {
 
 /* Session options (kd_session_set_option). */
 #define KD_OPT_FORCE_EXACT_K 1 /* evaluate every bucket id in FP64 (no FP32 filter) */
-#define KD_OPT_MAX_LEVELS 2    /* levels of the tile hierarchy run per ingest (default 8) */
+#define KD_OPT_MAX_LEVELS 2    /* cap on tile-hierarchy levels per ingest (default 32) */
+#define KD_OPT_STAGE_TIMING 3  /* record CUDA events between ingest stages */
 
 typedef struct kd_session kd_session;
 typedef struct kd_store kd_store;
@@ -71,6 +72,13 @@ KD_API int kd_session_sync(kd_session* s);
 KD_API int kd_session_set_option(kd_session* s, int option, int value);
 /* The CUDA stream (cudaStream_t) all work of this session is ordered on. */
 KD_API void* kd_session_stream(kd_session* s);
+/* Accumulated per-stage device milliseconds of ingests (prep, sort, plan, level0,
+ * levels, commit; recorded when KD_OPT_STAGE_TIMING is on), kernels launched and
+ * ingests run since the last reset.  Returns the number of stages.  No reference
+ * counterpart (the reference times with perf_counter_ns, bench/bench_gpu.mojo:72). */
+KD_API int kd_session_stats(kd_session* s, double* stage_ms, int cap, int64_t* launches,
+                            int64_t* ingests);
+KD_API void kd_session_reset_stats(kd_session* s);
 
 /* gpu_compress_batch[S] (gpu/add_batch.mojo:629-663): P-path compress of an
  * arbitrary (mean, weight) set -> mean-sorted centroids.  out arrays hold cap
@@ -120,6 +128,9 @@ KD_API int kd_store_from_bytes(kd_store* st, uint32_t key, const uint8_t* buf, i
 
 KD_API int kd_store_stats(kd_store* st, int64_t* num_keys, int64_t* total_centroids,
                           size_t* device_bytes);
+/* Centroid count of every key (num_keys int32), e.g. GroupedTDigest.centroid_count
+ * for all keys at once (grouped.mojo:182-185). */
+KD_API int kd_store_counts(kd_store* st, int32_t* out, int flags);
 
 #ifdef __cplusplus
 }

@@ -17,14 +17,17 @@ KD_OK, KD_EINVAL, KD_EEMPTY, KD_ERANGE, KD_ECONVERGE, KD_ENOMEM, KD_ECUDA, KD_ET
 KD_K0, KD_K1, KD_K2, KD_K3 = 0, 1, 2, 3
 KD_CLOCK_COUNT, KD_CLOCK_TIME = 0, 1
 KD_PTR_DEVICE = 1
-KD_OPT_FORCE_EXACT_K, KD_OPT_MAX_LEVELS = 1, 2
+KD_OPT_FORCE_EXACT_K, KD_OPT_MAX_LEVELS, KD_OPT_STAGE_TIMING = 1, 2, 3
+STAGES = ("prep", "sort", "plan", "level0", "levels", "commit")
 
 EXPORTED = (
     "kd_version", "kd_status_string", "kd_session_create", "kd_session_destroy",
     "kd_last_error", "kd_session_sync", "kd_session_set_option", "kd_session_stream",
+    "kd_session_stats", "kd_session_reset_stats",
     "kd_compress", "kd_store_create", "kd_store_destroy", "kd_store_ingest",
     "kd_store_quantile", "kd_store_cdf", "kd_store_merge", "kd_store_get_digest",
     "kd_store_set_digest", "kd_store_to_bytes", "kd_store_from_bytes", "kd_store_stats",
+    "kd_store_counts",
 )
 
 _P = ctypes.c_void_p
@@ -65,6 +68,8 @@ def load(path: str = LIB_PATH):
     L.kd_session_set_option.argtypes = [_P, ctypes.c_int, ctypes.c_int]
     L.kd_session_stream.restype = _P
     L.kd_session_stream.argtypes = [_P]
+    L.kd_session_stats.argtypes = [_P, _P, ctypes.c_int, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]
+    L.kd_session_reset_stats.argtypes = [_P]
     L.kd_compress.argtypes = [_P, ctypes.c_int, _D, _P, _P, _I64, ctypes.c_int, _P, _P, _I64,
                               ctypes.POINTER(_I64)]
     L.kd_store_create.argtypes = [_P, _I64, ctypes.c_int, _D, _D, ctypes.POINTER(_P)]
@@ -77,6 +82,7 @@ def load(path: str = LIB_PATH):
     L.kd_store_set_digest.argtypes = [_P, ctypes.c_uint32, _P, _P, _P, _I64]
     L.kd_store_to_bytes.argtypes = [_P, ctypes.c_uint32, _P, _I64, ctypes.POINTER(_I64)]
     L.kd_store_from_bytes.argtypes = [_P, ctypes.c_uint32, _P, _I64]
+    L.kd_store_counts.argtypes = [_P, _P, ctypes.c_int]
     L.kd_store_stats.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                  ctypes.POINTER(ctypes.c_size_t)]
     _lib = L

@@ -62,11 +62,12 @@ static void dfree(KdSession* s, void* p, size_t bytes) {
 }
 
 void kd_ws_free(KdWorkspace& w) {
-  void* ptrs[] = {w.k64[0], w.k64[1], w.key[0], w.key[1], w.idx[0], w.idx[1], w.hist, w.partials,
-                  w.tkey, w.tstart, w.tm, w.tprior, w.tbuf, w.tsf, w.tpscale, w.ttiles,
-                  w.ttile_off, w.tinter_off, w.st_clock, w.st_ls, w.st_min, w.st_max, w.st_count,
-                  w.lv_storage, w.scr_m[0], w.scr_m[1], w.scr_w[0], w.scr_w[1], w.tcount[0],
-                  w.tcount[1], w.doff[0], w.doff[1], w.totals, w.err};
+  void* ptrs[] = {w.k64[0], w.k64[1], w.key[0], w.key[1], w.idx[0], w.idx[1], w.ghist,
+                  w.rs_state, w.rs_ticket, w.partials,
+                  w.tkey, w.tstart, w.tm, w.tprior, w.tbuf, w.tsf, w.tpscale, w.tmap,
+                  w.st_clock, w.st_ls, w.st_min, w.st_max, w.st_count, w.lv_storage,
+                  w.work[0], w.work[1], w.work[2], w.work[3], w.dx[0], w.dx[1], w.dw[0], w.dw[1], w.scr_m, w.scr_w,
+                  w.tcount, w.doff, w.needs, w.totals, w.err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (w.h_err) cudaFreeHost(w.h_err);
@@ -80,29 +81,43 @@ void kd_ws_free(KdWorkspace& w) {
   w.d_in_bytes = d_in_bytes;
 }
 
-static size_t ws_bytes(long long n, long long keys, long long inter, long long partials) {
+static size_t ws_bytes(long long n, long long keys, long long inter, long long work,
+                       long long merged, long long tmap, long long partials) {
   size_t b = 0;
   b += (size_t)n * (8 + 8 + 4 + 4 + 4 + 4);
-  b += (size_t)kd_rs_hist_entries(n) * 4;
+  b += (size_t)kd_rs_blocks(n) * 256 * 8 + KD_RS_MAXPASS * 256 * 4 + 8;
   b += (size_t)partials * sizeof(int4);
-  b += (size_t)keys * (4 * 8 + 8 * 6 + 1) + (size_t)keys * 7 * 4 * 2;
-  b += (size_t)inter * (KD_TILE * 16 * 2 + 16);
+  b += (size_t)keys * (4 * 4 + 1 + 8 * 6) + (size_t)keys * 8 * 4 * 2;
+  b += (size_t)tmap * 4;
+  b += (size_t)work * 8 * 4;
+  b += (size_t)merged * 16 * 2;
+  b += (size_t)inter * (KD_TILE * 16 + 8);
   return b;
 }
 
-int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter) {
+int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, long long work,
+                  long long merged, long long tmap) {
   KdWorkspace& w = s->ws;
-  if (n <= w.cap_n && keys <= w.cap_keys && inter <= w.cap_inter && w.err) return KD_OK;
-  long long nn = std::max(n, w.cap_n), kk = std::max(keys, w.cap_keys), ii = std::max(inter, w.cap_inter);
+  if (w.err && n <= w.cap_n && keys <= w.cap_keys && inter <= w.cap_inter && work <= w.cap_work &&
+      merged <= w.cap_merged && tmap <= w.cap_tmap)
+    return KD_OK;
+  long long nn = std::max(n, w.cap_n), kk = std::max(keys, w.cap_keys);
+  long long ii = std::max(inter, w.cap_inter), ww = std::max(work, w.cap_work);
+  long long mm = std::max(merged, w.cap_merged), tt = std::max(tmap, w.cap_tmap);
   if (nn > w.cap_n && w.cap_n > 0) nn = std::max(nn, std::min<long long>(2 * w.cap_n, (1LL << 31) - 1));
   nn = std::max<long long>(nn, 4096);
   kk = std::max<long long>(kk, 64);
   ii = std::max<long long>(ii, 64);
-  size_t old_bytes = w.err ? ws_bytes(w.cap_n, w.cap_keys, w.cap_inter, w.cap_partials) : 0;
+  ww = std::max<long long>(ww, 128);
+  mm = std::max<long long>(mm, 8192);
+  tt = std::max<long long>(tt, 1);
+  size_t old_bytes = w.err ? ws_bytes(w.cap_n, w.cap_keys, w.cap_inter, w.cap_work, w.cap_merged,
+                                      w.cap_tmap, w.cap_partials)
+                           : 0;
   kd_ws_free(w);
   s->mem_used -= std::min(s->mem_used, old_bytes);
-  long long parts = kd_scan_partials_needed(std::max({nn, kd_rs_hist_entries(nn), kk})) + 4;
-  size_t need = ws_bytes(nn, kk, ii, parts);
+  long long parts = kd_scan_partials_needed(std::max(nn, kk)) + 4;
+  size_t need = ws_bytes(nn, kk, ii, ww, mm, tt, parts);
   if (s->mem_budget && s->mem_used + need > s->mem_budget) {
     char buf[200];
     snprintf(buf, sizeof buf, "device-memory budget exceeded by the ingest workspace (%zu bytes)", need);
@@ -113,6 +128,7 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter) {
     cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
     if (e != cudaSuccess) {
       cudaGetLastError();
+      *p = nullptr;
       return false;
     }
     return true;
@@ -122,8 +138,19 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter) {
     ok &= A((void**)&w.k64[i], sizeof(uint64_t) * nn);
     ok &= A((void**)&w.key[i], sizeof(uint32_t) * nn);
     ok &= A((void**)&w.idx[i], sizeof(uint32_t) * nn);
+    ok &= A((void**)&w.work[2 * i], sizeof(int2) * ww);
+    ok &= A((void**)&w.work[2 * i + 1], sizeof(int2) * ww);
+    ok &= A((void**)&w.dx[i], sizeof(double) * mm);
+    ok &= A((void**)&w.dw[i], sizeof(double) * mm);
   }
-  ok &= A((void**)&w.hist, sizeof(int) * kd_rs_hist_entries(nn));
+  ok &= A((void**)&w.ghist, sizeof(unsigned) * KD_RS_MAXPASS * 256);
+  ok &= A((void**)&w.rs_state, sizeof(unsigned long long) * 256 * (size_t)kd_rs_blocks(nn));
+  ok &= A((void**)&w.rs_ticket, sizeof(unsigned long long));
+  if (ok) {
+    cudaMemset(w.rs_state, 0, sizeof(unsigned long long) * 256 * (size_t)kd_rs_blocks(nn));
+    w.cap_rs_tiles = kd_rs_blocks(nn);
+    w.rs_epoch = 0;
+  }
   ok &= A((void**)&w.partials, sizeof(int4) * parts);
   ok &= A((void**)&w.tkey, sizeof(uint32_t) * kk);
   ok &= A((void**)&w.tstart, sizeof(int) * kk);
@@ -132,21 +159,18 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter) {
   ok &= A((void**)&w.tbuf, kk);
   ok &= A((void**)&w.tsf, sizeof(double) * kk);
   ok &= A((void**)&w.tpscale, sizeof(double) * kk);
-  ok &= A((void**)&w.ttiles, sizeof(int) * kk);
-  ok &= A((void**)&w.ttile_off, sizeof(int) * kk);
-  ok &= A((void**)&w.tinter_off, sizeof(int) * kk);
+  ok &= A((void**)&w.tmap, sizeof(uint32_t) * tt);
   ok &= A((void**)&w.st_clock, sizeof(double) * kk);
   ok &= A((void**)&w.st_ls, sizeof(double) * kk);
   ok &= A((void**)&w.st_min, sizeof(double) * kk);
   ok &= A((void**)&w.st_max, sizeof(double) * kk);
   ok &= A((void**)&w.st_count, sizeof(int) * kk);
-  ok &= A((void**)&w.lv_storage, sizeof(int) * (kk * 7 * 2 + 64));
-  for (int i = 0; i < 2; ++i) {
-    ok &= A((void**)&w.scr_m[i], sizeof(double) * KD_TILE * ii);
-    ok &= A((void**)&w.scr_w[i], sizeof(double) * KD_TILE * ii);
-    ok &= A((void**)&w.tcount[i], sizeof(int) * ii);
-    ok &= A((void**)&w.doff[i], sizeof(int) * ii);
-  }
+  ok &= A((void**)&w.lv_storage, sizeof(int) * (kk * 8 * 2 + 64));
+  ok &= A((void**)&w.scr_m, sizeof(double) * KD_TILE * ii);
+  ok &= A((void**)&w.scr_w, sizeof(double) * KD_TILE * ii);
+  ok &= A((void**)&w.tcount, sizeof(int) * ii);
+  ok &= A((void**)&w.doff, sizeof(int) * (ii + 1));
+  ok &= A((void**)&w.needs, sizeof(int) * 4);
   ok &= A((void**)&w.totals, sizeof(int4) * 8);
   ok &= A((void**)&w.err, sizeof(KdErrHost));
   ok &= cudaHostAlloc((void**)&w.h_err, sizeof(KdErrHost), cudaHostAllocDefault) == cudaSuccess;
@@ -163,17 +187,25 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter) {
     L.src_tiles = lvp; lvp += kk;
     L.mprev = lvp; lvp += kk;
     L.m = lvp; lvp += kk;
-    L.tile_off = lvp; lvp += kk;
+    L.base = lvp; lvp += kk;
     L.inter_off = lvp; lvp += kk;
+    lvp += kk;  // spare
+    L.work_l = w.work[2 * i];
+    L.work_s = w.work[2 * i + 1];
   }
   for (int i = 0; i < 2; ++i) {
     w.lv[i].A = lvp++;
-    w.lv[i].T = lvp++;
+    w.lv[i].Tl = lvp++;
+    w.lv[i].Ts = lvp++;
     w.lv[i].I = lvp++;
+    w.lv[i].M = lvp++;
   }
   w.cap_n = nn;
   w.cap_keys = kk;
   w.cap_inter = ii;
+  w.cap_work = ww;
+  w.cap_merged = mm;
+  w.cap_tmap = tt;
   w.cap_partials = parts;
   s->mem_used += need;
   return KD_OK;
@@ -334,6 +366,8 @@ KD_API void kd_session_destroy(kd_session* h) {
   if (s->ws.d_in) cudaFree(s->ws.d_in);
   s->ws.d_in = nullptr;
   kd_ws_free(s->ws);
+  for (int i = 0; i <= KD_NSTAGES; ++i)
+    if (s->stats.ev[i]) cudaEventDestroy(s->stats.ev[i]);
   cudaStreamDestroy(s->stream);
   delete h;
 }
@@ -349,10 +383,35 @@ KD_API int kd_session_sync(kd_session* h) {
 
 KD_API void* kd_session_stream(kd_session* h) { return h ? (void*)h->s.stream : nullptr; }
 
+KD_API int kd_session_stats(kd_session* h, double* stage_ms, int cap, int64_t* launches,
+                            int64_t* ingests) {
+  if (!h) return KD_EINVAL;
+  const KdStageStats& t = h->s.stats;
+  for (int i = 0; i < cap && i < KD_NSTAGES; ++i) stage_ms[i] = t.ms[i];
+  if (launches) *launches = t.launches;
+  if (ingests) *ingests = t.ingests;
+  return KD_NSTAGES;
+}
+
+KD_API void kd_session_reset_stats(kd_session* h) {
+  if (!h) return;
+  KdStageStats& t = h->s.stats;
+  for (int i = 0; i < KD_NSTAGES; ++i) t.ms[i] = 0.0;
+  t.launches = 0;
+  t.ingests = 0;
+}
+
 KD_API int kd_session_set_option(kd_session* h, int option, int value) {
   if (!h) return KD_EINVAL;
   KdSession* s = &h->s;
   if (option == KD_OPT_FORCE_EXACT_K) s->force_exact = value ? 1 : 0;
+  else if (option == KD_OPT_STAGE_TIMING) {
+    if (value && !s->stats.enabled) {
+      for (int i = 0; i <= KD_NSTAGES; ++i)
+        if (!s->stats.ev[i]) KD_CK(cudaEventCreate(&s->stats.ev[i]));
+    }
+    s->stats.enabled = value ? 1 : 0;
+  }
   else if (option == KD_OPT_MAX_LEVELS) {
     if (value < 1 || value > 64) return fail(s, KD_EINVAL, "max levels must be in [1, 64]");
     s->max_levels = value;
@@ -609,6 +668,18 @@ KD_API int kd_store_stats(kd_store* h, int64_t* num_keys, int64_t* total_centroi
     for (int v : c) t += v;
     *total_centroids = t;
   }
+  return KD_OK;
+}
+
+KD_API int kd_store_counts(kd_store* h, int32_t* out, int flags) {
+  if (!h || !out) return KD_EINVAL;
+  KdStore* st = &h->st;
+  KdSession* s = st->sess;
+  cudaSetDevice(s->device);
+  KD_CK(cudaMemcpyAsync(out, st->d.count, (size_t)st->d.K * 4,
+                        (flags & KD_PTR_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                        s->stream));
+  KD_CK(cudaStreamSynchronize(s->stream));
   return KD_OK;
 }
 

@@ -37,19 +37,25 @@ struct KdErrHost {
   long long index;
 };
 
-// Per-level plan of the P-path hierarchy (levels >= 1 hold only the keys whose
-// input exceeded one tile at the previous level).
+// Per-level plan of the P-path hierarchy.  Level 0 holds every touched key;
+// level L >= 1 holds the keys whose input exceeded one tile at level L-1.  The
+// input of a level is a dense array (means, weights): key a owns
+// [base[a], base[a] + m[a]); its tiles are listed in `work` as (a, tile).
 struct KdLevelDev {
-  int* A;          // number of active keys (device scalar)
-  int* j;          // touched ordinal
-  int* src_base;   // first intermediate tile (previous level) holding the input
+  int* A;          // active keys (device scalar)
+  int* j;          // touched ordinal of active key a
+  int* src_base;   // first intermediate tile of the previous level holding its input
   int* src_tiles;  // number of those tiles
   int* mprev;      // input size at the previous level
   int* m;          // input size at this level
-  int* tile_off;   // exclusive prefix of tiles over active keys
-  int* inter_off;  // exclusive prefix of intermediate tiles
-  int* T;          // total tiles (device scalar)
-  int* I;          // total intermediate tiles (device scalar)
+  int* base;       // offset of its input in the dense array
+  int* inter_off;  // first intermediate output tile (when not final)
+  int2* work_l;    // (a, tile) of tiles above KD_SERIAL_TILE_MAX elements (warp per tile)
+  int2* work_s;    // (a, tile) of smaller tiles (lane per tile)
+  int* Tl;         // large work tiles (device scalar)
+  int* Ts;         // small work tiles (device scalar)
+  int* I;          // intermediate tiles (device scalar)
+  int* M;          // dense elements (device scalar)
 };
 
 struct KdWorkspace {
@@ -60,7 +66,11 @@ struct KdWorkspace {
   uint64_t* k64[2] = {nullptr, nullptr};
   uint32_t* key[2] = {nullptr, nullptr};
   uint32_t* idx[2] = {nullptr, nullptr};
-  int* hist = nullptr;
+  unsigned* ghist = nullptr;             // digit counts of every radix pass
+  unsigned long long* rs_state = nullptr; // look-back words, 256 per sort tile
+  unsigned long long* rs_ticket = nullptr;
+  long long cap_rs_tiles = 0;
+  unsigned rs_epoch = 0;
   int4* partials = nullptr;
   long long cap_partials = 0;
   // touched keys
@@ -71,9 +81,8 @@ struct KdWorkspace {
   unsigned char* tbuf = nullptr;
   double* tsf = nullptr;
   double* tpscale = nullptr;
-  int* ttiles = nullptr;
-  int* ttile_off = nullptr;
-  int* tinter_off = nullptr;
+  uint32_t* tmap = nullptr;  // key -> touched ordinal (valid for touched keys only)
+  long long cap_tmap = 0;
   double* st_clock = nullptr;
   double* st_ls = nullptr;
   double* st_min = nullptr;
@@ -86,11 +95,18 @@ struct KdWorkspace {
   // levels
   KdLevelDev lv[2];
   int* lv_storage = nullptr;
-  // intermediate tiles (ping-pong)
-  double* scr_m[2] = {nullptr, nullptr};
-  double* scr_w[2] = {nullptr, nullptr};
-  int* tcount[2] = {nullptr, nullptr};
-  int* doff[2] = {nullptr, nullptr};
+  long long cap_work = 0;      // work tiles per level
+  long long cap_merged = 0;    // dense elements per level
+  int2* work[4] = {nullptr, nullptr, nullptr, nullptr};  // (large, small) x 2 levels
+  double* dx[2] = {nullptr, nullptr};  // dense level inputs (ping-pong)
+  double* dw[2] = {nullptr, nullptr};
+  // intermediate tile outputs (one set: a level's outputs are compacted into
+  // the next dense input before the next level writes again)
+  double* scr_m = nullptr;
+  double* scr_w = nullptr;
+  int* tcount = nullptr;
+  int* doff = nullptr;
+  int* needs = nullptr;  // device: required (work, merged, inter) capacities
   // scalars: U, T0, I0, A1 ... (int4 totals)
   int4* totals = nullptr;
   KdErrHost* err = nullptr;   // device
@@ -103,6 +119,16 @@ struct KdWorkspace {
   size_t d_in_bytes = 0;
 };
 
+// Per-stage device timing of ingests (CUDA events on the session stream).
+#define KD_NSTAGES 6  // prep, sort, plan, level0, levels, commit
+struct KdStageStats {
+  int enabled = 0;
+  cudaEvent_t ev[KD_NSTAGES + 1] = {};
+  double ms[KD_NSTAGES] = {};
+  long long launches = 0;  // kernels launched by the engine
+  long long ingests = 0;
+};
+
 struct KdSession {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -110,9 +136,10 @@ struct KdSession {
   size_t mem_used = 0;
   int num_sms = 0;
   int force_exact = 0;
-  int max_levels = 8;
+  int max_levels = 32;
   std::string last_error;
   KdWorkspace ws;
+  KdStageStats stats;
   struct KdStore* scratch_store = nullptr;  // 1-key store for stateless compress
 };
 
@@ -120,6 +147,7 @@ struct KdStore {
   KdSession* sess = nullptr;
   KdStoreDev d{};
   size_t bytes = 0;
+  int levels_hint = 3;  // hierarchy levels >= 1 the last ingest needed
 };
 
 // Pipeline entry points (kd_pipeline.cu).  All work is enqueued on sess->stream.
@@ -136,6 +164,7 @@ int kd_pipeline_merge(KdSession* s, KdStore* dst, KdStore* src, const long long*
                       const uint32_t* h_parts, long long ngroups);
 int kd_store_alloc(KdSession* s, KdStore* st);
 void kd_store_free(KdStore* st);
-int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter);
+int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, long long work,
+                  long long merged, long long tmap);
 void kd_ws_free(KdWorkspace& ws);
 int kd_cuda_fail(KdSession* s, cudaError_t e, const char* what);

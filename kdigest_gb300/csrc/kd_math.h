@@ -59,6 +59,10 @@
 #define KD_SCALE_K2 2
 #define KD_SCALE_K3 3
 
+/* Tiles of at most this many elements sum their weights serially, left to
+ * right; larger tiles use the 32-lane chunked order (one warp per tile). */
+#define KD_SERIAL_TILE_MAX 128
+
 /* Clamp distance from the q = 0 / 1 singularities (scale.mojo:32-47, Float64). */
 #define KD_Q_EPS 1e-15
 

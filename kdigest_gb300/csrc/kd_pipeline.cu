@@ -26,6 +26,7 @@
 #include "kd_sort.cuh"
 
 #define KD_ERANGE_SCRATCH 100  // internal: intermediate scratch too small (index = needed)
+#define KD_EMORE_LEVELS 101    // internal: keys still above one tile after the levels run
 
 __device__ __forceinline__ size_t slot_base(long long K, int buf, long long key) {
   return ((size_t)buf * (size_t)K + (size_t)key) * KD_TILE;
@@ -44,166 +45,300 @@ __device__ __forceinline__ double canon(double v) { return v == 0.0 ? 0.0 : v; }
 // ---------------------------------------------------------------------------
 // Warp tile compress (canonical association order; see oracle/kd_oracle.c)
 // ---------------------------------------------------------------------------
-struct WarpTile {
-  double x[KD_SMEM_SLOTS];
-  double w[KD_SMEM_SLOTS];
-  double L[KD_SMEM_SLOTS];  // in-chunk inclusive prefix of w
-  unsigned char f[KD_SMEM_SLOTS];  // bit0 head, bit1 end
+// Shared-memory staging of one tile for one warp.  CAP is the largest tile it
+// holds: KD_SERIAL_TILE_MAX (serial canonical order, one chunk) or KD_TILE
+// (32 lane chunks of E = ceil(n/32) elements).  Element p of the tile lives at
+// slot (p / E) * SE + p % E with SE = E | 1, which keeps the 64-bit accesses of
+// the 32 lanes on distinct banks.
+template <int CAP>
+struct WarpTileT {
+  static constexpr int SLOTS = CAP == KD_TILE ? KD_SMEM_SLOTS : CAP + 1;
+  double x[SLOTS];
+  double w[SLOTS];
+  // in-chunk inclusive prefix of w (double, or int64 bits in the integral path);
+  // after the segment pass: the weight sum of each segment at its end element
+  double L[SLOTS];
+  double P[32];                  // exclusive prefix of the chunk totals (bits)
+  unsigned char hf[SLOTS];       // head flags
+  unsigned char ef[SLOTS];       // end flags
+  unsigned short headpos[CAP];   // tile position of the first element of segment s
+  unsigned short endpos[CAP];    // tile position of the last element of segment s
 };
+typedef WarpTileT<KD_TILE> WarpTile;
+typedef WarpTileT<KD_SERIAL_TILE_MAX> WarpTileSmall;
 
-__device__ __forceinline__ void emit_centroid(double* om, double* ow, int slot, double sw,
-                                              double swx, double lo_v, double hi_v) {
-  double mean = sw > 0.0 ? KD_DIV(swx, sw) : 0.0;
-  mean = mean < lo_v ? lo_v : mean;
-  mean = mean > hi_v ? hi_v : mean;
-  om[slot] = mean;
-  ow[slot] = sw;
+// Integral weight in [1, 2^42): a tile of such weights has every partial sum
+// exact in FP64 (total < 2^52), so int64 arithmetic reproduces the canonical
+// FP64 sums bit for bit.
+__device__ __forceinline__ bool kd_is_small_int(double w) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+  if (b >> 63) return false;
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  if (e < 0 || e > 41) return false;
+  return (b & ((1ull << (52 - e)) - 1ull)) == 0;
+}
+__device__ __forceinline__ long long kd_small_int(double w) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  return (long long)(((b & 0xfffffffffffffull) | (1ull << 52)) >> (52 - e));
 }
 
-// Compresses the n (<= 1024) staged elements of `t`; lane c owns elements
-// [c*E, c*E+E) stored at t.*[c*SE + j].  The loader has filled x, w and L.
-// Returns the number of centroids written to om/ow[0..).
-__device__ int warp_compress(WarpTile& t, int n, int scale, double compression, int force_exact,
-                             double* __restrict__ om, double* __restrict__ ow) {
+template <bool kInt>
+struct TileAcc;
+template <>
+struct TileAcc<false> {
+  typedef double T;
+  __device__ static T from_w(double w) { return w; }
+  __device__ static T add(T a, T b) { return KD_ADD(a, b); }
+  __device__ static T sub(T a, T b) { return KD_SUB(a, b); }
+  __device__ static T shfl_up(T v, int o) { return __shfl_up_sync(0xffffffffu, v, o); }
+  __device__ static T shfl(T v, int l) { return __shfl_sync(0xffffffffu, v, l); }
+  __device__ static double to_d(T v) { return v; }
+  __device__ static float to_f(T v) { return kd_d2f_trunc(v); }
+  __device__ static bool is_zero(T v) { return ((unsigned long long)__double_as_longlong(v) << 1) == 0; }
+  __device__ static double store(T v) { return v; }
+  __device__ static T load(double v) { return v; }
+};
+template <>
+struct TileAcc<true> {
+  typedef long long T;
+  __device__ static T from_w(double w) { return kd_small_int(w); }
+  __device__ static T add(T a, T b) { return a + b; }
+  __device__ static T sub(T a, T b) { return a - b; }
+  __device__ static T shfl_up(T v, int o) { return __shfl_up_sync(0xffffffffu, v, o); }
+  __device__ static T shfl(T v, int l) { return __shfl_sync(0xffffffffu, v, l); }
+  __device__ static double to_d(T v) { return (double)v; }
+  __device__ static float to_f(T v) { return kd_i2f_trunc(v); }
+  __device__ static bool is_zero(T v) { return v == 0; }
+  __device__ static double store(T v) { return __longlong_as_double(v); }
+  __device__ static T load(double v) { return __double_as_longlong(v); }
+};
+
+__device__ __forceinline__ int tile_slot(int p, int E, int SE, unsigned inv) {
+  const int c = (int)(((unsigned)p * inv) >> 16);  // exact p / E for p < 1024, E <= 1024
+  return c * SE + (p - c * E);
+}
+// Chunk length of a tile: the whole tile (serial order) up to
+// KD_SERIAL_TILE_MAX elements, else ceil(n / 32).
+__device__ __forceinline__ int tile_chunk(int n) {
+  return n <= KD_SERIAL_TILE_MAX ? n : (n + 31) >> 5;
+}
+__device__ __forceinline__ unsigned tile_inv(int E) {
+  return (65536u + (unsigned)E - 1u) / (unsigned)E;
+}
+
+// Compresses the n staged elements of `t` (the loader has filled x and w in
+// the slot layout of tile_chunk(n)).  Writes the centroids to om/ow[0..) and
+// returns their number.  Canonical sums: serial within each chunk, Kogge-Stone
+// over the 32 chunk totals for the prefix; for segment sums, serial within a
+// chunk and a segmented Kogge-Stone carry across chunks.  With one chunk
+// (n <= KD_SERIAL_TILE_MAX) both reduce to plain serial sums.
+template <bool kInt, int CAP>
+__device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compression,
+                             int force_exact, double* __restrict__ om, double* __restrict__ ow) {
+  typedef TileAcc<kInt> A;
+  typedef typename A::T T;
   const int lane = threadIdx.x & 31;
-  const int E = (n + 31) >> 5;
+  const int E = tile_chunk(n);
   const int SE = E | 1;
+  const unsigned inv = tile_inv(E);
   const int lo = lane * E;
   const int cnt = max(0, min(E, n - lo));
   const int sb = lane * SE;
 
-  // Chunk totals -> Kogge-Stone over lanes -> exclusive lane prefix P.
-  double S = cnt > 0 ? t.L[sb + cnt - 1] : 0.0;
-  double I = S;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    double v = shfl_up_d(I, o);
-    if (lane >= o) I = KD_ADD(I, v);
+  // 1. In-chunk inclusive prefix of the weights, serial per lane.
+  T acc = 0;
+  for (int j = 0; j < cnt; ++j) {
+    const T wv = A::from_w(t.w[sb + j]);
+    acc = j == 0 ? wv : A::add(acc, wv);
+    t.L[sb + j] = A::store(acc);
   }
-  double P = shfl_up_d(I, 1);
-  const int cl = (n - 1) / E;  // lane holding the last element
-  double last_cum = 0.0;
-  if (cnt > 0) last_cum = lane == 0 ? t.L[sb + cnt - 1] : KD_ADD(P, t.L[sb + cnt - 1]);
-  double tot = shfl_d(last_cum, cl);
-  if (!(tot > 0.0)) tot = 1.0;
-  const KFilterTile ft = kfilter_tile(scale, compression, tot);
+  // 2. Chunk totals -> Kogge-Stone over lanes -> exclusive chunk prefix.
+  T I = cnt > 0 ? acc : (T)0;
+  if (CAP > KD_SERIAL_TILE_MAX) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T v = A::shfl_up(I, o);
+      if (lane >= o) I = A::add(I, v);
+    }
+    t.P[lane] = A::store(A::shfl_up(I, 1));
+  }
+  const int cl = (n - 1) / E;  // chunk holding the last element
+  T last_cum = 0;
+  if (cnt > 0) last_cum = lane == 0 ? acc : A::add(A::load(t.P[lane]), acc);
+  T tot = A::shfl(last_cum, cl);
+  double totd = A::to_d(tot);
+  if (!(totd > 0.0)) {  // add_batch.mojo:98-100 (only reachable with non-integral weights)
+    totd = 1.0;
+    tot = (T)1;
+  }
+  __syncwarp();
+  const KFilterTile ft = kfilter_tile(scale, compression, kInt ? A::to_f(tot) : kd_d2f_trunc(totd));
 
-  // Bucket ids and head / end flags.
-  int32_t prev_id = 0, first_id = 0;
-  int nend = 0;
+  // 3. Bucket ids, 32 consecutive elements per round; heads compacted by ballot.
   double nrm64 = 0.0;
   bool have_nrm = false;
-  for (int j = 0; j < E; ++j) {
-    const bool act = j < cnt;
-    double cum = 0.0;
+  int32_t carry_id = 0;
+  int nheads = 0;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int r0 = 0; r0 < n; r0 += 32) {
+    const int p = r0 + lane;
+    const bool act = p < n;
+    T cum = 0;
     int32_t id = 0;
     bool ok = true;
+    int slot = 0;
     if (act) {
-      cum = lane == 0 ? t.L[sb + j] : KD_ADD(P, t.L[sb + j]);
-      ok = !force_exact && kfilter_id(scale, ft, cum, tot, &id);
+      const int c = (int)(((unsigned)p * inv) >> 16);
+      slot = c * SE + (p - c * E);
+      const T Lp = A::load(t.L[slot]);
+      cum = c == 0 ? Lp : A::add(A::load(t.P[c]), Lp);
+      const float q = A::to_f(cum) / ft.t32;
+      float r;
+      bool rz = false;
+      if (q > 0.25f) {
+        const T rem = A::sub(tot, cum);
+        rz = A::is_zero(rem);
+        r = A::to_f(rem) / ft.t32;
+      } else {
+        r = 1.f - q;
+      }
+      ok = !force_exact && kfilter_id(scale, ft, q, r, rz, &id);
     }
     const bool need = act && !ok;
     if (__any_sync(0xffffffffu, need)) {
       if (!have_nrm) {
-        nrm64 = kd_normalizer(scale, compression, tot);
+        nrm64 = kd_normalizer(scale, compression, totd);
         have_nrm = true;
       }
-      if (need) id = kd_bucket(scale, cum, tot, nrm64);
+      if (need) id = kd_bucket(scale, A::to_d(cum), totd, nrm64);
     }
-    if (act) {
-      unsigned char h = 0;
-      if (j > 0 && id != prev_id) {
-        h = 1;
-        t.f[sb + j - 1] |= 2;
-        ++nend;
-      }
-      t.f[sb + j] = h;
-      if (j == 0) first_id = id;
-      prev_id = id;
-    }
+    int32_t prev = __shfl_up_sync(0xffffffffu, id, 1);
+    if (lane == 0) prev = carry_id;
+    const bool head = act && (p == 0 || id != prev);
+    const unsigned hb = __ballot_sync(0xffffffffu, head);
+    if (head) t.headpos[nheads + __popc(hb & lt_mask)] = (unsigned short)p;
+    nheads += __popc(hb);
+    carry_id = __shfl_sync(0xffffffffu, id, 31);
   }
-  const int32_t left_last = __shfl_up_sync(0xffffffffu, prev_id, 1);
-  const int32_t right_first = __shfl_down_sync(0xffffffffu, first_id, 1);
-  if (cnt > 0) {
-    if (lane == 0 || first_id != left_last) t.f[sb] |= 1;
-    if (lo + cnt == n || right_first != prev_id) {
-      t.f[sb + cnt - 1] |= 2;
-      ++nend;
+  __syncwarp();
+  const int total_out = nheads;
+
+  // 4. Segment sums; every segment parks its sums at its end element
+  //    (L: weight, w: weight * value) and records its end position.
+  if (CAP <= KD_SERIAL_TILE_MAX || n <= KD_SERIAL_TILE_MAX) {
+    // One chunk: plain serial sums, one lane per segment.
+    for (int sI = lane; sI < total_out; sI += 32) {
+      const int h = t.headpos[sI];
+      const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
+      T aw = A::from_w(t.w[h]);
+      double awx = KD_MUL(t.w[h], t.x[h]);
+      for (int i = h + 1; i <= e; ++i) {
+        const double wi = t.w[i];
+        aw = A::add(aw, A::from_w(wi));
+        awx = KD_ADD(awx, KD_MUL(wi, t.x[i]));
+      }
+      t.endpos[sI] = (unsigned short)e;
+      t.L[e] = A::store(aw);
+      t.w[e] = awx;
+    }
+  } else {
+    // Lane chunks: flags from the head list, serial pieces per chunk, then a
+    // segmented Kogge-Stone carry of the trailing pieces across lanes.
+    for (int q = lane; q < n; q += 32) {
+      const int sl = tile_slot(q, E, SE, inv);
+      t.hf[sl] = 0;
+      t.ef[sl] = 0;
+    }
+    __syncwarp();
+    for (int sI = lane; sI < total_out; sI += 32) {
+      const int h = t.headpos[sI];
+      t.hf[tile_slot(h, E, SE, inv)] = 1;
+      const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
+      t.ef[tile_slot(e, E, SE, inv)] = 1;
+      t.endpos[sI] = (unsigned short)e;
+    }
+    __syncwarp();
+    // output slot of a segment = number of heads before it; a lane's first end
+    // closes the segment of the last head at or before the chunk start
+    T aw = 0;
+    double awx = 0.0;
+    bool head_seen = false;
+    bool pend = false;
+    T pend_w = 0;
+    double pend_wx = 0.0;
+    int pend_se = 0;
+    for (int j = 0; j < cnt; ++j) {
+      const double wi = t.w[sb + j], xi = t.x[sb + j];
+      const double wx = KD_MUL(wi, xi);
+      const T wv = A::from_w(wi);
+      const bool hd = t.hf[sb + j];
+      if (hd || j == 0) {
+        aw = wv;
+        awx = wx;
+      } else {
+        aw = A::add(aw, wv);
+        awx = KD_ADD(awx, wx);
+      }
+      if (hd) head_seen = true;
+      if (t.ef[sb + j]) {
+        if (head_seen) {
+          t.L[sb + j] = A::store(aw);
+          t.w[sb + j] = awx;
+        } else {
+          pend = true;
+          pend_w = aw;
+          pend_wx = awx;
+          pend_se = sb + j;
+        }
+      }
+    }
+    T Vw = aw;
+    double Vwx = awx;
+    int F = head_seen ? 1 : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T tw = A::shfl_up(Vw, o);
+      const double twx = shfl_up_d(Vwx, o);
+      const int tf = __shfl_up_sync(0xffffffffu, F, o);
+      if (lane >= o) {
+        if (!F) {
+          Vw = A::add(Vw, tw);
+          Vwx = KD_ADD(Vwx, twx);
+        }
+        F |= tf;
+      }
+    }
+    const T cw = A::shfl_up(Vw, 1);
+    const double cwx = shfl_up_d(Vwx, 1);
+    if (pend) {
+      t.L[pend_se] = A::store(A::add(cw, pend_w));
+      t.w[pend_se] = KD_ADD(cwx, pend_wx);
     }
   }
   __syncwarp();
 
-  // Output slots: exclusive prefix of segment ends over lanes.
-  int incl_e = nend;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int v = __shfl_up_sync(0xffffffffu, incl_e, o);
-    if (lane >= o) incl_e += v;
-  }
-  int slot = incl_e - nend;
-  const int total_out = __shfl_sync(0xffffffffu, incl_e, 31);
-
-  // Segment sums: serial pieces inside the chunk.
-  double aw = 0.0, awx = 0.0, head_x = 0.0;
-  bool head_seen = false;
-  int last_head = -1;
-  bool pend = false;
-  double pend_w = 0.0, pend_wx = 0.0, pend_x = 0.0;
-  int pend_slot = 0;
-  for (int j = 0; j < cnt; ++j) {
-    const unsigned char f = t.f[sb + j];
-    const double wi = t.w[sb + j], xi = t.x[sb + j];
-    const double wx = KD_MUL(wi, xi);
-    if ((f & 1) || j == 0) {
-      aw = wi;
-      awx = wx;
+  // 5. Centroids, 32 at a time: mean = sum(wx) / sum(w) clamped to the
+  //    segment's [first, last] value (add_batch.mojo:205-218).  A segment whose
+  //    first and last values are equal needs no division: the clamp yields it.
+  for (int sI = lane; sI < total_out; sI += 32) {
+    const int e = t.endpos[sI];
+    const int h = t.headpos[sI];
+    const int se = tile_slot(e, E, SE, inv), sh = tile_slot(h, E, SE, inv);
+    const double sw = A::to_d(A::load(t.L[se]));
+    const double swx = t.w[se];
+    const double lo_v = t.x[sh], hi_v = t.x[se];
+    double mean;
+    if (__double_as_longlong(lo_v) == __double_as_longlong(hi_v)) {
+      mean = lo_v;
     } else {
-      aw = KD_ADD(aw, wi);
-      awx = KD_ADD(awx, wx);
+      mean = __double_as_longlong(sw) > 0 ? KD_DIV(swx, sw) : 0.0;
+      const uint64_t km = kd_order_key(mean);
+      if (km < kd_order_key(lo_v)) mean = lo_v;
+      else if (km > kd_order_key(hi_v)) mean = hi_v;
     }
-    if (f & 1) {
-      head_seen = true;
-      head_x = xi;
-      last_head = lo + j;
-    }
-    if (f & 2) {
-      if (head_seen) {
-        emit_centroid(om, ow, slot, aw, awx, head_x, xi);
-      } else {
-        pend = true;
-        pend_w = aw;
-        pend_wx = awx;
-        pend_x = xi;
-        pend_slot = slot;
-      }
-      ++slot;
-    }
-  }
-  // Segmented Kogge-Stone of the trailing pieces carries sums across lanes.
-  double Vw = aw, Vwx = awx;
-  int F = head_seen ? 1 : 0;
-  int hp = last_head;  // inclusive max-scan of head positions
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    double tw = shfl_up_d(Vw, o), twx = shfl_up_d(Vwx, o);
-    int tf = __shfl_up_sync(0xffffffffu, F, o);
-    int th = __shfl_up_sync(0xffffffffu, hp, o);
-    if (lane >= o) {
-      if (!F) {
-        Vw = KD_ADD(Vw, tw);
-        Vwx = KD_ADD(Vwx, twx);
-      }
-      F |= tf;
-      hp = max(hp, th);
-    }
-  }
-  const double cw = shfl_up_d(Vw, 1), cwx = shfl_up_d(Vwx, 1);
-  const int hprev = __shfl_up_sync(0xffffffffu, hp, 1);
-  if (pend) {
-    const int hq = max(hprev, 0);
-    const int hl = hq / E;
-    const double hx = t.x[hl * SE + (hq - hl * E)];
-    emit_centroid(om, ow, pend_slot, KD_ADD(cw, pend_w), KD_ADD(cwx, pend_wx), hx, pend_x);
+    om[sI] = mean;
+    ow[sI] = sw;
   }
   __syncwarp();
   return total_out;
@@ -244,11 +379,15 @@ struct TouchedDst {
   const uint32_t* key;
   uint32_t* tkey;
   int* tstart;
+  uint32_t* tmap;
   long long cap;
+  long long K;
   __device__ void operator()(long long i, int4 excl, int4 v) const {
     if (v.x && excl.x < cap) {
-      tkey[excl.x] = key[i];
+      const uint32_t k = key[i];
+      tkey[excl.x] = k;
       tstart[excl.x] = (int)i;
+      if ((long long)k < K) tmap[k] = (uint32_t)excl.x;
     }
   }
 };
@@ -352,318 +491,421 @@ __global__ void k_prepare(PrepareArgs a) {
   a.st_max[j] = mx;
 }
 
+// Tiles of a key with m input elements: floor(m/1024) full tiles plus a partial
+// tile of r = m mod 1024 elements; only that partial tile can be small.
+struct TileSplit {
+  int small, large;
+};
+__device__ __forceinline__ TileSplit tile_split(int m) {
+  const int full = m / KD_TILE, r = m - full * KD_TILE;
+  TileSplit t;
+  t.small = (r > 0 && r <= KD_SERIAL_TILE_MAX) ? 1 : 0;
+  t.large = full + (r > KD_SERIAL_TILE_MAX ? 1 : 0);
+  return t;
+}
+__device__ __forceinline__ void write_work(const KdLevelDev& lv, int a, int m, int s_off, int l_off,
+                                           long long cap_work) {
+  const int full = m / KD_TILE, r = m - full * KD_TILE;
+  int nl = full;
+  if (r > KD_SERIAL_TILE_MAX) ++nl;
+  for (int lt = 0; lt < nl; ++lt)
+    if (l_off + lt < cap_work) lv.work_l[l_off + lt] = make_int2(a, lt);
+  if (r > 0 && r <= KD_SERIAL_TILE_MAX && s_off < cap_work) lv.work_s[s_off] = make_int2(a, full);
+}
+
+// Level-0 plan over the touched keys: small / large tiles, multi-tile keys and
+// the dense offset of every key's merged input.
 struct Plan0Src {
   const int4* totals;
   const int* tm;
   __device__ int4 operator()(long long j) const {
     if (j >= totals[0].x) return make_int4(0, 0, 0, 0);
     const int m = tm[j];
-    const int tiles = (m + KD_TILE - 1) / KD_TILE;
-    const bool fin = tiles <= 1;
-    return make_int4(tiles, fin ? 0 : tiles, fin ? 0 : 1, 0);
+    const TileSplit t = tile_split(m);
+    return make_int4(t.small, t.large, m > KD_TILE ? 1 : 0, m);
   }
 };
 struct Plan0Dst {
   const int4* totals;
   const int* tm;
-  int* ttile_off;
-  int* tinter_off;
-  int* ttiles;
+  KdLevelDev cur;
   KdLevelDev nxt;
+  long long cap_work;
+  long long cap_keys;
   __device__ void operator()(long long j, int4 excl, int4 v) const {
     if (j >= totals[0].x) return;
-    ttile_off[j] = excl.x;
-    tinter_off[j] = excl.y;
-    ttiles[j] = v.x;
-    if (v.z) {
+    cur.j[j] = (int)j;
+    cur.m[j] = v.w;
+    cur.base[j] = excl.w;
+    write_work(cur, (int)j, v.w, excl.x, excl.y, cap_work);
+    if (v.z && excl.z < cap_keys) {
       nxt.j[excl.z] = (int)j;
-      nxt.src_base[excl.z] = excl.y;
-      nxt.src_tiles[excl.z] = v.x;
-      nxt.mprev[excl.z] = tm[j];
+      nxt.src_tiles[excl.z] = v.x + v.y;
+      nxt.mprev[excl.z] = v.w;
     }
   }
 };
 
-struct L0Args {
+struct InterArgs {
+  const int* A;  // multi-tile keys of level 0
+  KdLevelDev cur;
+  KdLevelDev nxt;
+  int* I;
+  long long cap_inter;
+  int* needs;
+  KdErrHost* err;
+};
+
+// Intermediate-tile offsets of the level-0 keys that exceed one tile (one block).
+__global__ void __launch_bounds__(1024) k_inter0(InterArgs p) {
+  __shared__ int4 sw[32];
+  const int A = *p.A;
+  const int per = (A + blockDim.x - 1) / blockDim.x;
+  const int a0 = min(A, (int)threadIdx.x * per), a1 = min(A, a0 + per);
+  int sum = 0;
+  for (int a = a0; a < a1; ++a) sum += p.nxt.src_tiles[a];
+  int4 tot;
+  const int4 incl = block_scan_incl(make_int4(sum, 0, 0, 0), sw, &tot);
+  int run = incl.x - sum;
+  for (int a = a0; a < a1; ++a) {
+    p.nxt.src_base[a] = run;
+    p.cur.inter_off[p.nxt.j[a]] = run;
+    run += p.nxt.src_tiles[a];
+  }
+  if (threadIdx.x == 0) {
+    *p.I = tot.x;
+    if (tot.x > p.cap_inter) {
+      atomicMax(&p.needs[2], tot.x);
+      kd_err_set(p.err, KD_ERANGE_SCRATCH, tot.x);
+    }
+  }
+}
+
+struct MergeArgs {
   KdStoreDev s;
   long long n;
   const uint64_t* k64;
-  const uint32_t* idx;
+  const uint32_t* skey;
+  const uint32_t* sidx;
   const double* wts;
   const uint32_t* tkey;
+  const uint32_t* tmap;
   const int* tstart;
-  const int* tm;
   const int* tprior;
   const unsigned char* tbuf;
   const double* tsf;
   const double* tpscale;
-  const int* ttile_off;
-  const int* ttiles;
-  const int* tinter_off;
+  const int* base;
   const int4* totals;
+  double* dx;
+  double* dw;
+  long long cap_merged;
+  int* needs;
+  KdErrHost* err;
+};
+
+__device__ __forceinline__ bool merged_fits(const MergeArgs& a) {
+  const int M0 = a.totals[1].w;
+  if (M0 > a.cap_merged) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      atomicMax(&a.needs[1], M0);
+      kd_err_set(a.err, KD_ERANGE_SCRATCH, M0);
+    }
+    return false;
+  }
+  return true;
+}
+
+// New samples: merged position = rank among the key's new samples + number of
+// prior centroids with mean <= value (priors precede new samples on ties, their
+// indices being lower, gpu/grouped.mojo:489-538).
+__global__ void k_merge_new(MergeArgs a) {
+  if (kd_err_get(a.err) || !merged_fits(a)) return;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const uint32_t k = a.skey[i];
+    const int j = (int)a.tmap[k];
+    const int jn = (int)(i - a.tstart[j]);
+    const int np = a.tprior[j];
+    const uint64_t vk = a.k64[i];
+    int lo = 0;
+    if (np > 0) {
+      const double* pm = a.s.slot_m + slot_base(a.s.K, a.tbuf[j] ^ 1, k);
+      int hi = np;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (kd_order_key(pm[mid]) <= vk) lo = mid + 1;
+        else hi = mid;
+      }
+    }
+    const long long pos = (long long)a.base[j] + jn + lo;
+    a.dx[pos] = kd_from_order_key(vk);
+    a.dw[pos] = a.wts ? a.wts[a.sidx[i]] : a.tsf[j];
+  }
+}
+
+// Prior centroids: merged position = prior index + number of new samples with
+// value < mean.  One warp per touched key.
+__global__ void k_merge_prior(MergeArgs a) {
+  if (kd_err_get(a.err) || !merged_fits(a)) return;
+  const int U = a.totals[0].x;
+  const int lane = threadIdx.x & 31;
+  for (int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < U;
+       j += (gridDim.x * blockDim.x) >> 5) {
+    const int np = a.tprior[j];
+    if (np == 0) continue;
+    const uint32_t k = a.tkey[j];
+    const int s0 = a.tstart[j];
+    const int nn = (j + 1 < U ? a.tstart[j + 1] : (int)a.n) - s0;
+    const int live = a.tbuf[j] ^ 1;
+    const double* pm = a.s.slot_m + slot_base(a.s.K, live, k);
+    const double* pw = a.s.slot_w + slot_base(a.s.K, live, k);
+    const double pscale = a.tpscale[j];
+    const bool rescale = pscale != 1.0;
+    const uint64_t* nk = a.k64 + s0;
+    for (int i = lane; i < np; i += 32) {
+      const uint64_t pk = kd_order_key(pm[i]);
+      int lo = 0, hi = nn;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (nk[mid] < pk) lo = mid + 1;
+        else hi = mid;
+      }
+      const long long pos = (long long)a.base[j] + i + lo;
+      a.dx[pos] = kd_from_order_key(pk);
+      a.dw[pos] = rescale ? KD_MUL(pw[i], pscale) : pw[i];
+    }
+  }
+}
+
+struct TileArgs {
+  KdStoreDev s;
+  const int* Tl;
+  const int* Ts;
+  const int* I;
+  KdLevelDev lv;
+  const double* dx;
+  const double* dw;
+  const uint32_t* tkey;
+  const unsigned char* tbuf;
+  int* st_count;
   double* scr_m;
   double* scr_w;
   int* tcount;
-  int* st_count;
+  long long cap_work;
   long long cap_inter;
+  int* needs;
   int force_exact;
   KdErrHost* err;
 };
 
-// Level 0: merge-path load of (prior centroids ++ new samples) fused with the
-// tile compress.  Priors precede new samples on ties (their indices are lower).
-__global__ void __launch_bounds__(32 * KD_WARPS_PER_BLOCK) k_level0(L0Args a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  WarpTile& t = reinterpret_cast<WarpTile*>(smem_raw)[threadIdx.x >> 5];
-  if (kd_err_get(a.err)) return;
-  const int U = a.totals[0].x;
-  const int T0 = a.totals[1].x;
-  const int I0 = a.totals[1].y;
-  if (I0 > a.cap_inter) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) kd_err_set(a.err, KD_ERANGE_SCRATCH, I0);
-    return;
+__device__ __forceinline__ bool tiles_fit(const TileArgs& a, int T) {
+  const int I = *a.I;
+  if (T > a.cap_work || I > a.cap_inter) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      atomicMax(&a.needs[0], T);
+      atomicMax(&a.needs[2], I);
+      kd_err_set(a.err, KD_ERANGE_SCRATCH, T);
+    }
+    return false;
   }
+  return true;
+}
+
+// Output location of tile (ai, lt): the key's back slot when its input fits one
+// tile, else the tile's intermediate slot.
+struct TileOut {
+  double* m;
+  double* w;
+  int* count;
+};
+__device__ __forceinline__ TileOut tile_out(const TileArgs& a, int ai, int lt, int j, int m) {
+  TileOut o;
+  if (m <= KD_TILE) {
+    const uint32_t key = a.tkey[j];
+    const int backb = a.tbuf[j];
+    o.m = a.s.slot_m + slot_base(a.s.K, backb, key);
+    o.w = a.s.slot_w + slot_base(a.s.K, backb, key);
+    o.count = a.st_count + j;
+  } else {
+    const int it = a.lv.inter_off[ai] + lt;
+    o.m = a.scr_m + (size_t)it * KD_TILE;
+    o.w = a.scr_w + (size_t)it * KD_TILE;
+    o.count = a.tcount + it;
+  }
+  return o;
+}
+
+// One warp per tile: coalesced load into the slot layout of the tile's chunk
+// length, then the tile compress.  CAP = KD_TILE serves the large work list
+// (tiles above KD_SERIAL_TILE_MAX elements), CAP = KD_SERIAL_TILE_MAX the small
+// one; both lists are consumed by their own launch.
+template <int CAP>
+__global__ void __launch_bounds__(32 * (CAP == KD_TILE ? 1 : 4)) k_tiles(TileArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int WPB = CAP == KD_TILE ? 1 : 4;
+  WarpTileT<CAP>& t = reinterpret_cast<WarpTileT<CAP>*>(smem_raw)[threadIdx.x >> 5];
+  if (kd_err_get(a.err)) return;
+  const int T = CAP == KD_TILE ? *a.Tl : *a.Ts;
+  if (!tiles_fit(a, T)) return;
+  const int2* work = CAP == KD_TILE ? a.lv.work_l : a.lv.work_s;
   const int lane = threadIdx.x & 31;
   const KdStoreDev& s = a.s;
-  for (int w = blockIdx.x * KD_WARPS_PER_BLOCK + (threadIdx.x >> 5); w < T0;
-       w += gridDim.x * KD_WARPS_PER_BLOCK) {
-    int lo = 0, hi = U - 1;  // last j with ttile_off[j] <= w
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (a.ttile_off[mid] <= w) lo = mid;
-      else hi = mid - 1;
+  for (int w = blockIdx.x * WPB + (threadIdx.x >> 5); w < T; w += gridDim.x * WPB) {
+    const int2 wk = work[w];
+    const int ai = wk.x, lt = wk.y;
+    const int j = a.lv.j[ai];
+    const int m = a.lv.m[ai];
+    const long long src = (long long)a.lv.base[ai] + (long long)lt * KD_TILE;
+    const int n = min(KD_TILE, m - lt * KD_TILE);
+    const int E = tile_chunk(n), SE = E | 1;
+    const unsigned inv = tile_inv(E);
+    bool integral = true;
+    for (int p = lane; p < n; p += 32) {
+      const int slot = tile_slot(p, E, SE, inv);
+      const double wv = a.dw[src + p];
+      t.x[slot] = a.dx[src + p];
+      t.w[slot] = wv;
+      integral = integral && kd_is_small_int(wv);
     }
-    const int j = lo;
-    const int lt = w - a.ttile_off[j];
-    const int m = a.tm[j];
-    const int tstart_m = lt * KD_TILE;
-    const int n = min(KD_TILE, m - tstart_m);
-    const uint32_t key = a.tkey[j];
-    const int np = a.tprior[j];
-    const int backb = a.tbuf[j];
-    const double* pm = s.slot_m + slot_base(s.K, backb ^ 1, key);
-    const double* pw = s.slot_w + slot_base(s.K, backb ^ 1, key);
-    const double pscale = a.tpscale[j];
-    const bool rescale = pscale != 1.0;
-    const int ns = a.tstart[j];
-    const int nn = (j + 1 < U ? a.tstart[j + 1] : (int)a.n) - ns;
-    const uint64_t* nk = a.k64 + ns;
-    const double sf = a.tsf[j];
-
-    // Lane chunk [lo_e, lo_e + cnt) of merged positions.
-    const int E = (n + 31) >> 5, SE = E | 1;
-    const int lo_e = lane * E;
-    const int cnt = max(0, min(E, n - lo_e));
-    const int sb = lane * SE;
-    if (cnt > 0) {
-      const int d0 = tstart_m + lo_e;
-      int ilo = max(0, d0 - nn), ihi = min(d0, np);
-      while (ilo < ihi) {
-        int mid = (ilo + ihi) >> 1;
-        if (canon(pm[mid]) <= kd_from_order_key(nk[d0 - mid - 1])) ilo = mid + 1;
-        else ihi = mid;
-      }
-      int i = ilo, jn = d0 - ilo;
-      double acc = 0.0;
-      for (int c = 0; c < cnt; ++c) {
-        double xv, wv;
-        bool take_prior = i < np;
-        if (take_prior && jn < nn) take_prior = canon(pm[i]) <= kd_from_order_key(nk[jn]);
-        if (take_prior) {
-          xv = canon(pm[i]);
-          wv = rescale ? KD_MUL(pw[i], pscale) : pw[i];
-          ++i;
-        } else {
-          xv = kd_from_order_key(nk[jn]);
-          wv = a.wts ? a.wts[a.idx[ns + jn]] : sf;
-          ++jn;
-        }
-        acc = c == 0 ? wv : KD_ADD(acc, wv);
-        t.x[sb + c] = xv;
-        t.w[sb + c] = wv;
-        t.L[sb + c] = acc;
-      }
-    }
+    integral = __all_sync(0xffffffffu, integral);
     __syncwarp();
-    const bool fin = a.ttiles[j] == 1;
-    double* om;
-    double* ow;
-    if (fin) {
-      om = s.slot_m + slot_base(s.K, backb, key);
-      ow = s.slot_w + slot_base(s.K, backb, key);
-    } else {
-      const size_t base = (size_t)(a.tinter_off[j] + lt) * KD_TILE;
-      om = a.scr_m + base;
-      ow = a.scr_w + base;
-    }
-    const int c = warp_compress(t, n, s.scale, s.compression, a.force_exact, om, ow);
-    if (lane == 0) {
-      if (fin) a.st_count[j] = c;
-      else a.tcount[a.tinter_off[j] + lt] = c;
-    }
+    const TileOut o = tile_out(a, ai, lt, j, m);
+    const int c = integral
+                      ? warp_compress<true, CAP>(t, n, s.scale, s.compression, a.force_exact, o.m, o.w)
+                      : warp_compress<false, CAP>(t, n, s.scale, s.compression, a.force_exact, o.m, o.w);
+    if (lane == 0) *o.count = c;
   }
 }
 
 struct PlanArgs {
+  const int* A;
+  const int* Iprev;  // intermediate tiles written by the previous level
   KdLevelDev cur;
   KdLevelDev nxt;
-  const int* prev_count;
-  int* prev_doff;
+  const int* tcount;
+  int* gpre;  // dense offset of every previous-level intermediate tile
   const uint32_t* tkey;
+  long long cap_work;
   long long cap_inter;
   long long cap_keys;
+  long long cap_merged;
+  int* needs;
   KdErrHost* err;
 };
 
-// Levels >= 1: per active key, dense offsets of its previous-level survivors
-// (the reference's _scan_counts_kernel, add_batch.mojo:407-452) and the new
-// tiling; keys still above one tile move on to the next level.
+// Levels >= 1 (one block).  The previous level's survivors are laid out densely
+// in intermediate-tile order, so one scan of the tile counts gives every active
+// key its dense base and size (the reference's _scan_counts_kernel,
+// add_batch.mojo:407-452); then each key's new tiling and work lists, and the
+// keys still above one tile move on to the next level.
 __global__ void __launch_bounds__(1024) k_plan(PlanArgs p) {
   __shared__ int4 sw[32];
-  const int A = *p.cur.A;
+  const int A = *p.A;
   if (A == 0 || kd_err_get(p.err)) {
     if (threadIdx.x == 0) {
-      *p.cur.T = 0;
+      *p.cur.Tl = 0;
+      *p.cur.Ts = 0;
       *p.cur.I = 0;
+      *p.cur.M = 0;
       *p.nxt.A = 0;
     }
     return;
   }
+  // 1. exclusive scan of the previous level's tile counts -> gpre
+  const int I = *p.Iprev;
+  {
+    const int per = (I + blockDim.x - 1) / blockDim.x;
+    const int s0 = min(I, (int)threadIdx.x * per), s1 = min(I, s0 + per);
+    int sum = 0;
+    for (int s = s0; s < s1; ++s) sum += p.tcount[s];
+    int4 tot;
+    int4 incl = block_scan_incl(make_int4(sum, 0, 0, 0), sw, &tot);
+    int run = incl.x - sum;
+    for (int s = s0; s < s1; ++s) {
+      p.gpre[s] = run;
+      run += p.tcount[s];
+    }
+    if (threadIdx.x == 0) p.gpre[I] = tot.x;
+    __syncthreads();
+  }
+  // 2. per active key: dense base / size, tiling
   const int per = (A + blockDim.x - 1) / blockDim.x;
   const int a0 = min(A, (int)threadIdx.x * per), a1 = min(A, a0 + per);
   int4 acc = make_int4(0, 0, 0, 0);
+  int acc_inter = 0;
   for (int a = a0; a < a1; ++a) {
-    int run = 0;
-    const int sbase = p.cur.src_base[a], sn = p.cur.src_tiles[a];
-    for (int s = sbase; s < sbase + sn; ++s) {
-      p.prev_doff[s] = run;
-      run += p.prev_count[s];
-    }
-    p.cur.m[a] = run;
-    if (run >= p.cur.mprev[a]) kd_err_set(p.err, KD_ECONVERGE, (long long)p.tkey[p.cur.j[a]]);
-    const int tiles = (run + KD_TILE - 1) / KD_TILE;
-    const bool fin = tiles <= 1;
-    acc = i4add(acc, make_int4(tiles, fin ? 0 : tiles, fin ? 0 : 1, 0));
+    const int sb = p.cur.src_base[a], se = sb + p.cur.src_tiles[a];
+    const int base = p.gpre[sb];
+    const int m = p.gpre[se] - base;
+    p.cur.base[a] = base;
+    p.cur.m[a] = m;
+    if (m >= p.cur.mprev[a]) kd_err_set(p.err, KD_ECONVERGE, (long long)p.tkey[p.cur.j[a]]);
+    const TileSplit t = tile_split(m);
+    const bool fin = m <= KD_TILE;
+    acc = i4add(acc, make_int4(t.small, t.large, fin ? 0 : 1, m));
+    acc_inter += fin ? 0 : t.small + t.large;
   }
-  int4 tot;
-  int4 incl = block_scan_incl(acc, sw, &tot);
-  int4 run = make_int4(incl.x - acc.x, incl.y - acc.y, incl.z - acc.z, 0);
+  int4 tot, tot2;
+  const int4 incl = block_scan_incl(acc, sw, &tot);
+  const int4 incl2 = block_scan_incl(make_int4(acc_inter, 0, 0, 0), sw, &tot2);
+  int4 run = make_int4(incl.x - acc.x, incl.y - acc.y, incl.z - acc.z, incl.w - acc.w);
+  int run_inter = incl2.x - acc_inter;
   for (int a = a0; a < a1; ++a) {
     const int m = p.cur.m[a];
-    const int tiles = (m + KD_TILE - 1) / KD_TILE;
-    const bool fin = tiles <= 1;
-    p.cur.tile_off[a] = run.x;
-    p.cur.inter_off[a] = run.y;
-    if (!fin) {
+    const TileSplit t = tile_split(m);
+    const bool fin = m <= KD_TILE;
+    p.cur.inter_off[a] = run_inter;
+    write_work(p.cur, a, m, run.x, run.y, p.cap_work);
+    if (!fin && run.z < p.cap_keys) {
       p.nxt.j[run.z] = p.cur.j[a];
-      p.nxt.src_base[run.z] = run.y;
-      p.nxt.src_tiles[run.z] = tiles;
+      p.nxt.src_base[run.z] = run_inter;
+      p.nxt.src_tiles[run.z] = t.small + t.large;
       p.nxt.mprev[run.z] = m;
     }
-    run = i4add(run, make_int4(tiles, fin ? 0 : tiles, fin ? 0 : 1, 0));
+    run = i4add(run, make_int4(t.small, t.large, fin ? 0 : 1, m));
+    run_inter += fin ? 0 : t.small + t.large;
   }
   if (threadIdx.x == 0) {
-    *p.cur.T = tot.x;
-    *p.cur.I = tot.y;
+    *p.cur.Ts = tot.x;
+    *p.cur.Tl = tot.y;
+    *p.cur.I = tot2.x;
+    *p.cur.M = tot.w;
     *p.nxt.A = tot.z;
-    if (tot.y > p.cap_inter) kd_err_set(p.err, KD_ERANGE_SCRATCH, tot.y);
+    if (tot.x > p.cap_work || tot.y > p.cap_work || tot2.x > p.cap_inter || tot.w > p.cap_merged) {
+      atomicMax(&p.needs[0], max(tot.x, tot.y));
+      atomicMax(&p.needs[1], tot.w);
+      atomicMax(&p.needs[2], tot2.x);
+      kd_err_set(p.err, KD_ERANGE_SCRATCH, tot.y);
+    }
   }
 }
 
-struct LLArgs {
-  KdStoreDev s;
-  KdLevelDev cur;
-  const uint32_t* tkey;
-  const unsigned char* tbuf;
-  int* st_count;
-  const double* src_m;
-  const double* src_w;
-  const int* src_count;
-  const int* src_doff;
-  double* dst_m;
-  double* dst_w;
-  int* dst_count;
-  int force_exact;
+struct CompactArgs {
+  const int* Iprev;
+  const int* tcount;
+  const int* gpre;
+  const double* scr_m;
+  const double* scr_w;
+  double* dx;
+  double* dw;
   KdErrHost* err;
 };
 
-// Levels >= 1: dense load of the previous level's survivors (the gather of
-// _gather_tiles_kernel, add_batch.mojo:455-478, fused into the load).
-__global__ void __launch_bounds__(32 * KD_WARPS_PER_BLOCK) k_level(LLArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  WarpTile& t = reinterpret_cast<WarpTile*>(smem_raw)[threadIdx.x >> 5];
-  if (kd_err_get(a.err)) return;
-  const int A = *a.cur.A;
-  const int T = *a.cur.T;
+// Packs the previous level's survivors densely, one warp per intermediate tile
+// (the gather of _gather_tiles_kernel, add_batch.mojo:455-478).
+__global__ void k_compact(CompactArgs c) {
+  if (kd_err_get(c.err)) return;
+  const int I = *c.Iprev;
   const int lane = threadIdx.x & 31;
-  const KdStoreDev& s = a.s;
-  for (int w = blockIdx.x * KD_WARPS_PER_BLOCK + (threadIdx.x >> 5); w < T;
-       w += gridDim.x * KD_WARPS_PER_BLOCK) {
-    int lo = 0, hi = A - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (a.cur.tile_off[mid] <= w) lo = mid;
-      else hi = mid - 1;
-    }
-    const int ai = lo;
-    const int lt = w - a.cur.tile_off[ai];
-    const int m = a.cur.m[ai];
-    const int dstart = lt * KD_TILE;
-    const int n = min(KD_TILE, m - dstart);
-    const int j = a.cur.j[ai];
-    const uint32_t key = a.tkey[j];
-    const int sbase = a.cur.src_base[ai], sn = a.cur.src_tiles[ai];
-    const int E = (n + 31) >> 5, SE = E | 1;
-    const int lo_e = lane * E;
-    const int cnt = max(0, min(E, n - lo_e));
-    const int sb = lane * SE;
-    if (cnt > 0) {
-      const int d0 = dstart + lo_e;
-      int l2 = sbase, h2 = sbase + sn - 1;  // last source tile with doff <= d0
-      while (l2 < h2) {
-        int mid = (l2 + h2 + 1) >> 1;
-        if (a.src_doff[mid] <= d0) l2 = mid;
-        else h2 = mid - 1;
-      }
-      int sidx = l2;
-      int r = d0 - a.src_doff[sidx];
-      double acc = 0.0;
-      const int send = sbase + sn;
-      for (int c = 0; c < cnt; ++c) {
-        while (r >= a.src_count[sidx] && sidx + 1 < send) {
-          ++sidx;
-          r = 0;
-        }
-        if (r >= a.src_count[sidx]) {  // inconsistent counts: never read past the key's tiles
-          kd_err_set(a.err, KD_ECONVERGE, -2);
-          break;
-        }
-        const size_t off = (size_t)sidx * KD_TILE + r;
-        const double xv = a.src_m[off], wv = a.src_w[off];
-        ++r;
-        acc = c == 0 ? wv : KD_ADD(acc, wv);
-        t.x[sb + c] = xv;
-        t.w[sb + c] = wv;
-        t.L[sb + c] = acc;
-      }
-    }
-    __syncwarp();
-    const bool fin = m <= KD_TILE;
-    double* om;
-    double* ow;
-    const int backb = a.tbuf[j];
-    if (fin) {
-      om = s.slot_m + slot_base(s.K, backb, key);
-      ow = s.slot_w + slot_base(s.K, backb, key);
-    } else {
-      const size_t base = (size_t)(a.cur.inter_off[ai] + lt) * KD_TILE;
-      om = a.dst_m + base;
-      ow = a.dst_w + base;
-    }
-    const int c = warp_compress(t, n, s.scale, s.compression, a.force_exact, om, ow);
-    if (lane == 0) {
-      if (fin) a.st_count[j] = c;
-      else a.dst_count[a.cur.inter_off[ai] + lt] = c;
+  for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < I;
+       s += (gridDim.x * blockDim.x) >> 5) {
+    const int cnt = c.tcount[s];
+    const long long d = c.gpre[s];
+    const size_t so = (size_t)s * KD_TILE;
+    for (int r = lane; r < cnt; r += 32) {
+      c.dx[d + r] = c.scr_m[so + r];
+      c.dw[d + r] = c.scr_w[so + r];
     }
   }
 }
@@ -688,7 +930,7 @@ struct CommitArgs {
 __global__ void k_commit(CommitArgs a) {
   const int U = a.totals[0].x;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j == 0 && *a.remaining > 0) kd_err_set(a.err, KD_ECONVERGE, -1);
+  if (j == 0 && *a.remaining > 0) kd_err_set(a.err, KD_EMORE_LEVELS, *a.remaining);
   if (j >= U) return;
   if (kd_err_get(a.err) || *a.remaining > 0) return;
   const KdStoreDev& s = a.s;
@@ -966,15 +1208,21 @@ static const char* err_text(int code) {
   }
 }
 
-static int level_grid(KdSession* s) { return s->num_sms * 2; }
+static int level_grid(KdSession* s) { return s->num_sms * 6; }
 
-static size_t tile_smem() { return sizeof(WarpTile) * KD_WARPS_PER_BLOCK; }
+static size_t tile_smem() { return sizeof(WarpTile); }
+static size_t tile_smem_small() { return sizeof(WarpTileSmall) * 4; }
 
 static int ensure_attrs(KdSession* s) {
   static bool done = false;
   if (done) return KD_OK;
-  KD_CK(cudaFuncSetAttribute(k_level0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem()));
-  KD_CK(cudaFuncSetAttribute(k_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem()));
+  KD_CK(cudaFuncSetAttribute(k_tiles<KD_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem()));
+  KD_CK(cudaFuncSetAttribute(kd_rs_onesweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kd_rs_smem(true)));
+  KD_CK(cudaFuncSetAttribute(kd_rs_onesweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kd_rs_smem(false)));
+  KD_CK(cudaFuncSetAttribute(k_tiles<KD_SERIAL_TILE_MAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tile_smem_small()));
   done = true;
   return KD_OK;
 }
@@ -993,10 +1241,13 @@ int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const 
   cudaStream_t str = s->stream;
   const KdStoreDev sd = st->d;
   const long long keys_max = std::min<long long>(n, sd.K);
-  long long inter = std::max<long long>(64, 2 * (n / KD_TILE) + 64);
-  if (s->ws.cap_inter > inter) inter = s->ws.cap_inter;
+  long long want_inter = std::max<long long>(64, 2 * (n / KD_TILE) + 64);
+  long long want_work = 2 * keys_max + n / KD_TILE + 64;
+  long long want_merged = 2 * n + 64 * keys_max + 1024;
   for (int attempt = 0; attempt < 4; ++attempt) {
-    rc = kd_ws_reserve(s, n, keys_max, inter);
+    KdWorkspace& w0 = s->ws;
+    rc = kd_ws_reserve(s, n, keys_max, std::max(want_inter, w0.cap_inter),
+                       std::max(want_work, w0.cap_work), std::max(want_merged, w0.cap_merged), sd.K);
     if (rc) return rc;
     KdWorkspace& w = s->ws;
     {
@@ -1006,64 +1257,134 @@ int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const 
       KD_CK(cudaMemcpyAsync(w.err, w.h_err, sizeof(KdErrHost), cudaMemcpyHostToDevice, str));
     }
     KD_CK(cudaMemsetAsync(w.totals, 0, sizeof(int4) * 8, str));
+    KD_CK(cudaMemsetAsync(w.needs, 0, sizeof(int) * 4, str));
     const bool with_idx = d_wts != nullptr;
+    KdStageStats& T = s->stats;
+    auto mark = [&](int i) {
+      if (T.enabled) cudaEventRecord(T.ev[i], str);
+    };
+    const int key_bits = key_bits_for(sd.K);
+    long long launches = 0;
+    mark(0);
     {
       int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
       k_prep<<<grid, 256, 0, str>>>(n, d_keys, d_vals, d_wts, sd.K, w.k64[0], w.key[0],
                                     with_idx ? w.idx[0] : nullptr, w.err);
+      launches += 1;
     }
-    KdSortBufs sb{{w.k64[0], w.k64[1]}, {w.key[0], w.key[1]}, {w.idx[0], w.idx[1]}, w.hist, w.partials};
-    const int r = kd_radix_sort(sb, n, key_bits_for(sd.K), with_idx, str);
+    mark(1);
+    KdSortBufs sb{{w.k64[0], w.k64[1]}, {w.key[0], w.key[1]}, {w.idx[0], w.idx[1]}, w.ghist,
+                  w.rs_state, w.rs_ticket, &w.rs_epoch, w.cap_rs_tiles,
+                  &reinterpret_cast<KdErr*>(w.err)->code};
+    const int r = kd_radix_sort(sb, n, key_bits, with_idx, s->num_sms, str);
+    launches += kd_radix_sort_launches(n, key_bits);
+    mark(2);
     const uint64_t* k64 = w.k64[r];
     const uint32_t* skey = w.key[r];
     const uint32_t* sidx = with_idx ? w.idx[r] : nullptr;
-    kd_scan(TouchedSrc{skey}, TouchedDst{skey, w.tkey, w.tstart, w.cap_keys}, n, w.partials,
-            &w.totals[0], str);
+    kd_scan(TouchedSrc{skey}, TouchedDst{skey, w.tkey, w.tstart, w.tmap, w.cap_keys, sd.K}, n,
+            w.partials, &w.totals[0], str);
     {
       PrepareArgs pa{sd, n, k64, w.tkey, w.tstart, w.totals, mode, timestamp,
                      d_merge_min, d_merge_max, d_merge_clock, w.tm, w.tprior, w.tbuf, w.tsf,
                      w.tpscale, w.st_clock, w.st_ls, w.st_min, w.st_max, w.err};
       k_prepare<<<(int)((keys_max + 255) / 256), 256, 0, str>>>(pa);
     }
-    // Level-1 active list is produced directly by the level-0 plan.
-    KdLevelDev l1 = w.lv[1];
-    l1.A = ((int*)&w.totals[1]) + 2;
-    kd_scan(Plan0Src{w.totals, w.tm},
-            Plan0Dst{w.totals, w.tm, w.ttile_off, w.tinter_off, w.ttiles, l1}, keys_max,
-            w.partials, &w.totals[1], str);
+    // Level-0 arrays live in lv[0]; its scalars in totals[1] = (Ts, Tl, A1, M0)
+    // and totals[2].x = I0.
+    KdLevelDev l0 = w.lv[0];
+    l0.Ts = (int*)&w.totals[1] + 0;
+    l0.Tl = (int*)&w.totals[1] + 1;
+    l0.M = (int*)&w.totals[1] + 3;
+    l0.I = (int*)&w.totals[2] + 0;
+    int* a1 = (int*)&w.totals[1] + 2;
+    kd_scan(Plan0Src{w.totals, w.tm}, Plan0Dst{w.totals, w.tm, l0, w.lv[1], w.cap_work, w.cap_keys},
+            keys_max, w.partials, &w.totals[1], str);
     {
-      L0Args la{sd, n, k64, sidx, d_wts, w.tkey, w.tstart, w.tm, w.tprior, w.tbuf, w.tsf,
-                w.tpscale, w.ttile_off, w.ttiles, w.tinter_off, w.totals, w.scr_m[0],
-                w.scr_w[0], w.tcount[0], w.st_count, w.cap_inter, s->force_exact, w.err};
-      k_level0<<<level_grid(s), 32 * KD_WARPS_PER_BLOCK, tile_smem(), str>>>(la);
-    }
-    int* remaining = l1.A;
-    for (int L = 1; L <= s->max_levels; ++L) {
-      KdLevelDev cur = w.lv[L & 1];
-      KdLevelDev nxt = w.lv[(L + 1) & 1];
-      if (L == 1) cur.A = l1.A;
-      // the next level's A lives in its own scalar (never aliased to totals)
-      PlanArgs pa{cur, nxt, w.tcount[(L - 1) & 1], w.doff[(L - 1) & 1], w.tkey, w.cap_inter,
-                  w.cap_keys, w.err};
-      k_plan<<<1, 1024, 0, str>>>(pa);
-      LLArgs la{sd, cur, w.tkey, w.tbuf, w.st_count, w.scr_m[(L - 1) & 1], w.scr_w[(L - 1) & 1],
-                w.tcount[(L - 1) & 1], w.doff[(L - 1) & 1], w.scr_m[L & 1], w.scr_w[L & 1],
-                w.tcount[L & 1], s->force_exact, w.err};
-      k_level<<<level_grid(s), 32 * KD_WARPS_PER_BLOCK, tile_smem(), str>>>(la);
-      remaining = nxt.A;
+      InterArgs ia{a1, l0, w.lv[1], l0.I, w.cap_inter, w.needs, w.err};
+      k_inter0<<<1, 1024, 0, str>>>(ia);
     }
     {
-      CommitArgs ca{sd, w.totals, w.tkey, w.tbuf, w.st_count, w.st_clock, w.st_ls, w.st_min,
-                    w.st_max, remaining, w.err};
-      k_commit<<<(int)((keys_max + 127) / 128), 128, 0, str>>>(ca);
+      MergeArgs ma{sd, n, k64, skey, sidx, d_wts, w.tkey, w.tmap, w.tstart, w.tprior, w.tbuf,
+                   w.tsf, w.tpscale, l0.base, w.totals, w.dx[0], w.dw[0], w.cap_merged, w.needs, w.err};
+      int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
+      k_merge_new<<<grid, 256, 0, str>>>(ma);
+      int pgrid = (int)std::min<long long>((keys_max * 32 + 255) / 256, (long long)s->num_sms * 16);
+      k_merge_prior<<<pgrid, 256, 0, str>>>(ma);
     }
-    KD_CK(cudaGetLastError());
-    KD_CK(cudaMemcpyAsync(w.h_err, w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, str));
-    KD_CK(cudaStreamSynchronize(str));
+    launches += 3 + 1 + 3 + 1 + 2;
+    mark(3);
+    auto launch_tiles = [&](const KdLevelDev& lv, const double* dx, const double* dw) {
+      TileArgs ta{sd, lv.Tl, lv.Ts, lv.I, lv, dx, dw, w.tkey, w.tbuf, w.st_count, w.scr_m,
+                  w.scr_w, w.tcount, w.cap_work, w.cap_inter, w.needs, s->force_exact, w.err};
+      k_tiles<KD_TILE><<<level_grid(s), 32, tile_smem(), str>>>(ta);
+      k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * 8, 128, tile_smem_small(), str>>>(ta);
+      launches += 2;
+    };
+    launch_tiles(l0, w.dx[0], w.dw[0]);
+    mark(4);
+    // Levels >= 1: run the number of levels the store needed last time, then
+    // commit; if keys remain above one tile, continue from where it stopped.
+    const int* curA = a1;
+    const int* Iprev = l0.I;
+    int L = 0;
+    int levels_goal = std::max(1, std::min(st->levels_hint, s->max_levels));
+    for (;;) {
+      for (; L < levels_goal; ) {
+        ++L;
+        KdLevelDev cur = w.lv[L & 1];
+        KdLevelDev nxt = w.lv[(L + 1) & 1];
+        cur.A = const_cast<int*>(curA);
+        PlanArgs pa{curA, Iprev, cur, nxt, w.tcount, w.doff, w.tkey, w.cap_work, w.cap_inter,
+                    w.cap_keys, w.cap_merged, w.needs, w.err};
+        k_plan<<<1, 1024, 0, str>>>(pa);
+        CompactArgs ca{Iprev, w.tcount, w.doff, w.scr_m, w.scr_w, w.dx[L & 1], w.dw[L & 1], w.err};
+        k_compact<<<s->num_sms * 4, 256, 0, str>>>(ca);
+        launches += 2;
+        launch_tiles(cur, w.dx[L & 1], w.dw[L & 1]);
+        curA = nxt.A;
+        Iprev = cur.I;
+      }
+      mark(5);
+      {
+        CommitArgs ca{sd, w.totals, w.tkey, w.tbuf, w.st_count, w.st_clock, w.st_ls, w.st_min,
+                      w.st_max, curA, w.err};
+        k_commit<<<(int)((keys_max + 127) / 128), 128, 0, str>>>(ca);
+        launches += 1;
+      }
+      mark(6);
+      KD_CK(cudaGetLastError());
+      KD_CK(cudaMemcpyAsync(w.h_err, w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, str));
+      KD_CK(cudaMemcpyAsync(w.h_scalars, w.needs, sizeof(int) * 4, cudaMemcpyDeviceToHost, str));
+      KD_CK(cudaStreamSynchronize(str));
+      if (w.h_err->code == KD_EMORE_LEVELS && L < s->max_levels) {
+        // keys still above one tile: reset the status word and run more levels
+        KdErrHost init{0, 0, 0x7fffffffffffffffLL};
+        *w.h_err = init;
+        KD_CK(cudaMemcpyAsync(w.err, w.h_err, sizeof(KdErrHost), cudaMemcpyHostToDevice, str));
+        levels_goal = std::min(s->max_levels, L + 2);
+        continue;
+      }
+      break;
+    }
+    if (w.h_err->code == KD_EMORE_LEVELS) w.h_err->code = KD_ECONVERGE;
+    if (w.h_err->code == 0) st->levels_hint = std::max(1, L);
+    T.launches += launches;
+    T.ingests += 1;
+    if (T.enabled) {
+      for (int i = 0; i < KD_NSTAGES; ++i) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, T.ev[i], T.ev[i + 1]);
+        T.ms[i] += ms;
+      }
+    }
     const KdErrHost e = *w.h_err;
     if (e.code == 0) return KD_OK;
     if (e.code == KD_ERANGE_SCRATCH) {
-      inter = std::max<long long>(inter * 2, e.index + e.index / 2 + 64);
+      const int* need = w.h_scalars;
+      want_work = std::max<long long>(want_work, (long long)need[0] + need[0] / 4 + 64);
+      want_merged = std::max<long long>(want_merged, (long long)need[1] + need[1] / 4 + 1024);
+      want_inter = std::max<long long>(want_inter, (long long)need[2] + need[2] / 4 + 64);
       continue;
     }
     char buf[256];
@@ -1071,14 +1392,14 @@ int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const 
     s->last_error = buf;
     return e.code;
   }
-  s->last_error = "intermediate scratch could not be sized";
+  s->last_error = "ingest scratch could not be sized";
   return KD_ENOMEM;
 }
 
 int kd_pipeline_quantile(KdSession* s, KdStore* st, const uint32_t* d_keys, const double* d_q,
                          long long nq, double* d_out, int is_cdf) {
   if (nq <= 0) return KD_OK;
-  int rc = kd_ws_reserve(s, 1, 1, 64);
+  int rc = s->ws.err ? KD_OK : kd_ws_reserve(s, 1, 1, 64, 64, 64, 1);
   if (rc) return rc;
   KdWorkspace& w = s->ws;
   cudaStream_t str = s->stream;

@@ -6,9 +6,14 @@
 // digits are stable, so elements with equal (key, value) keep their input order,
 // which is exactly the reference's index tie-break.
 //
-// Each pass: per-block digit histograms (warp-private shared counters), one
-// device-wide exclusive scan of the digit-major histogram, then a stable
-// scatter in which every warp ranks its 32-element rounds with __match_any_sync.
+// One histogram pass computes the digit counts of every pass (they do not
+// depend on the order of the elements).  Each pass is then one kernel: a block
+// takes the next tile through an atomic ticket, ranks its elements stably with
+// warp __match_any_sync, publishes its per-digit counts, obtains the counts of
+// all preceding tiles by decoupled look-back, stages the tile in shared memory
+// in digit order and writes it out in coalesced runs.  Look-back waits are
+// bounded: a block that gives up poisons its entry, raises KD_ETIMEOUT and the
+// batch is not committed.
 #pragma once
 
 #include "kd_scan.cuh"
@@ -18,129 +23,227 @@
 #define KD_RS_PER_WARP 512
 #define KD_RS_ROUNDS (KD_RS_PER_WARP / 32)
 #define KD_RS_TILE (KD_RS_WARPS * KD_RS_PER_WARP)
+#define KD_RS_MAXPASS 12
+#define KD_RS_SPIN_LIMIT (1 << 22)
 
-__device__ __forceinline__ unsigned rs_digit(const uint64_t* k64, const uint32_t* key, long long i,
-                                             int shift, int from_key) {
-  return from_key ? ((key[i] >> shift) & 255u) : (unsigned)((k64[i] >> shift) & 255ull);
+// Look-back words: [63:48] epoch, [47:46] status (1 aggregate, 2 inclusive),
+// [45:0] count.
+#define KD_LB_AGG 1ull
+#define KD_LB_INC 2ull
+__device__ __forceinline__ unsigned long long lb_pack(unsigned epoch, unsigned long long st,
+                                                      unsigned long long cnt) {
+  return ((unsigned long long)epoch << 48) | (st << 46) | cnt;
 }
 
-static __global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_hist(const uint64_t* __restrict__ k64,
-                                                           const uint32_t* __restrict__ key,
-                                                           long long n, int shift, int from_key,
-                                                           int* __restrict__ hist, int nb) {
-  __shared__ unsigned cnt[KD_RS_WARPS][256];
-  for (int t = threadIdx.x; t < KD_RS_WARPS * 256; t += KD_RS_THREADS) (&cnt[0][0])[t] = 0;
+static __global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_hist_all(
+    const uint64_t* __restrict__ k64, const uint32_t* __restrict__ key, long long n,
+    int key_passes, unsigned* __restrict__ ghist) {
+  __shared__ unsigned h[KD_RS_MAXPASS][256];
+  for (int t = threadIdx.x; t < KD_RS_MAXPASS * 256; t += KD_RS_THREADS) (&h[0][0])[t] = 0;
   __syncthreads();
-  const int warp = threadIdx.x >> 5;
-  const long long base = (long long)blockIdx.x * KD_RS_TILE;
-#pragma unroll 4
-  for (int r = 0; r < KD_RS_TILE / KD_RS_THREADS; ++r) {
-    long long i = base + (long long)r * KD_RS_THREADS + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[warp][rs_digit(k64, key, i, shift, from_key)], 1u);
-  }
-  __syncthreads();
-  if (threadIdx.x < 256) {
-    unsigned s = 0;
+  for (long long i = (long long)blockIdx.x * KD_RS_THREADS + threadIdx.x; i < n;
+       i += (long long)gridDim.x * KD_RS_THREADS) {
+    const uint64_t v = k64[i];
 #pragma unroll
-    for (int w = 0; w < KD_RS_WARPS; ++w) s += cnt[w][threadIdx.x];
-    hist[(long long)threadIdx.x * nb + blockIdx.x] = (int)s;
+    for (int p = 0; p < 8; ++p) atomicAdd(&h[p][(unsigned)(v >> (8 * p)) & 255u], 1u);
+    const uint32_t kk = key[i];
+    for (int p = 0; p < key_passes; ++p) atomicAdd(&h[8 + p][(kk >> (8 * p)) & 255u], 1u);
+  }
+  __syncthreads();
+  const int used = (8 + key_passes) * 256;
+  for (int t = threadIdx.x; t < used; t += KD_RS_THREADS) {
+    const unsigned c = (&h[0][0])[t];
+    if (c) atomicAdd(&ghist[t], c);
   }
 }
+
+struct KdRsPass {
+  const uint64_t* kin;
+  const uint32_t* keyin;
+  const uint32_t* idxin;
+  uint64_t* kout;
+  uint32_t* keyout;
+  uint32_t* idxout;
+  long long n;
+  int shift;
+  int from_key;
+  const unsigned* ghist;  // 256 digit counts of this pass
+  unsigned long long* state;
+  unsigned long long* ticket;
+  unsigned long long ticket_base;
+  unsigned epoch;
+  int* err_code;  // device status word (KdErr.code)
+};
 
 template <bool kIdx>
-__global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_scatter(
-    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ keyin,
-    const uint32_t* __restrict__ idxin, uint64_t* __restrict__ kout, uint32_t* __restrict__ keyout,
-    uint32_t* __restrict__ idxout, long long n, int shift, int from_key,
-    const int* __restrict__ offs, int nb) {
+__global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_onesweep(KdRsPass a) {
+  extern __shared__ __align__(16) unsigned char rs_smem[];
+  uint64_t* sk = reinterpret_cast<uint64_t*>(rs_smem);
+  uint32_t* skey = reinterpret_cast<uint32_t*>(sk + KD_RS_TILE);
+  uint32_t* sidx = skey + KD_RS_TILE;
   __shared__ unsigned wcnt[KD_RS_WARPS][256];
+  __shared__ unsigned blk_off[256];
+  __shared__ long long gpos[256];
+  __shared__ unsigned gbase_s[256];
+  __shared__ int4 scan_tmp[32];
+  __shared__ int bid_s;
+  if (threadIdx.x == 0) bid_s = (int)(atomicAdd(a.ticket, 1ull) - a.ticket_base);
   for (int t = threadIdx.x; t < KD_RS_WARPS * 256; t += KD_RS_THREADS) (&wcnt[0][0])[t] = 0;
   __syncthreads();
+  const int b = bid_s;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long base = (long long)blockIdx.x * KD_RS_TILE + (long long)warp * KD_RS_PER_WARP;
+  const long long tile0 = (long long)b * KD_RS_TILE;
+  const long long base = tile0 + (long long)warp * KD_RS_PER_WARP;
   const unsigned lt_mask = (1u << lane) - 1u;
+  const int shift = a.shift;
+  uint64_t kv[KD_RS_ROUNDS];
+  uint32_t kk[KD_RS_ROUNDS];
   unsigned rank[KD_RS_ROUNDS];
 #pragma unroll
   for (int r = 0; r < KD_RS_ROUNDS; ++r) {
-    long long i = base + r * 32 + lane;
-    bool valid = i < n;
-    unsigned d = valid ? rs_digit(kin, keyin, i, shift, from_key) : 256u;
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    unsigned before = peers & lt_mask;
-    unsigned c = valid ? wcnt[warp][d] : 0u;
+    const long long i = base + r * 32 + lane;
+    const bool valid = i < a.n;
+    kv[r] = valid ? a.kin[i] : 0ull;
+    kk[r] = valid ? a.keyin[i] : 0u;
+    const unsigned d = valid ? (a.from_key ? (kk[r] >> shift) & 255u : (unsigned)(kv[r] >> shift) & 255u)
+                             : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const unsigned before = peers & lt_mask;
+    const unsigned c = valid ? wcnt[warp][d] : 0u;
     __syncwarp();
     if (valid && before == 0) wcnt[warp][d] = c + __popc(peers);
     __syncwarp();
     rank[r] = c + __popc(before);
   }
   __syncthreads();
+  // per digit: exclusive prefix over warps, tile count, tile offset, global base
+  unsigned cnt_d = 0;
   if (threadIdx.x < 256) {
     unsigned s = 0;
 #pragma unroll
     for (int w = 0; w < KD_RS_WARPS; ++w) {
-      unsigned v = wcnt[w][threadIdx.x];
+      const unsigned v = wcnt[w][threadIdx.x];
       wcnt[w][threadIdx.x] = s;
       s += v;
     }
+    cnt_d = s;
   }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < KD_RS_ROUNDS; ++r) {
-    long long i = base + r * 32 + lane;
-    if (i < n) {
-      uint64_t kv = kin[i];
-      uint32_t kk = keyin[i];
-      unsigned d = from_key ? ((kk >> shift) & 255u) : (unsigned)((kv >> shift) & 255ull);
-      long long pos = (long long)offs[(long long)d * nb + blockIdx.x] + wcnt[warp][d] + rank[r];
-      kout[pos] = kv;
-      keyout[pos] = kk;
-      if (kIdx) idxout[pos] = idxin[i];
+  {
+    int4 tot;
+    const unsigned g = threadIdx.x < 256 ? a.ghist[threadIdx.x] : 0u;
+    const int4 inc = block_scan_incl(make_int4((int)cnt_d, (int)g, 0, 0), scan_tmp, &tot);
+    if (threadIdx.x < 256) {
+      blk_off[threadIdx.x] = (unsigned)(inc.x - (int)cnt_d);
+      gbase_s[threadIdx.x] = (unsigned)(inc.y - (int)g);
     }
   }
+  // decoupled look-back, one thread per digit
+  if (threadIdx.x < 256) {
+    const int d = threadIdx.x;
+    volatile unsigned long long* st = a.state;
+    unsigned long long excl = 0;
+    if (b == 0) {
+      st[d] = lb_pack(a.epoch, KD_LB_INC, cnt_d);
+    } else {
+      st[(size_t)b * 256 + d] = lb_pack(a.epoch, KD_LB_AGG, cnt_d);
+      long long p = b - 1;
+      long long spins = 0;
+      bool timed_out = false;
+      while (p >= 0) {
+        const unsigned long long v = st[(size_t)p * 256 + d];
+        if ((unsigned)(v >> 48) != a.epoch || ((v >> 46) & 3ull) == 0ull) {
+          if (++spins > KD_RS_SPIN_LIMIT) {
+            timed_out = true;
+            break;
+          }
+          continue;
+        }
+        excl += v & ((1ull << 46) - 1ull);
+        if (((v >> 46) & 3ull) == KD_LB_INC) break;
+        --p;
+      }
+      if (timed_out) atomicCAS(a.err_code, 0, KD_ETIMEOUT);
+      st[(size_t)b * 256 + d] = lb_pack(a.epoch, KD_LB_INC, excl + cnt_d);
+    }
+    gpos[d] = (long long)gbase_s[d] + (long long)excl;
+  }
+  __syncthreads();
+  // stage in digit order
+#pragma unroll
+  for (int r = 0; r < KD_RS_ROUNDS; ++r) {
+    const long long i = base + r * 32 + lane;
+    if (i < a.n) {
+      const unsigned d = a.from_key ? (kk[r] >> shift) & 255u : (unsigned)(kv[r] >> shift) & 255u;
+      const unsigned lp = blk_off[d] + wcnt[warp][d] + rank[r];
+      sk[lp] = kv[r];
+      skey[lp] = kk[r];
+      if (kIdx) sidx[lp] = a.idxin[i];
+    }
+  }
+  __syncthreads();
+  // coalesced write-out of digit runs
+  const int cnt = (int)min((long long)KD_RS_TILE, a.n - tile0);
+  for (int i = threadIdx.x; i < cnt; i += KD_RS_THREADS) {
+    const uint64_t v = sk[i];
+    const uint32_t k2 = skey[i];
+    const unsigned d = a.from_key ? (k2 >> shift) & 255u : (unsigned)(v >> shift) & 255u;
+    const long long pos = gpos[d] + (i - (int)blk_off[d]);
+    a.kout[pos] = v;
+    a.keyout[pos] = k2;
+    if (kIdx) a.idxout[pos] = sidx[i];
+  }
 }
-
-struct KdHistSrc {
-  const int* h;
-  __device__ int4 operator()(long long i) const { return make_int4(h[i], 0, 0, 0); }
-};
-struct KdHistDst {
-  int* h;
-  __device__ void operator()(long long i, int4 excl, int4) const { h[i] = excl.x; }
-};
 
 struct KdSortBufs {
   uint64_t* k64[2];
   uint32_t* key[2];
-  uint32_t* idx[2];  // may be null
-  int* hist;         // 256 * nb
-  int4* partials;    // scan partials for 256 * nb entries
+  uint32_t* idx[2];               // may be null
+  unsigned* ghist;                // KD_RS_MAXPASS * 256
+  unsigned long long* state;      // 256 per tile
+  unsigned long long* ticket;     // device ticket counter (reset per sort)
+  unsigned* epoch;                // host-side epoch of the look-back words
+  long long state_tiles;          // tiles the look-back array holds
+  int* err_code;
 };
 
 static inline int kd_rs_blocks(long long n) { return (int)((n + KD_RS_TILE - 1) / KD_RS_TILE); }
-static inline long long kd_rs_hist_entries(long long n) { return 256LL * kd_rs_blocks(n); }
+static inline size_t kd_rs_smem(bool with_idx) {
+  return (size_t)KD_RS_TILE * (8 + 4 + (with_idx ? 4 : 0));
+}
 
 // Sorts by (key, k64); returns the index (0/1) of the buffer set holding the result.
 static inline int kd_radix_sort(KdSortBufs& b, long long n, int key_bits, bool with_idx,
-                                cudaStream_t st) {
+                                int num_sms, cudaStream_t st) {
   int src = 0;
   if (n <= 1) return src;
   const int nb = kd_rs_blocks(n);
-  const long long entries = 256LL * nb;
-  auto pass = [&](int shift, int from_key) {
+  const int key_passes = (key_bits + 7) / 8;
+  cudaMemsetAsync(b.ghist, 0, sizeof(unsigned) * KD_RS_MAXPASS * 256, st);
+  cudaMemsetAsync(b.ticket, 0, sizeof(unsigned long long), st);
+  unsigned long long ticket_base = 0;
+  kd_rs_hist_all<<<num_sms * 8, KD_RS_THREADS, 0, st>>>(b.k64[0], b.key[0], n, key_passes, b.ghist);
+  auto pass = [&](int shift, int from_key, int pidx) {
     const int dst = src ^ 1;
-    kd_rs_hist<<<nb, KD_RS_THREADS, 0, st>>>(b.k64[src], b.key[src], n, shift, from_key, b.hist, nb);
-    kd_scan(KdHistSrc{b.hist}, KdHistDst{b.hist}, entries, b.partials, (int4*)nullptr, st);
+    *b.epoch += 1;
+    if (*b.epoch >= 65535u) {  // epochs wrap: clear the look-back words
+      cudaMemsetAsync(b.state, 0, sizeof(unsigned long long) * 256 * (size_t)b.state_tiles, st);
+      *b.epoch = 1;
+    }
+    KdRsPass a{b.k64[src], b.key[src], b.idx[src], b.k64[dst], b.key[dst], b.idx[dst], n, shift,
+               from_key, b.ghist + pidx * 256, b.state, b.ticket, ticket_base, *b.epoch,
+               b.err_code};
     if (with_idx)
-      kd_rs_scatter<true><<<nb, KD_RS_THREADS, 0, st>>>(b.k64[src], b.key[src], b.idx[src],
-                                                        b.k64[dst], b.key[dst], b.idx[dst], n,
-                                                        shift, from_key, b.hist, nb);
+      kd_rs_onesweep<true><<<nb, KD_RS_THREADS, kd_rs_smem(true), st>>>(a);
     else
-      kd_rs_scatter<false><<<nb, KD_RS_THREADS, 0, st>>>(b.k64[src], b.key[src], nullptr,
-                                                         b.k64[dst], b.key[dst], nullptr, n, shift,
-                                                         from_key, b.hist, nb);
+      kd_rs_onesweep<false><<<nb, KD_RS_THREADS, kd_rs_smem(false), st>>>(a);
+    ticket_base += (unsigned long long)nb;
     src = dst;
   };
-  for (int shift = 0; shift < 64; shift += 8) pass(shift, 0);
-  for (int shift = 0; shift < key_bits; shift += 8) pass(shift, 1);
+  for (int p = 0; p < 8; ++p) pass(8 * p, 0, p);
+  for (int p = 0; p < key_passes; ++p) pass(8 * p, 1, 8 + p);
   return src;
+}
+
+static inline int kd_radix_sort_launches(long long n, int key_bits) {
+  return n > 1 ? 1 + 8 + (key_bits + 7) / 8 : 0;
 }

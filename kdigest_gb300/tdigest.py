@@ -90,6 +90,18 @@ class GpuSession:
     def sync(self):
         _check(self._h, N.load().kd_session_sync(self._h))
 
+    def stats(self) -> dict:
+        ms = np.zeros(8)
+        launches = ctypes.c_int64(0)
+        ingests = ctypes.c_int64(0)
+        n = N.load().kd_session_stats(self._h, N.ptr(ms), 8, ctypes.byref(launches),
+                                      ctypes.byref(ingests))
+        return {"stage_ms": dict(zip(N.STAGES, ms[:n].tolist())), "launches": launches.value,
+                "ingests": ingests.value}
+
+    def reset_stats(self):
+        N.load().kd_session_reset_stats(self._h)
+
     @property
     def stream(self) -> int:
         return N.load().kd_session_stream(self._h) or 0
@@ -432,6 +444,11 @@ class GroupedTDigest:
 
     def centroid_count(self, key: int) -> int:
         return int(self._store.digest(self._key(key))[0][7])
+
+    def centroid_counts(self) -> np.ndarray:
+        out = np.empty(self.num_keys, np.int32)
+        self._store._chk(N.load().kd_store_counts(self._store._h, N.ptr(out), 0))
+        return out
 
     def centroids(self, key: int):
         _, m, w = self._store.digest(self._key(key))

@@ -42,12 +42,57 @@ static double canon(double v) { return v == 0.0 ? 0.0 : v; } /* -0.0 -> +0.0 */
 /*   - the tile total is the cum of its last element;                         */
 /*   - segment sums: serial within a chunk, carried across chunks by a        */
 /*     segmented Kogge-Stone scan of each lane's trailing piece.              */
+/* Tiles of at most KD_SERIAL_TILE_MAX elements (one GPU lane each) sum       */
+/* serially, left to right, instead.                                          */
 /* For integral weights every one of these sums is exact, so the result is    */
 /* independent of the order and equals any other exact evaluation.            */
 /* ------------------------------------------------------------------------- */
+static int tile_compress_serial(int scale, double compression, const double* x, const double* w,
+                                int n, double* out_m, double* out_w, int32_t* ids_out) {
+  double cum[KD_SERIAL_TILE_MAX];
+  int32_t id[KD_SERIAL_TILE_MAX];
+  double acc = w[0];
+  cum[0] = acc;
+  for (int i = 1; i < n; ++i) {
+    acc = acc + w[i];
+    cum[i] = acc;
+  }
+  double tot = cum[n - 1];
+  if (!(tot > 0.0)) tot = 1.0;
+  double nrm = kd_normalizer(scale, compression, tot);
+  for (int i = 0; i < n; ++i) id[i] = kd_bucket(scale, cum[i], tot, nrm);
+  if (ids_out)
+    for (int i = 0; i < n; ++i) ids_out[i] = id[i];
+  int cnt = 0, head = 0;
+  double sw = 0.0, swx = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double wx = w[i] * x[i];
+    if (i == 0 || id[i] != id[i - 1]) {
+      head = i;
+      sw = w[i];
+      swx = wx;
+    } else {
+      sw = sw + w[i];
+      swx = swx + wx;
+    }
+    if (i == n - 1 || id[i] != id[i + 1]) {
+      double mean = sw > 0.0 ? swx / sw : 0.0;
+      double lo_v = x[head], hi_v = x[i];
+      mean = mean < lo_v ? lo_v : mean;
+      mean = mean > hi_v ? hi_v : mean;
+      out_m[cnt] = mean;
+      out_w[cnt] = sw;
+      ++cnt;
+    }
+  }
+  return cnt;
+}
+
 int kdo_tile_compress(int scale, double compression, const double* x, const double* w,
                       int n, double* out_m, double* out_w, int32_t* ids_out) {
   if (n <= 0) return 0;
+  if (n <= KD_SERIAL_TILE_MAX)
+    return tile_compress_serial(scale, compression, x, w, n, out_m, out_w, ids_out);
   const int E = (n + 31) / 32;
   double L[KDO_BLOCK_CAP], cum[KDO_BLOCK_CAP];
   int32_t id[KDO_BLOCK_CAP];

@@ -1,0 +1,61 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports
+every entry point include/kdigest_gb300.h declares; host API validation."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            names |= set(re.findall(r"KD_API\s+[\w\s\*]+?\b(kd_\w+)\s*\(", src))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert {"kd_session_create", "kd_store_ingest", "kd_store_quantile", "kd_compress",
+            "kd_store_merge", "kd_store_to_bytes"} <= names
+
+
+def test_library_exports_every_declared_symbol(kd):
+    lib = ctypes.CDLL(os.path.join(ROOT, "kdigest_gb300", "libkdigest_gb300.so"))
+    missing = [n for n in sorted(_declared()) if not hasattr(lib, n)]
+    assert not missing, missing
+    from kdigest_gb300 import _native
+
+    assert set(_native.EXPORTED) == _declared()
+
+
+def test_library_reports_no_device_without_gpu(kd):
+    """Without a GPU the engine refuses to create a session (no CPU fallback)."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from kdigest_gb300 import _native
+
+    L = _native.load()
+    h = ctypes.c_void_p()
+    rc = L.kd_session_create(0, 0, ctypes.byref(h))
+    assert rc == _native.KD_ECUDA and not h.value
+    assert L.kd_status_string(rc) == b"CUDA error"
+
+
+def test_decay_constructors():
+    """test/test_decay.mojo:41-63."""
+    from kdigest_gb300 import Decay
+
+    assert not Decay.none().is_active()
+    assert Decay.rate(0.5).is_active() and Decay.rate(0.5).rate_lambda == 0.5
+    import math
+
+    assert abs(Decay.half_life(10.0).rate_lambda - math.log(2.0) / 10.0) < 1e-12
+    for h in (0.0, -1.0):
+        with pytest.raises(ValueError):
+            Decay.half_life(h)
