@@ -28,7 +28,7 @@ struct kd_store {
   } while (0)
 
 static int fail(KdSession* s, int code, const char* msg) {
-  s->last_error = msg;
+  kd_set_msg(s, msg);
   return code;
 }
 
@@ -42,7 +42,7 @@ static int dalloc(KdSession* s, void** p, size_t bytes) {
     char buf[200];
     snprintf(buf, sizeof buf, "device-memory budget exceeded (%zu + %zu > %zu bytes)", s->mem_used,
              bytes, s->mem_budget);
-    s->last_error = buf;
+    kd_set_msg(s, buf);
     return KD_ENOMEM;
   }
   cudaError_t e = cudaMalloc(p, bytes);
@@ -121,7 +121,7 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
   if (s->mem_budget && s->mem_used + need > s->mem_budget) {
     char buf[200];
     snprintf(buf, sizeof buf, "device-memory budget exceeded by the ingest workspace (%zu bytes)", need);
-    s->last_error = buf;
+    kd_set_msg(s, buf);
     return KD_ENOMEM;
   }
   auto A = [&](void** p, size_t bytes) -> bool {
@@ -237,7 +237,7 @@ int kd_store_alloc(KdSession* s, KdStore* st) {
     char buf[200];
     snprintf(buf, sizeof buf, "device-memory budget exceeded by a %lld-key store (%zu bytes)",
              (long long)K, bytes);
-    s->last_error = buf;
+    kd_set_msg(s, buf);
     return KD_ENOMEM;
   }
   void* p[12] = {};
@@ -372,7 +372,7 @@ KD_API void kd_session_destroy(kd_session* h) {
   delete h;
 }
 
-KD_API const char* kd_last_error(kd_session* h) { return h ? h->s.last_error.c_str() : "null session"; }
+KD_API const char* kd_last_error(kd_session* h) { return h ? h->s.last_error : "null session"; }
 
 KD_API int kd_session_sync(kd_session* h) {
   if (!h) return KD_EINVAL;

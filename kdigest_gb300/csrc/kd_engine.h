@@ -137,7 +137,7 @@ struct KdSession {
   int num_sms = 0;
   int force_exact = 0;
   int max_levels = 32;
-  std::string last_error;
+  char last_error[256] = {0};  // fixed buffer: reporting an error never allocates
   KdWorkspace ws;
   KdStageStats stats;
   struct KdStore* scratch_store = nullptr;  // 1-key store for stateless compress
@@ -168,3 +168,16 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
                   long long merged, long long tmap);
 void kd_ws_free(KdWorkspace& ws);
 int kd_cuda_fail(KdSession* s, cudaError_t e, const char* what);
+void kd_set_msg(KdSession* s, const char* msg);
+// One-time kernel attributes (shared-memory opt-ins); no allocation.
+int kd_pipeline_prepare_device(KdSession* s);
+
+// One ingest attempt on a caller-provided workspace (allocates nothing).
+// Returns a KD_* status, or KD_ERANGE_SCRATCH_INTERNAL when a capacity of `w`
+// was too small (w.h_scalars[0..2] then hold the needed work / dense /
+// intermediate capacities).
+#define KD_ERANGE_SCRATCH_INTERNAL 100
+int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_t* d_keys,
+                        const double* d_vals, const double* d_wts, long long n, int mode,
+                        double timestamp, const double* d_merge_min, const double* d_merge_max,
+                        const double* d_merge_clock);

@@ -25,7 +25,7 @@
 #include "kd_scan.cuh"
 #include "kd_sort.cuh"
 
-#define KD_ERANGE_SCRATCH 100  // internal: intermediate scratch too small (index = needed)
+#define KD_ERANGE_SCRATCH KD_ERANGE_SCRATCH_INTERNAL  // scratch too small (index = needed)
 #define KD_EMORE_LEVELS 101    // internal: keys still above one tile after the levels run
 
 __device__ __forceinline__ size_t slot_base(long long K, int buf, long long key) {
@@ -1182,8 +1182,12 @@ __global__ void k_merge_headers(KdStoreDev src, const uint32_t* parts, const lon
 // ---------------------------------------------------------------------------
 // Host orchestration
 // ---------------------------------------------------------------------------
+void kd_set_msg(KdSession* s, const char* msg) {
+  snprintf(s->last_error, sizeof s->last_error, "%s", msg);
+}
+
 int kd_cuda_fail(KdSession* s, cudaError_t e, const char* what) {
-  s->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  snprintf(s->last_error, sizeof s->last_error, "%s: %s", what, cudaGetErrorString(e));
   return KD_ECUDA;
 }
 
@@ -1213,7 +1217,7 @@ static int level_grid(KdSession* s) { return s->num_sms * 6; }
 static size_t tile_smem() { return sizeof(WarpTile); }
 static size_t tile_smem_small() { return sizeof(WarpTileSmall) * 4; }
 
-static int ensure_attrs(KdSession* s) {
+int kd_pipeline_prepare_device(KdSession* s) {
   static bool done = false;
   if (done) return KD_OK;
   KD_CK(cudaFuncSetAttribute(k_tiles<KD_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem()));
@@ -1227,29 +1231,14 @@ static int ensure_attrs(KdSession* s) {
   return KD_OK;
 }
 
-int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const double* d_vals,
-                       const double* d_wts, long long n, int mode, double timestamp,
-                       const double* d_merge_min, const double* d_merge_max,
-                       const double* d_merge_clock) {
-  if (n <= 0) return KD_OK;
-  if (n > (1LL << 31) - 1) {
-    s->last_error = "batch too large (limit 2^31 - 1 samples per call)";
-    return KD_ERANGE;
-  }
-  int rc = ensure_attrs(s);
-  if (rc) return rc;
+int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_t* d_keys,
+                        const double* d_vals, const double* d_wts, long long n, int mode,
+                        double timestamp, const double* d_merge_min, const double* d_merge_max,
+                        const double* d_merge_clock) {
   cudaStream_t str = s->stream;
   const KdStoreDev sd = st->d;
   const long long keys_max = std::min<long long>(n, sd.K);
-  long long want_inter = std::max<long long>(64, 2 * (n / KD_TILE) + 64);
-  long long want_work = 2 * keys_max + n / KD_TILE + 64;
-  long long want_merged = 2 * n + 64 * keys_max + 1024;
-  for (int attempt = 0; attempt < 4; ++attempt) {
-    KdWorkspace& w0 = s->ws;
-    rc = kd_ws_reserve(s, n, keys_max, std::max(want_inter, w0.cap_inter),
-                       std::max(want_work, w0.cap_work), std::max(want_merged, w0.cap_merged), sd.K);
-    if (rc) return rc;
-    KdWorkspace& w = s->ws;
+  {
     {
       // index starts at +inf so that the first offending sample wins the atomicMin
       KdErrHost init{0, 0, 0x7fffffffffffffffLL};
@@ -1378,21 +1367,45 @@ int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const 
         T.ms[i] += ms;
       }
     }
-    const KdErrHost e = *w.h_err;
-    if (e.code == 0) return KD_OK;
-    if (e.code == KD_ERANGE_SCRATCH) {
-      const int* need = w.h_scalars;
-      want_work = std::max<long long>(want_work, (long long)need[0] + need[0] / 4 + 64);
-      want_merged = std::max<long long>(want_merged, (long long)need[1] + need[1] / 4 + 1024);
-      want_inter = std::max<long long>(want_inter, (long long)need[2] + need[2] / 4 + 64);
-      continue;
-    }
-    char buf[256];
-    snprintf(buf, sizeof buf, "%s (at index %lld)", err_text(e.code), e.index);
-    s->last_error = buf;
-    return e.code;
   }
-  s->last_error = "ingest scratch could not be sized";
+  const KdErrHost e = *w.h_err;
+  if (e.code == 0) return KD_OK;
+  if (e.code == KD_ERANGE_SCRATCH) return KD_ERANGE_SCRATCH;
+  char buf[256];
+  snprintf(buf, sizeof buf, "%s (at index %lld)", err_text(e.code), e.index);
+  kd_set_msg(s, buf);
+  return e.code;
+}
+
+int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const double* d_vals,
+                       const double* d_wts, long long n, int mode, double timestamp,
+                       const double* d_merge_min, const double* d_merge_max,
+                       const double* d_merge_clock) {
+  if (n <= 0) return KD_OK;
+  if (n > (1LL << 31) - 1) {
+    kd_set_msg(s, "batch too large (limit 2^31 - 1 samples per call)");
+    return KD_ERANGE;
+  }
+  int rc = kd_pipeline_prepare_device(s);
+  if (rc) return rc;
+  const long long keys_max = std::min<long long>(n, st->d.K);
+  long long want_inter = std::max<long long>(64, 2 * (n / KD_TILE) + 64);
+  long long want_work = 2 * keys_max + n / KD_TILE + 64;
+  long long want_merged = 2 * n + 64 * keys_max + 1024;
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    KdWorkspace& w0 = s->ws;
+    rc = kd_ws_reserve(s, n, keys_max, std::max(want_inter, w0.cap_inter),
+                       std::max(want_work, w0.cap_work), std::max(want_merged, w0.cap_merged), st->d.K);
+    if (rc) return rc;
+    rc = kd_pipeline_attempt(s, st, s->ws, d_keys, d_vals, d_wts, n, mode, timestamp, d_merge_min,
+                             d_merge_max, d_merge_clock);
+    if (rc != KD_ERANGE_SCRATCH) return rc;
+    const int* need = s->ws.h_scalars;
+    want_work = std::max<long long>(want_work, (long long)need[0] + need[0] / 4 + 64);
+    want_merged = std::max<long long>(want_merged, (long long)need[1] + need[1] / 4 + 1024);
+    want_inter = std::max<long long>(want_inter, (long long)need[2] + need[2] / 4 + 64);
+  }
+  kd_set_msg(s, "ingest scratch could not be sized");
   return KD_ENOMEM;
 }
 
@@ -1414,7 +1427,7 @@ int kd_pipeline_quantile(KdSession* s, KdStore* st, const uint32_t* d_keys, cons
   if (w.h_err->code) {
     char buf[256];
     snprintf(buf, sizeof buf, "%s (query %lld)", err_text(w.h_err->code), w.h_err->index);
-    s->last_error = buf;
+    kd_set_msg(s, buf);
     return w.h_err->code;
   }
   return KD_OK;
@@ -1424,13 +1437,13 @@ int kd_pipeline_merge(KdSession* s, KdStore* dst, KdStore* src, const long long*
                       const uint32_t* h_parts, long long ngroups) {
   if (ngroups <= 0) return KD_OK;
   if (ngroups > dst->d.K) {
-    s->last_error = "more groups than keys in the destination store";
+    kd_set_msg(s, "more groups than keys in the destination store");
     return KD_EINVAL;
   }
   const long long nparts = h_goff[ngroups];
   for (long long p = 0; p < nparts; ++p)
     if ((long long)h_parts[p] >= src->d.K) {
-      s->last_error = "part key out of range of the source store";
+      kd_set_msg(s, "part key out of range of the source store");
       return KD_EINVAL;
     }
   cudaStream_t str = s->stream;

@@ -75,8 +75,10 @@ struct KdRsPass {
   int* err_code;  // device status word (KdErr.code)
 };
 
+#define KD_LB_WINDOW 16
+
 template <bool kIdx>
-__global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_onesweep(KdRsPass a) {
+__global__ void __launch_bounds__(KD_RS_THREADS, 3) kd_rs_onesweep(KdRsPass a) {
   extern __shared__ __align__(16) unsigned char rs_smem[];
   uint64_t* sk = reinterpret_cast<uint64_t*>(rs_smem);
   uint32_t* skey = reinterpret_cast<uint32_t*>(sk + KD_RS_TILE);
@@ -84,7 +86,6 @@ __global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_onesweep(KdRsPass a) {
   __shared__ unsigned wcnt[KD_RS_WARPS][256];
   __shared__ unsigned blk_off[256];
   __shared__ long long gpos[256];
-  __shared__ unsigned gbase_s[256];
   __shared__ int4 scan_tmp[32];
   __shared__ int bid_s;
   if (threadIdx.x == 0) bid_s = (int)(atomicAdd(a.ticket, 1ull) - a.ticket_base);
@@ -96,27 +97,35 @@ __global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_onesweep(KdRsPass a) {
   const long long base = tile0 + (long long)warp * KD_RS_PER_WARP;
   const unsigned lt_mask = (1u << lane) - 1u;
   const int shift = a.shift;
-  uint64_t kv[KD_RS_ROUNDS];
-  uint32_t kk[KD_RS_ROUNDS];
-  unsigned rank[KD_RS_ROUNDS];
+  // 1. stable rank of every element among the warp's elements of its digit;
+  //    ranks (< 512) are packed two per register
+  unsigned rank2[KD_RS_ROUNDS / 2];
+  unsigned char dig[KD_RS_ROUNDS];
+  unsigned dv[KD_RS_ROUNDS];
+  // all loads of the thread first, so their latency is exposed once
 #pragma unroll
   for (int r = 0; r < KD_RS_ROUNDS; ++r) {
     const long long i = base + r * 32 + lane;
-    const bool valid = i < a.n;
-    kv[r] = valid ? a.kin[i] : 0ull;
-    kk[r] = valid ? a.keyin[i] : 0u;
-    const unsigned d = valid ? (a.from_key ? (kk[r] >> shift) & 255u : (unsigned)(kv[r] >> shift) & 255u)
-                             : 256u;
+    dv[r] = 256u;
+    if (i < a.n) dv[r] = a.from_key ? (a.keyin[i] >> shift) & 255u : (unsigned)(a.kin[i] >> shift) & 255u;
+  }
+#pragma unroll
+  for (int r = 0; r < KD_RS_ROUNDS; ++r) {
+    const unsigned d = dv[r];
+    const bool valid = d < 256u;
+    dig[r] = (unsigned char)(d & 255u);
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const unsigned before = peers & lt_mask;
     const unsigned c = valid ? wcnt[warp][d] : 0u;
     __syncwarp();
     if (valid && before == 0) wcnt[warp][d] = c + __popc(peers);
     __syncwarp();
-    rank[r] = c + __popc(before);
+    const unsigned rk = c + __popc(before);
+    if (r & 1) rank2[r >> 1] |= rk << 16;
+    else rank2[r >> 1] = rk;
   }
   __syncthreads();
-  // per digit: exclusive prefix over warps, tile count, tile offset, global base
+  // 2. per digit: exclusive prefix over warps, tile count, tile offset
   unsigned cnt_d = 0;
   if (threadIdx.x < 256) {
     unsigned s = 0;
@@ -128,16 +137,18 @@ __global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_onesweep(KdRsPass a) {
     }
     cnt_d = s;
   }
+  unsigned gbase = 0;
   {
     int4 tot;
     const unsigned g = threadIdx.x < 256 ? a.ghist[threadIdx.x] : 0u;
     const int4 inc = block_scan_incl(make_int4((int)cnt_d, (int)g, 0, 0), scan_tmp, &tot);
     if (threadIdx.x < 256) {
       blk_off[threadIdx.x] = (unsigned)(inc.x - (int)cnt_d);
-      gbase_s[threadIdx.x] = (unsigned)(inc.y - (int)g);
+      gbase = (unsigned)(inc.y - (int)g);
     }
   }
-  // decoupled look-back, one thread per digit
+  // 3. decoupled look-back, one thread per digit, KD_LB_WINDOW predecessors per
+  //    round trip (independent loads), bounded waits
   if (threadIdx.x < 256) {
     const int d = threadIdx.x;
     volatile unsigned long long* st = a.state;
@@ -146,42 +157,56 @@ __global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_onesweep(KdRsPass a) {
       st[d] = lb_pack(a.epoch, KD_LB_INC, cnt_d);
     } else {
       st[(size_t)b * 256 + d] = lb_pack(a.epoch, KD_LB_AGG, cnt_d);
-      long long p = b - 1;
+      long long hi = b - 1;  // next predecessor to account for
       long long spins = 0;
-      bool timed_out = false;
-      while (p >= 0) {
-        const unsigned long long v = st[(size_t)p * 256 + d];
-        if ((unsigned)(v >> 48) != a.epoch || ((v >> 46) & 3ull) == 0ull) {
-          if (++spins > KD_RS_SPIN_LIMIT) {
-            timed_out = true;
+      bool done = false, timed_out = false;
+      while (!done) {
+        unsigned long long v[KD_LB_WINDOW];
+#pragma unroll
+        for (int k = 0; k < KD_LB_WINDOW; ++k)
+          v[k] = hi - k >= 0 ? st[(size_t)(hi - k) * 256 + d] : lb_pack(a.epoch, KD_LB_INC, 0);
+        // consume the window from hi downwards up to the first not-ready word
+        int k = 0;
+        for (; k < KD_LB_WINDOW; ++k) {
+          const unsigned long long w = v[k];
+          const bool ready = (unsigned)(w >> 48) == a.epoch && ((w >> 46) & 3ull) != 0ull;
+          if (!ready) break;
+          excl += w & ((1ull << 46) - 1ull);
+          if (((w >> 46) & 3ull) == KD_LB_INC) {
+            done = true;
             break;
           }
-          continue;
         }
-        excl += v & ((1ull << 46) - 1ull);
-        if (((v >> 46) & 3ull) == KD_LB_INC) break;
-        --p;
+        if (done) break;
+        hi -= k;
+        if (k == 0 && ++spins > KD_RS_SPIN_LIMIT) {
+          timed_out = true;
+          break;
+        }
       }
       if (timed_out) atomicCAS(a.err_code, 0, KD_ETIMEOUT);
       st[(size_t)b * 256 + d] = lb_pack(a.epoch, KD_LB_INC, excl + cnt_d);
     }
-    gpos[d] = (long long)gbase_s[d] + (long long)excl;
+    gpos[d] = (long long)gbase + (long long)excl;
   }
   __syncthreads();
-  // stage in digit order
+  // 4. stage in digit order (the tile is re-read from L1/L2)
 #pragma unroll
   for (int r = 0; r < KD_RS_ROUNDS; ++r) {
     const long long i = base + r * 32 + lane;
     if (i < a.n) {
-      const unsigned d = a.from_key ? (kk[r] >> shift) & 255u : (unsigned)(kv[r] >> shift) & 255u;
-      const unsigned lp = blk_off[d] + wcnt[warp][d] + rank[r];
-      sk[lp] = kv[r];
-      skey[lp] = kk[r];
+      const unsigned d = dig[r];
+      const unsigned rk = (rank2[r >> 1] >> ((r & 1) * 16)) & 0xffffu;
+      const unsigned lp = blk_off[d] + wcnt[warp][d] + rk;
+      const uint64_t kvv = a.kin[i];
+      const uint32_t kkv = a.keyin[i];
+      sk[lp] = kvv;
+      skey[lp] = kkv;
       if (kIdx) sidx[lp] = a.idxin[i];
     }
   }
   __syncthreads();
-  // coalesced write-out of digit runs
+  // 5. coalesced write-out of digit runs
   const int cnt = (int)min((long long)KD_RS_TILE, a.n - tile0);
   for (int i = threadIdx.x; i < cnt; i += KD_RS_THREADS) {
     const uint64_t v = sk[i];
