@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -1218,8 +1219,11 @@ static size_t tile_smem() { return sizeof(WarpTile); }
 static size_t tile_smem_small() { return sizeof(WarpTileSmall) * 4; }
 
 int kd_pipeline_prepare_device(KdSession* s) {
-  static bool done = false;
-  if (done) return KD_OK;
+  // Function attributes are per device: remember which devices are set up.
+  // Setting them twice (two threads racing here) is harmless.
+  static std::atomic<bool> done[64];
+  std::atomic<bool>* flag = (s->device >= 0 && s->device < 64) ? &done[s->device] : nullptr;
+  if (flag && flag->load(std::memory_order_acquire)) return KD_OK;
   KD_CK(cudaFuncSetAttribute(k_tiles<KD_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem()));
   KD_CK(cudaFuncSetAttribute(kd_rs_onesweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kd_rs_smem(true)));
@@ -1227,7 +1231,7 @@ int kd_pipeline_prepare_device(KdSession* s) {
                              (int)kd_rs_smem(false)));
   KD_CK(cudaFuncSetAttribute(k_tiles<KD_SERIAL_TILE_MAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)tile_smem_small()));
-  done = true;
+  if (flag) flag->store(true, std::memory_order_release);
   return KD_OK;
 }
 
