@@ -132,6 +132,28 @@ KD_API int kd_store_stats(kd_store* st, int64_t* num_keys, int64_t* total_centro
  * for all keys at once (grouped.mojo:182-185). */
 KD_API int kd_store_counts(kd_store* st, int32_t* out, int flags);
 
+/* No counterpart in the reference.  kd_compress for callers that cannot call
+ * cudaMalloc: a host program whose own pool owns all device memory (memory taken
+ * behind its back is unaccounted and may not exist), or a latency-critical loop
+ * where cudaMalloc/cudaFree would synchronise the device.  Same arguments and
+ * results as kd_compress, without a session: work runs on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream) of the current device, and
+ * the call returns once that work is done.  It allocates nothing: its working
+ * memory is one fixed device array of KD_NOALLOC_SCRATCH_BYTES in the library,
+ * held on every GPU that loads the library until the process exits.
+ * n > KD_NOALLOC_MAX_N returns KD_ERANGE with *out_n = 0.  The first call on a
+ * device resolves that array's address and sets kernel attributes; make it
+ * before any stream capture.  All calls on a device share the array (it keeps
+ * the last call's contents; each call clears what must start at zero), so calls
+ * whose GPU work overlaps race and give wrong results.  On failure, msg (may be
+ * NULL) receives up to msg_cap bytes of text. */
+#define KD_NOALLOC_MAX_N 16384
+#define KD_NOALLOC_SCRATCH_BYTES (2 * 1024 * 1024)
+KD_API int kd_compress_noalloc(int scale, double compression, const double* means,
+                               const double* weights, int64_t n, int flags, double* out_means,
+                               double* out_weights, int64_t cap, int64_t* out_n, void* stream,
+                               char* msg, int msg_cap);
+
 #ifdef __cplusplus
 }
 #endif

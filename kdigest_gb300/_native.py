@@ -27,7 +27,7 @@ EXPORTED = (
     "kd_compress", "kd_store_create", "kd_store_destroy", "kd_store_ingest",
     "kd_store_quantile", "kd_store_cdf", "kd_store_merge", "kd_store_get_digest",
     "kd_store_set_digest", "kd_store_to_bytes", "kd_store_from_bytes", "kd_store_stats",
-    "kd_store_counts",
+    "kd_store_counts", "kd_compress_noalloc",
 )
 
 _P = ctypes.c_void_p
@@ -83,6 +83,8 @@ def load(path: str = LIB_PATH):
     L.kd_store_to_bytes.argtypes = [_P, ctypes.c_uint32, _P, _I64, ctypes.POINTER(_I64)]
     L.kd_store_from_bytes.argtypes = [_P, ctypes.c_uint32, _P, _I64]
     L.kd_store_counts.argtypes = [_P, _P, ctypes.c_int]
+    L.kd_compress_noalloc.argtypes = [ctypes.c_int, _D, _P, _P, _I64, ctypes.c_int, _P, _P, _I64,
+                                      ctypes.POINTER(_I64), _P, ctypes.c_char_p, ctypes.c_int]
     L.kd_store_stats.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                  ctypes.POINTER(ctypes.c_size_t)]
     _lib = L
