@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <vector>
 
@@ -60,13 +61,31 @@ struct WarpTileT {
   // after the segment pass: the weight sum of each segment at its end element
   double L[SLOTS];
   double P[32];                  // exclusive prefix of the chunk totals (bits)
+  // hf/ef also hold a list of up to CAP tile positions (unsigned short) while
+  // they are free: the elements left to the FP64 bucket path, then the
+  // segments whose mean needs a division.
   unsigned char hf[SLOTS];       // head flags
   unsigned char ef[SLOTS];       // end flags
-  unsigned short headpos[CAP];   // tile position of the first element of segment s
+  // headpos/endpos also hold the bucket id (int) of every element until the
+  // head pass, which writes headpos[k] only after id k has been read.
+  alignas(8) unsigned short headpos[CAP];  // tile position of the first element of segment s
   unsigned short endpos[CAP];    // tile position of the last element of segment s
+
+  __device__ unsigned short* poslist() { return reinterpret_cast<unsigned short*>(hf); }
+  __device__ int* ids() { return reinterpret_cast<int*>(headpos); }
 };
 typedef WarpTileT<KD_TILE> WarpTile;
 typedef WarpTileT<KD_SERIAL_TILE_MAX> WarpTileSmall;
+static_assert(offsetof(WarpTile, ef) == offsetof(WarpTile, hf) + WarpTile::SLOTS &&
+                  2 * WarpTile::SLOTS >= 2 * KD_TILE,
+              "position list overlays hf/ef");
+static_assert(offsetof(WarpTileSmall, ef) == offsetof(WarpTileSmall, hf) + WarpTileSmall::SLOTS &&
+                  2 * WarpTileSmall::SLOTS >= 2 * KD_SERIAL_TILE_MAX,
+              "position list overlays hf/ef");
+static_assert(offsetof(WarpTile, endpos) == offsetof(WarpTile, headpos) + 2 * KD_TILE &&
+                  offsetof(WarpTileSmall, endpos) ==
+                      offsetof(WarpTileSmall, headpos) + 2 * KD_SERIAL_TILE_MAX,
+              "bucket ids overlay headpos/endpos");
 
 // Integral weight in [1, 2^42): a tile of such weights has every partial sum
 // exact in FP64 (total < 2^52), so int64 arithmetic reproduces the canonical
@@ -97,6 +116,9 @@ struct TileAcc<false> {
   __device__ static double to_d(T v) { return v; }
   __device__ static float to_f(T v) { return kd_d2f_trunc(v); }
   __device__ static bool is_zero(T v) { return ((unsigned long long)__double_as_longlong(v) << 1) == 0; }
+  // exact comparisons (positive finite operands): a == b, and 2a == b (doubling is exact)
+  __device__ static bool eq(T a, T b) { return __double_as_longlong(a) == __double_as_longlong(b); }
+  __device__ static bool is_half(T a, T b) { return __double_as_longlong(KD_ADD(a, a)) == __double_as_longlong(b); }
   __device__ static double store(T v) { return v; }
   __device__ static T load(double v) { return v; }
 };
@@ -111,6 +133,8 @@ struct TileAcc<true> {
   __device__ static double to_d(T v) { return (double)v; }
   __device__ static float to_f(T v) { return kd_i2f_trunc(v); }
   __device__ static bool is_zero(T v) { return v == 0; }
+  __device__ static bool eq(T a, T b) { return a == b; }
+  __device__ static bool is_half(T a, T b) { return a + a == b; }
   __device__ static double store(T v) { return __longlong_as_double(v); }
   __device__ static T load(double v) { return __double_as_longlong(v); }
 };
@@ -136,7 +160,8 @@ __device__ __forceinline__ unsigned tile_inv(int E) {
 // (n <= KD_SERIAL_TILE_MAX) both reduce to plain serial sums.
 template <bool kInt, int CAP>
 __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compression,
-                             int force_exact, double* __restrict__ om, double* __restrict__ ow) {
+                             int force_exact, int32_t id_last, double* __restrict__ om,
+                             double* __restrict__ ow) {
   typedef TileAcc<kInt> A;
   typedef typename A::T T;
   const int lane = threadIdx.x & 31;
@@ -176,51 +201,75 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
   __syncwarp();
   const KFilterTile ft = kfilter_tile(scale, compression, kInt ? A::to_f(tot) : kd_d2f_trunc(totd));
 
-  // 3. Bucket ids, 32 consecutive elements per round; heads compacted by ballot.
-  double nrm64 = 0.0;
-  bool have_nrm = false;
+  // 3a. Bucket ids of all elements in independent rounds.  Exact shortcuts
+  //     first: q == 1/2 gives k == 0 exactly for K1..K3 (asin(0), log(1)), and
+  //     the last element of a K0/K1 tile (q == 1) has the launch constant
+  //     id_last.  Then the FP32 filter; positions it cannot resolve go to a
+  //     list for the FP64 path.
+  int* const ids = t.ids();
+  unsigned short* const plist = t.poslist();
+  const unsigned lt_mask = (1u << lane) - 1u;
+  int nneed = 0;
+  for (int r0 = 0; r0 < n; r0 += 32) {
+    const int p = r0 + lane;
+    bool need = false;
+    if (p < n) {
+      const int c = (int)(((unsigned)p * inv) >> 16);
+      const int slot = c * SE + (p - c * E);
+      const T Lp = A::load(t.L[slot]);
+      const T cum = c == 0 ? Lp : A::add(A::load(t.P[c]), Lp);
+      int32_t id = 0;
+      bool ok = false;
+      if (!force_exact) {
+        const bool rz = A::eq(cum, tot);
+        if (scale != KD_SCALE_K0 && A::is_half(cum, tot)) {
+          ok = true;  // q == 1/2: id 0
+        } else if (rz && scale <= KD_SCALE_K1) {
+          id = id_last;
+          ok = true;
+        } else {
+          const float q = A::to_f(cum) / ft.t32;
+          const float r = q > 0.25f ? A::to_f(A::sub(tot, cum)) / ft.t32 : 1.f - q;
+          ok = kfilter_id(scale, ft, q, r, rz, &id);
+        }
+      }
+      ids[p] = id;
+      need = !ok;
+    }
+    const unsigned nb = __ballot_sync(0xffffffffu, need);
+    if (need) plist[nneed + __popc(nb & lt_mask)] = (unsigned short)p;
+    nneed += __popc(nb);
+  }
+  __syncwarp();
+  // 3b. The FP64 path for the listed positions, 32 at a time.
+  if (nneed > 0) {
+    const double nrm64 = kd_normalizer(scale, compression, totd);
+    for (int k = lane; k < nneed; k += 32) {
+      const int p = plist[k];
+      const int c = (int)(((unsigned)p * inv) >> 16);
+      const int slot = c * SE + (p - c * E);
+      const T Lp = A::load(t.L[slot]);
+      const T cum = c == 0 ? Lp : A::add(A::load(t.P[c]), Lp);
+      ids[p] = kd_bucket(scale, A::to_d(cum), totd, nrm64);
+    }
+  }
+  __syncwarp();
+  // 3c. Heads (an id change or the first element), compacted by ballot.  Writing
+  //     headpos[k] (k <= p) only clobbers ids of elements already read.
   int32_t carry_id = 0;
   int nheads = 0;
-  const unsigned lt_mask = (1u << lane) - 1u;
   for (int r0 = 0; r0 < n; r0 += 32) {
     const int p = r0 + lane;
     const bool act = p < n;
-    T cum = 0;
-    int32_t id = 0;
-    bool ok = true;
-    int slot = 0;
-    if (act) {
-      const int c = (int)(((unsigned)p * inv) >> 16);
-      slot = c * SE + (p - c * E);
-      const T Lp = A::load(t.L[slot]);
-      cum = c == 0 ? Lp : A::add(A::load(t.P[c]), Lp);
-      const float q = A::to_f(cum) / ft.t32;
-      float r;
-      bool rz = false;
-      if (q > 0.25f) {
-        const T rem = A::sub(tot, cum);
-        rz = A::is_zero(rem);
-        r = A::to_f(rem) / ft.t32;
-      } else {
-        r = 1.f - q;
-      }
-      ok = !force_exact && kfilter_id(scale, ft, q, r, rz, &id);
-    }
-    const bool need = act && !ok;
-    if (__any_sync(0xffffffffu, need)) {
-      if (!have_nrm) {
-        nrm64 = kd_normalizer(scale, compression, totd);
-        have_nrm = true;
-      }
-      if (need) id = kd_bucket(scale, A::to_d(cum), totd, nrm64);
-    }
+    const int32_t id = act ? ids[p] : 0;
     int32_t prev = __shfl_up_sync(0xffffffffu, id, 1);
     if (lane == 0) prev = carry_id;
     const bool head = act && (p == 0 || id != prev);
     const unsigned hb = __ballot_sync(0xffffffffu, head);
+    carry_id = __shfl_sync(0xffffffffu, id, 31);
+    __syncwarp();
     if (head) t.headpos[nheads + __popc(hb & lt_mask)] = (unsigned short)p;
     nheads += __popc(hb);
-    carry_id = __shfl_sync(0xffffffffu, id, 31);
   }
   __syncwarp();
   const int total_out = nheads;
@@ -232,6 +281,11 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
     for (int sI = lane; sI < total_out; sI += 32) {
       const int h = t.headpos[sI];
       const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
+      t.endpos[sI] = (unsigned short)e;
+      if (h == e) {  // a single element: its weight; its mean is its value
+        t.L[e] = A::store(A::from_w(t.w[e]));
+        continue;
+      }
       T aw = A::from_w(t.w[h]);
       double awx = KD_MUL(t.w[h], t.x[h]);
       for (int i = h + 1; i <= e; ++i) {
@@ -239,7 +293,6 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
         aw = A::add(aw, A::from_w(wi));
         awx = KD_ADD(awx, KD_MUL(wi, t.x[i]));
       }
-      t.endpos[sI] = (unsigned short)e;
       t.L[e] = A::store(aw);
       t.w[e] = awx;
     }
@@ -319,27 +372,48 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
   }
   __syncwarp();
 
-  // 5. Centroids, 32 at a time: mean = sum(wx) / sum(w) clamped to the
-  //    segment's [first, last] value (add_batch.mojo:205-218).  A segment whose
-  //    first and last values are equal needs no division: the clamp yields it.
-  for (int sI = lane; sI < total_out; sI += 32) {
+  // 5. Centroids: mean = sum(wx) / sum(w) clamped to the segment's [first,
+  //    last] value (add_batch.mojo:205-218).  A segment whose first and last
+  //    values are equal needs no division (the clamp yields that value); the
+  //    others are listed and divided 32 at a time with every lane busy.
+  unsigned short* const dlist = t.poslist();
+  int ndiv = 0;
+  for (int s0 = 0; s0 < total_out; s0 += 32) {
+    const int sI = s0 + lane;
+    bool div = false;
+    if (sI < total_out) {
+      const int e = t.endpos[sI];
+      const int h = t.headpos[sI];
+      const int se = tile_slot(e, E, SE, inv), sh = tile_slot(h, E, SE, inv);
+      const double sw = A::to_d(A::load(t.L[se]));
+      const double lo_v = t.x[sh], hi_v = t.x[se];
+      ow[sI] = sw;
+      if (__double_as_longlong(lo_v) == __double_as_longlong(hi_v)) {
+        om[sI] = lo_v;
+      } else if (!(__double_as_longlong(sw) > 0)) {  // zero weight: 0, clamped
+        const uint64_t k0 = kd_order_key(0.0);
+        om[sI] = k0 < kd_order_key(lo_v) ? lo_v : (k0 > kd_order_key(hi_v) ? hi_v : 0.0);
+      } else {
+        div = true;
+      }
+    }
+    const unsigned db = __ballot_sync(0xffffffffu, div);
+    if (div) dlist[ndiv + __popc(db & lt_mask)] = (unsigned short)sI;
+    ndiv += __popc(db);
+  }
+  __syncwarp();
+  for (int k = lane; k < ndiv; k += 32) {
+    const int sI = dlist[k];
     const int e = t.endpos[sI];
     const int h = t.headpos[sI];
     const int se = tile_slot(e, E, SE, inv), sh = tile_slot(h, E, SE, inv);
     const double sw = A::to_d(A::load(t.L[se]));
-    const double swx = t.w[se];
     const double lo_v = t.x[sh], hi_v = t.x[se];
-    double mean;
-    if (__double_as_longlong(lo_v) == __double_as_longlong(hi_v)) {
-      mean = lo_v;
-    } else {
-      mean = __double_as_longlong(sw) > 0 ? KD_DIV(swx, sw) : 0.0;
-      const uint64_t km = kd_order_key(mean);
-      if (km < kd_order_key(lo_v)) mean = lo_v;
-      else if (km > kd_order_key(hi_v)) mean = hi_v;
-    }
+    double mean = KD_DIV(t.w[se], sw);
+    const uint64_t km = kd_order_key(mean);
+    if (km < kd_order_key(lo_v)) mean = lo_v;
+    else if (km > kd_order_key(hi_v)) mean = hi_v;
     om[sI] = mean;
-    ow[sI] = sw;
   }
   __syncwarp();
   return total_out;
@@ -697,6 +771,7 @@ struct TileArgs {
   long long cap_inter;
   int* needs;
   int force_exact;
+  int id_last;  // bucket id at q == 1 for K0/K1 (a launch constant)
   KdErrHost* err;
 };
 
@@ -773,8 +848,10 @@ __global__ void __launch_bounds__(32 * (CAP == KD_TILE ? 1 : 4)) k_tiles(TileArg
     __syncwarp();
     const TileOut o = tile_out(a, ai, lt, j, m);
     const int c = integral
-                      ? warp_compress<true, CAP>(t, n, s.scale, s.compression, a.force_exact, o.m, o.w)
-                      : warp_compress<false, CAP>(t, n, s.scale, s.compression, a.force_exact, o.m, o.w);
+                      ? warp_compress<true, CAP>(t, n, s.scale, s.compression, a.force_exact,
+                                                 a.id_last, o.m, o.w)
+                      : warp_compress<false, CAP>(t, n, s.scale, s.compression, a.force_exact,
+                                                  a.id_last, o.m, o.w);
     if (lane == 0) *o.count = c;
   }
 }
@@ -1257,6 +1334,11 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
       if (T.enabled) cudaEventRecord(T.ev[i], str);
     };
     const int key_bits = key_bits_for(sd.K);
+    // K0/K1 normalisers do not depend on the tile total, so the id of q == 1
+    // is one constant per launch (host FP64, same arithmetic as the device).
+    const int id_last = sd.scale <= KD_SCALE_K1
+                            ? (int)kd_bucket(sd.scale, 1.0, 1.0, kd_normalizer(sd.scale, sd.compression, 1.0))
+                            : 0;
     long long launches = 0;
     mark(0);
     {
@@ -1309,7 +1391,8 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
     mark(3);
     auto launch_tiles = [&](const KdLevelDev& lv, const double* dx, const double* dw) {
       TileArgs ta{sd, lv.Tl, lv.Ts, lv.I, lv, dx, dw, w.tkey, w.tbuf, w.st_count, w.scr_m,
-                  w.scr_w, w.tcount, w.cap_work, w.cap_inter, w.needs, s->force_exact, w.err};
+                  w.scr_w, w.tcount, w.cap_work, w.cap_inter, w.needs, s->force_exact, id_last,
+                  w.err};
       k_tiles<KD_TILE><<<level_grid(s), 32, tile_smem(), str>>>(ta);
       k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * 8, 128, tile_smem_small(), str>>>(ta);
       launches += 2;
