@@ -53,6 +53,8 @@ def make_workload(seed: int = SEED, num_keys: int = NUM_KEYS, total: int = TOTAL
     cdf /= cdf[-1]
     perm = rng.permutation(num_keys).astype(np.uint32)
     mu = rng.uniform(-100.0, 100.0, num_keys)
+    if total <= 0 or total % batch:
+        raise ValueError(f"stream length {total} is not a positive multiple of the batch {batch}")
     nb = total // batch
     keys = np.empty(total, np.uint32)
     vals = np.empty(total, np.float64)
@@ -207,6 +209,26 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------------------
+# Replicas (N > 1): every rank ingests its own copy of the stream on its own
+# GPU; no collective touches the data path.
+# ----------------------------------------------------------------------------
+def max_over_ranks(dist, value: float, device=None) -> float:
+    """The slowest rank's time (the timed region ends when every rank is done)."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world: int, steps: int, batch: int, max_total_ms: float) -> float:
+    """Whole-job samples/s: the samples of all ranks over the slowest rank's time."""
+    return world * steps * batch / (max_total_ms / 1e3)
+
+
+# ----------------------------------------------------------------------------
 # GPU arm
 # ----------------------------------------------------------------------------
 def run_gpu(args):
@@ -286,12 +308,8 @@ def run_gpu(args):
     st = sess.stats()
     step_ms = sum(times) / len(times)
     local_total_ms = sum(times)
-    total_ms = local_total_ms
-    if dist:
-        t = torch.tensor([local_total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps * BATCH / (total_ms / 1e3)
+    total_ms = max_over_ranks(dist, local_total_ms, dev)
+    value = replica_value(world, args.steps, BATCH, total_ms)
 
     # Queries: 7 quantiles for every key, one launch, device pointers.
     qk = torch.arange(NUM_KEYS, dtype=torch.int32, device=dev).repeat_interleave(len(QUANTILES)).contiguous()
