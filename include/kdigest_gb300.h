@@ -56,6 +56,7 @@ extern "C" {
 #define KD_OPT_FORCE_EXACT_K 1 /* evaluate every bucket id in FP64 (no FP32 filter) */
 #define KD_OPT_MAX_LEVELS 2    /* cap on tile-hierarchy levels per ingest (default 32) */
 #define KD_OPT_STAGE_TIMING 3  /* record CUDA events between ingest stages */
+#define KD_OPT_GRAPHS 4        /* capture repeated ingest steps as CUDA graphs (default on) */
 
 typedef struct kd_session kd_session;
 typedef struct kd_store kd_store;

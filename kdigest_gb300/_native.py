@@ -17,7 +17,7 @@ KD_OK, KD_EINVAL, KD_EEMPTY, KD_ERANGE, KD_ECONVERGE, KD_ENOMEM, KD_ECUDA, KD_ET
 KD_K0, KD_K1, KD_K2, KD_K3 = 0, 1, 2, 3
 KD_CLOCK_COUNT, KD_CLOCK_TIME = 0, 1
 KD_PTR_DEVICE = 1
-KD_OPT_FORCE_EXACT_K, KD_OPT_MAX_LEVELS, KD_OPT_STAGE_TIMING = 1, 2, 3
+KD_OPT_FORCE_EXACT_K, KD_OPT_MAX_LEVELS, KD_OPT_STAGE_TIMING, KD_OPT_GRAPHS = 1, 2, 3, 4
 STAGES = ("prep", "sort", "plan", "level0", "levels", "commit")
 
 EXPORTED = (

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -67,10 +68,10 @@ void kd_ws_free(KdWorkspace& w) {
                   w.tkey, w.tstart, w.tm, w.tprior, w.tbuf, w.tsf, w.tpscale, w.tmap,
                   w.st_clock, w.st_ls, w.st_min, w.st_max, w.st_count, w.lv_storage,
                   w.work[0], w.work[1], w.work[2], w.work[3], w.dx[0], w.dx[1], w.dw[0], w.dw[1], w.scr_m, w.scr_w,
-                  w.tcount, w.doff, w.needs, w.totals, w.err};
+                  w.tcount, w.doff, w.needs, w.totals, w.d_call, w.rs_epoch_base};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  if (w.h_err) cudaFreeHost(w.h_err);
+  if (w.h_call) cudaFreeHost(w.h_call);
   if (w.h_scalars) cudaFreeHost(w.h_scalars);
   if (w.h_stage) cudaFreeHost(w.h_stage);
   // the host-call staging buffer is owned separately (stage_in / session destroy)
@@ -92,6 +93,7 @@ static size_t ws_bytes(long long n, long long keys, long long inter, long long w
   b += (size_t)work * 8 * 4;
   b += (size_t)merged * 16 * 2;
   b += (size_t)inter * (KD_TILE * 16 + 8);
+  b += sizeof(KdCallArgs) + sizeof(unsigned);
   return b;
 }
 
@@ -146,10 +148,12 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
   ok &= A((void**)&w.ghist, sizeof(unsigned) * KD_RS_MAXPASS * 256);
   ok &= A((void**)&w.rs_state, sizeof(unsigned long long) * 256 * (size_t)kd_rs_blocks(nn));
   ok &= A((void**)&w.rs_ticket, sizeof(unsigned long long));
+  ok &= A((void**)&w.rs_epoch_base, sizeof(unsigned));
   if (ok) {
     cudaMemset(w.rs_state, 0, sizeof(unsigned long long) * 256 * (size_t)kd_rs_blocks(nn));
+    cudaMemset(w.rs_epoch_base, 0, sizeof(unsigned));
     w.cap_rs_tiles = kd_rs_blocks(nn);
-    w.rs_epoch = 0;
+    w.rs_epochs_used = 0;
   }
   ok &= A((void**)&w.partials, sizeof(int4) * parts);
   ok &= A((void**)&w.tkey, sizeof(uint32_t) * kk);
@@ -172,13 +176,17 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
   ok &= A((void**)&w.doff, sizeof(int) * (ii + 1));
   ok &= A((void**)&w.needs, sizeof(int) * 4);
   ok &= A((void**)&w.totals, sizeof(int4) * 8);
-  ok &= A((void**)&w.err, sizeof(KdErrHost));
-  ok &= cudaHostAlloc((void**)&w.h_err, sizeof(KdErrHost), cudaHostAllocDefault) == cudaSuccess;
+  ok &= A((void**)&w.d_call, sizeof(KdCallArgs));
+  ok &= cudaHostAlloc((void**)&w.h_call, sizeof(KdCallArgs), cudaHostAllocDefault) == cudaSuccess;
   ok &= cudaHostAlloc((void**)&w.h_scalars, 64 * sizeof(int), cudaHostAllocDefault) == cudaSuccess;
   if (!ok) {
     kd_ws_free(w);
     return fail(s, KD_ENOMEM, "workspace allocation failed");
   }
+  w.err = &w.d_call->err;
+  w.h_err = &w.h_call->err;
+  static std::atomic<unsigned long long> generations{0};
+  w.generation = ++generations;  // buffers moved: captured graphs are stale
   int* lvp = w.lv_storage;
   for (int i = 0; i < 2; ++i) {
     KdLevelDev& L = w.lv[i];
@@ -281,7 +289,16 @@ int kd_store_alloc(KdSession* s, KdStore* st) {
   return KD_OK;
 }
 
+void kd_store_drop_graphs(KdStore* st) {
+  for (KdGraphEntry& g : st->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = KdGraphEntry();
+  }
+  st->last_eager = KdGraphKey();
+}
+
 void kd_store_free(KdStore* st) {
+  kd_store_drop_graphs(st);
   KdStoreDev& d = st->d;
   void* p[] = {d.slot_m, d.slot_w, d.prefix, d.cur, d.count, d.total, d.log_scale, d.clock,
                d.min_v, d.max_v, d.dfac};
@@ -415,6 +432,8 @@ KD_API int kd_session_set_option(kd_session* h, int option, int value) {
   else if (option == KD_OPT_MAX_LEVELS) {
     if (value < 1 || value > 64) return fail(s, KD_EINVAL, "max levels must be in [1, 64]");
     s->max_levels = value;
+  } else if (option == KD_OPT_GRAPHS) {
+    s->use_graphs = value ? 1 : 0;
   } else {
     return fail(s, KD_EINVAL, "unknown option");
   }

@@ -37,6 +37,21 @@ struct KdErrHost {
   long long index;
 };
 
+// Per-call inputs of an ingest, read by the kernels from device memory so that a
+// captured ingest graph replays with new inputs: one copy (pinned host block ->
+// device block) at the head of the step refreshes them together with the
+// initial status word.
+struct KdCallArgs {
+  const uint32_t* keys;
+  const double* vals;
+  const double* wts;
+  const double* merge_min;
+  const double* merge_max;
+  const double* merge_clock;
+  double timestamp;
+  KdErrHost err;  // the step's status word (device copy: KdWorkspace::err)
+};
+
 // Per-level plan of the P-path hierarchy.  Level 0 holds every touched key;
 // level L >= 1 holds the keys whose input exceeded one tile at level L-1.  The
 // input of a level is a dense array (means, weights): key a owns
@@ -70,7 +85,8 @@ struct KdWorkspace {
   unsigned long long* rs_state = nullptr; // look-back words, 256 per sort tile
   unsigned long long* rs_ticket = nullptr;
   long long cap_rs_tiles = 0;
-  unsigned rs_epoch = 0;
+  unsigned* rs_epoch_base = nullptr;        // device epoch base of the look-back words
+  unsigned long long rs_epochs_used = 0;     // host bookkeeping of that base
   int4* partials = nullptr;
   long long cap_partials = 0;
   // touched keys
@@ -109,9 +125,12 @@ struct KdWorkspace {
   int* needs = nullptr;  // device: required (work, merged, inter) capacities
   // scalars: U, T0, I0, A1 ... (int4 totals)
   int4* totals = nullptr;
-  KdErrHost* err = nullptr;   // device
-  KdErrHost* h_err = nullptr; // pinned host mirror
+  KdCallArgs* d_call = nullptr;  // device per-call block (err lives inside it)
+  KdCallArgs* h_call = nullptr;  // pinned host mirror
+  KdErrHost* err = nullptr;   // device: &d_call->err
+  KdErrHost* h_err = nullptr; // pinned host: &h_call->err
   int* h_scalars = nullptr;   // pinned host scalars
+  unsigned long long generation = 0;  // bumped whenever buffers move (graphs bake pointers)
   // host staging (pinned) for host-pointer inputs / outputs
   void* h_stage = nullptr;
   size_t h_stage_bytes = 0;
@@ -137,17 +156,47 @@ struct KdSession {
   int num_sms = 0;
   int force_exact = 0;
   int max_levels = 32;
+  int use_graphs = 1;  // capture repeated ingest steps as CUDA graphs
   char last_error[256] = {0};  // fixed buffer: reporting an error never allocates
   KdWorkspace ws;
   KdStageStats stats;
   struct KdStore* scratch_store = nullptr;  // 1-key store for stateless compress
 };
 
+// What a captured ingest step depends on besides the per-call block: launch
+// shapes, kernel arguments that are baked in, and the buffers.
+struct KdGraphKey {
+  long long n = -1;
+  int key_bits = 0, with_idx = 0, mode = 0, levels = 0, force_exact = 0, timing = 0;
+  int scale = 0;
+  double compression = 0.0;
+  unsigned long long generation = 0;
+  bool operator==(const KdGraphKey& o) const {
+    return n == o.n && key_bits == o.key_bits && with_idx == o.with_idx && mode == o.mode &&
+           levels == o.levels && force_exact == o.force_exact && timing == o.timing &&
+           scale == o.scale && compression == o.compression && generation == o.generation;
+  }
+};
+struct KdGraphEntry {
+  KdGraphKey key;
+  cudaGraphExec_t exec = nullptr;
+  // host view after the captured levels (for an eager continuation)
+  const int* curA = nullptr;
+  const int* Iprev = nullptr;
+  long long launches = 0;
+};
+#define KD_GRAPH_CACHE 4
+
 struct KdStore {
   KdSession* sess = nullptr;
   KdStoreDev d{};
   size_t bytes = 0;
   int levels_hint = 3;  // hierarchy levels >= 1 the last ingest needed
+  // Ingest steps captured as CUDA graphs: a step shape seen twice in a row is
+  // captured, later steps of that shape replay it.
+  KdGraphEntry graphs[KD_GRAPH_CACHE];
+  int graph_next = 0;
+  KdGraphKey last_eager;
 };
 
 // Pipeline entry points (kd_pipeline.cu).  All work is enqueued on sess->stream.
@@ -167,6 +216,7 @@ void kd_store_free(KdStore* st);
 int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, long long work,
                   long long merged, long long tmap);
 void kd_ws_free(KdWorkspace& ws);
+void kd_store_drop_graphs(KdStore* st);
 int kd_cuda_fail(KdSession* s, cudaError_t e, const char* what);
 void kd_set_msg(KdSession* s, const char* msg);
 // One-time kernel attributes (shared-memory opt-ins); no allocation.

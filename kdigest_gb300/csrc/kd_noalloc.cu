@@ -85,6 +85,7 @@ size_t carve(uintptr_t base, KdWorkspace& w, KdStoreDev& d, double** stage) {
   w.cap_rs_tiles = kd_rs_blocks(kN);
   w.rs_state = c.take<unsigned long long>(256 * w.cap_rs_tiles);
   w.rs_ticket = c.take<unsigned long long>(1);
+  w.rs_epoch_base = c.take<unsigned>(1);
   w.cap_partials = kd_scan_partials_needed(kN) + 4;
   w.partials = c.take<int4>(w.cap_partials);
   w.tkey = c.take<uint32_t>(kKeys);
@@ -107,7 +108,8 @@ size_t carve(uintptr_t base, KdWorkspace& w, KdStoreDev& d, double** stage) {
   w.doff = c.take<int>(kInter + 1);
   w.needs = c.take<int>(4);
   w.totals = c.take<int4>(8);
-  w.err = c.take<KdErrHost>(1);
+  w.d_call = c.take<KdCallArgs>(1);
+  w.err = &w.d_call->err;
   // Per level: eight per-key arrays, then five device scalars per level.
   for (int i = 0; i < 2; ++i) {
     KdLevelDev& L = w.lv[i];
@@ -135,7 +137,7 @@ size_t carve(uintptr_t base, KdWorkspace& w, KdStoreDev& d, double** stage) {
   w.cap_work = kWork;
   w.cap_merged = kMerged;
   w.cap_tmap = 1;
-  w.rs_epoch = 0;
+  w.rs_epochs_used = 0;
   // The 1-key store: two centroid slots, the quantile prefix and a 64-byte
   // header block (cur, count, total, log_scale, clock, min, max, dfac).
   d.K = 1;
@@ -240,6 +242,7 @@ KD_API int kd_compress_noalloc(int scale, double compression, const double* mean
 
   KdSession s;  // plain host object on the stack: no device or heap memory
   s.device = dev;
+  s.use_graphs = 0;  // instantiating a CUDA graph would allocate
   s.stream = (cudaStream_t)stream;
   s.num_sms = g_dev[dev].num_sms;
   KdStore st;
@@ -250,16 +253,19 @@ KD_API int kd_compress_noalloc(int scale, double compression, const double* mean
   st.d.scale = scale;
   st.d.compression = compression;
   st.d.lambda = 0.0;
-  KdErrHost h_err{};
+  KdCallArgs h_call{};
   int h_scalars[64] = {};
-  w.h_err = &h_err;
+  w.h_call = &h_call;
+  w.h_err = &h_call.err;
   w.h_scalars = h_scalars;
 
   cudaStream_t str = s.stream;
   // What must start at zero: the store header (slot selector, counts) and the
-  // sort's look-back words, whose epoch count restarts at zero every call.
+  // sort's look-back words with their epoch base, whose count restarts at zero
+  // every call.
   KD_NA_CK(cudaMemsetAsync(st.d.cur, 0, 64, str));
   KD_NA_CK(cudaMemsetAsync(w.rs_state, 0, sizeof(unsigned long long) * 256 * (size_t)w.cap_rs_tiles, str));
+  KD_NA_CK(cudaMemsetAsync(w.rs_epoch_base, 0, sizeof(unsigned), str));
   const double* dm = means;
   const double* dw = weights;
   if (!(flags & KD_PTR_DEVICE)) {

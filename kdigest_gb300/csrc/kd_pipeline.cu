@@ -422,9 +422,12 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
 // ---------------------------------------------------------------------------
 // Stage kernels
 // ---------------------------------------------------------------------------
-__global__ void k_prep(long long n, const uint32_t* __restrict__ keys, const double* __restrict__ vals,
-                       const double* __restrict__ wts, long long K, uint64_t* __restrict__ k64,
-                       uint32_t* __restrict__ kout, uint32_t* __restrict__ idx, KdErrHost* err) {
+__global__ void k_prep(long long n, const KdCallArgs* __restrict__ call, long long K,
+                       uint64_t* __restrict__ k64, uint32_t* __restrict__ kout,
+                       uint32_t* __restrict__ idx, KdErrHost* err) {
+  const uint32_t* __restrict__ keys = call->keys;
+  const double* __restrict__ vals = call->vals;
+  const double* __restrict__ wts = call->wts;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const uint32_t key = keys ? keys[i] : 0u;
@@ -475,10 +478,7 @@ struct PrepareArgs {
   const int* tstart;
   const int4* totals;
   int mode;
-  double timestamp;
-  const double* merge_min;
-  const double* merge_max;
-  const double* merge_clock;
+  const KdCallArgs* call;  // timestamp and merge inputs
   int* tm;
   int* tprior;
   unsigned char* tbuf;
@@ -514,9 +514,9 @@ __global__ void k_prepare(PrepareArgs a) {
     prior = 0;
     ls = 0.0;
     if (a.mode == KD_MODE_MERGE) {
-      mn = a.merge_min[key];
-      mx = a.merge_max[key];
-      clock = a.merge_clock[key];
+      mn = a.call->merge_min[key];
+      mx = a.call->merge_max[key];
+      clock = a.call->merge_clock[key];
     } else {
       mn = vmin;
       mx = vmax;
@@ -529,8 +529,8 @@ __global__ void k_prepare(PrepareArgs a) {
     if (a.mode == KD_MODE_COUNT) {
       new_clock = KD_ADD(clock, (double)nn);
       advance = true;
-    } else if (a.timestamp > clock) {
-      new_clock = a.timestamp;
+    } else if (a.call->timestamp > clock) {
+      new_clock = a.call->timestamp;
       advance = true;
     }
     if (advance) {
@@ -662,7 +662,7 @@ struct MergeArgs {
   const uint64_t* k64;
   const uint32_t* skey;
   const uint32_t* sidx;
-  const double* wts;
+  const KdCallArgs* call;  // per-sample weights (or null: unit weights)
   const uint32_t* tkey;
   const uint32_t* tmap;
   const int* tstart;
@@ -715,7 +715,8 @@ __global__ void k_merge_new(MergeArgs a) {
     }
     const long long pos = (long long)a.base[j] + jn + lo;
     a.dx[pos] = kd_from_order_key(vk);
-    a.dw[pos] = a.wts ? a.wts[a.sidx[i]] : a.tsf[j];
+    const double* wts = a.call->wts;
+    a.dw[pos] = wts ? wts[a.sidx[i]] : a.tsf[j];
   }
 }
 
@@ -1312,6 +1313,152 @@ int kd_pipeline_prepare_device(KdSession* s) {
   return KD_OK;
 }
 
+// Host view of an enqueued ingest step: where the hierarchy stands after its
+// levels (pointers into the workspace) and how many kernels it launched.
+struct KdStepView {
+  const int* curA = nullptr;
+  const int* Iprev = nullptr;
+  long long launches = 0;
+  cudaError_t err = cudaSuccess;  // first failed runtime call while enqueueing
+  void note(cudaError_t e) {
+    if (err == cudaSuccess) err = e;
+  }
+};
+
+// Stage events.  Inside a capture they must be external records, which become
+// event-record nodes of the graph (a plain record would only mark a capture
+// dependency and never complete).
+static void stage_mark(KdSession* s, int i) {
+  if (!s->stats.enabled) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s->stream, &cs);
+  if (cs == cudaStreamCaptureStatusActive)
+    cudaEventRecordWithFlags(s->stats.ev[i], s->stream, cudaEventRecordExternal);
+  else
+    cudaEventRecord(s->stats.ev[i], s->stream);
+}
+
+static KdSortBufs sort_bufs(KdWorkspace& w) {
+  return KdSortBufs{{w.k64[0], w.k64[1]}, {w.key[0], w.key[1]}, {w.idx[0], w.idx[1]}, w.ghist,
+                    w.rs_state, w.rs_ticket, w.rs_epoch_base, &w.rs_epochs_used, w.cap_rs_tiles,
+                    &reinterpret_cast<KdErr*>(w.err)->code};
+}
+
+static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, const KdLevelDev& lv,
+                          const double* dx, const double* dw, int id_last, KdStepView& v) {
+  cudaStream_t str = s->stream;
+  TileArgs ta{sd, lv.Tl, lv.Ts, lv.I, lv, dx, dw, w.tkey, w.tbuf, w.st_count, w.scr_m,
+              w.scr_w, w.tcount, w.cap_work, w.cap_inter, w.needs, s->force_exact, id_last,
+              w.err};
+  k_tiles<KD_TILE><<<level_grid(s), 32, tile_smem(), str>>>(ta);
+  k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * 8, 128, tile_smem_small(), str>>>(ta);
+  v.launches += 2;
+}
+
+// Hierarchy levels from+1 .. to (each: plan, compaction of the previous level's
+// outputs into a dense input, tiles).
+static void enqueue_levels(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, int from, int to,
+                           int id_last, KdStepView& v) {
+  cudaStream_t str = s->stream;
+  for (int L = from + 1; L <= to; ++L) {
+    KdLevelDev cur = w.lv[L & 1];
+    KdLevelDev nxt = w.lv[(L + 1) & 1];
+    cur.A = const_cast<int*>(v.curA);
+    PlanArgs pa{v.curA, v.Iprev, cur, nxt, w.tcount, w.doff, w.tkey, w.cap_work, w.cap_inter,
+                w.cap_keys, w.cap_merged, w.needs, w.err};
+    k_plan<<<1, 1024, 0, str>>>(pa);
+    CompactArgs ca{v.Iprev, w.tcount, w.doff, w.scr_m, w.scr_w, w.dx[L & 1], w.dw[L & 1], w.err};
+    k_compact<<<s->num_sms * 4, 256, 0, str>>>(ca);
+    v.launches += 2;
+    enqueue_tiles(s, w, sd, cur, w.dx[L & 1], w.dw[L & 1], id_last, v);
+    v.curA = nxt.A;
+    v.Iprev = cur.I;
+  }
+}
+
+// Commit (prune, prefix, slot flip) and the status readback.
+static void enqueue_tail(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, long long keys_max,
+                         KdStepView& v) {
+  cudaStream_t str = s->stream;
+  stage_mark(s, 5);
+  CommitArgs ca{sd, w.totals, w.tkey, w.tbuf, w.st_count, w.st_clock, w.st_ls, w.st_min,
+                w.st_max, v.curA, w.err};
+  k_commit<<<(int)((keys_max + 127) / 128), 128, 0, str>>>(ca);
+  v.launches += 1;
+  stage_mark(s, 6);
+  v.note(cudaGetLastError());
+  v.note(cudaMemcpyAsync(w.h_err, w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, str));
+  v.note(cudaMemcpyAsync(w.h_scalars, w.needs, sizeof(int) * 4, cudaMemcpyDeviceToHost, str));
+}
+
+// One whole ingest step as device work only (so it can be captured): the
+// per-call block, prep, sort, planning, level 0, `levels` hierarchy levels,
+// commit and readback.
+static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long long n, int mode,
+                               bool with_idx, int levels, int id_last) {
+  cudaStream_t str = s->stream;
+  const KdStoreDev sd = st->d;
+  const long long keys_max = std::min<long long>(n, sd.K);
+  const int key_bits = key_bits_for(sd.K);
+  KdStepView v;
+  v.note(cudaMemcpyAsync(w.d_call, w.h_call, sizeof(KdCallArgs), cudaMemcpyHostToDevice, str));
+  v.note(cudaMemsetAsync(w.totals, 0, sizeof(int4) * 8, str));
+  v.note(cudaMemsetAsync(w.needs, 0, sizeof(int) * 4, str));
+  stage_mark(s, 0);
+  {
+    int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
+    k_prep<<<grid, 256, 0, str>>>(n, w.d_call, sd.K, w.k64[0], w.key[0],
+                                  with_idx ? w.idx[0] : nullptr, w.err);
+    v.launches += 1;
+  }
+  stage_mark(s, 1);
+  KdSortBufs sb = sort_bufs(w);
+  const int r = kd_radix_sort(sb, n, key_bits, with_idx, s->num_sms, str);
+  v.launches += kd_radix_sort_launches(n, key_bits);
+  stage_mark(s, 2);
+  const uint64_t* k64 = w.k64[r];
+  const uint32_t* skey = w.key[r];
+  const uint32_t* sidx = with_idx ? w.idx[r] : nullptr;
+  kd_scan(TouchedSrc{skey}, TouchedDst{skey, w.tkey, w.tstart, w.tmap, w.cap_keys, sd.K}, n,
+          w.partials, &w.totals[0], str);
+  {
+    PrepareArgs pa{sd, n, k64, w.tkey, w.tstart, w.totals, mode, w.d_call, w.tm, w.tprior,
+                   w.tbuf, w.tsf, w.tpscale, w.st_clock, w.st_ls, w.st_min, w.st_max, w.err};
+    k_prepare<<<(int)((keys_max + 255) / 256), 256, 0, str>>>(pa);
+  }
+  // Level-0 arrays live in lv[0]; its scalars in totals[1] = (Ts, Tl, A1, M0)
+  // and totals[2].x = I0.
+  KdLevelDev l0 = w.lv[0];
+  l0.Ts = (int*)&w.totals[1] + 0;
+  l0.Tl = (int*)&w.totals[1] + 1;
+  l0.M = (int*)&w.totals[1] + 3;
+  l0.I = (int*)&w.totals[2] + 0;
+  int* a1 = (int*)&w.totals[1] + 2;
+  kd_scan(Plan0Src{w.totals, w.tm}, Plan0Dst{w.totals, w.tm, l0, w.lv[1], w.cap_work, w.cap_keys},
+          keys_max, w.partials, &w.totals[1], str);
+  {
+    InterArgs ia{a1, l0, w.lv[1], l0.I, w.cap_inter, w.needs, w.err};
+    k_inter0<<<1, 1024, 0, str>>>(ia);
+  }
+  {
+    MergeArgs ma{sd, n, k64, skey, sidx, w.d_call, w.tkey, w.tmap, w.tstart, w.tprior, w.tbuf,
+                 w.tsf, w.tpscale, l0.base, w.totals, w.dx[0], w.dw[0], w.cap_merged, w.needs, w.err};
+    int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
+    k_merge_new<<<grid, 256, 0, str>>>(ma);
+    int pgrid = (int)std::min<long long>((keys_max * 32 + 255) / 256, (long long)s->num_sms * 16);
+    k_merge_prior<<<pgrid, 256, 0, str>>>(ma);
+  }
+  v.launches += 3 + 1 + 3 + 1 + 2;
+  stage_mark(s, 3);
+  enqueue_tiles(s, w, sd, l0, w.dx[0], w.dw[0], id_last, v);
+  stage_mark(s, 4);
+  v.curA = a1;
+  v.Iprev = l0.I;
+  enqueue_levels(s, w, sd, 0, levels, id_last, v);
+  enqueue_tail(s, w, sd, keys_max, v);
+  return v;
+}
+
 int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_t* d_keys,
                         const double* d_vals, const double* d_wts, long long n, int mode,
                         double timestamp, const double* d_merge_min, const double* d_merge_max,
@@ -1319,140 +1466,109 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
   cudaStream_t str = s->stream;
   const KdStoreDev sd = st->d;
   const long long keys_max = std::min<long long>(n, sd.K);
-  {
-    {
-      // index starts at +inf so that the first offending sample wins the atomicMin
-      KdErrHost init{0, 0, 0x7fffffffffffffffLL};
-      *w.h_err = init;
-      KD_CK(cudaMemcpyAsync(w.err, w.h_err, sizeof(KdErrHost), cudaMemcpyHostToDevice, str));
-    }
-    KD_CK(cudaMemsetAsync(w.totals, 0, sizeof(int4) * 8, str));
-    KD_CK(cudaMemsetAsync(w.needs, 0, sizeof(int) * 4, str));
-    const bool with_idx = d_wts != nullptr;
-    KdStageStats& T = s->stats;
-    auto mark = [&](int i) {
-      if (T.enabled) cudaEventRecord(T.ev[i], str);
-    };
-    const int key_bits = key_bits_for(sd.K);
-    // K0/K1 normalisers do not depend on the tile total, so the id of q == 1
-    // is one constant per launch (host FP64, same arithmetic as the device).
-    const int id_last = sd.scale <= KD_SCALE_K1
-                            ? (int)kd_bucket(sd.scale, 1.0, 1.0, kd_normalizer(sd.scale, sd.compression, 1.0))
-                            : 0;
-    long long launches = 0;
-    mark(0);
-    {
-      int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
-      k_prep<<<grid, 256, 0, str>>>(n, d_keys, d_vals, d_wts, sd.K, w.k64[0], w.key[0],
-                                    with_idx ? w.idx[0] : nullptr, w.err);
-      launches += 1;
-    }
-    mark(1);
-    KdSortBufs sb{{w.k64[0], w.k64[1]}, {w.key[0], w.key[1]}, {w.idx[0], w.idx[1]}, w.ghist,
-                  w.rs_state, w.rs_ticket, &w.rs_epoch, w.cap_rs_tiles,
-                  &reinterpret_cast<KdErr*>(w.err)->code};
-    const int r = kd_radix_sort(sb, n, key_bits, with_idx, s->num_sms, str);
-    launches += kd_radix_sort_launches(n, key_bits);
-    mark(2);
-    const uint64_t* k64 = w.k64[r];
-    const uint32_t* skey = w.key[r];
-    const uint32_t* sidx = with_idx ? w.idx[r] : nullptr;
-    kd_scan(TouchedSrc{skey}, TouchedDst{skey, w.tkey, w.tstart, w.tmap, w.cap_keys, sd.K}, n,
-            w.partials, &w.totals[0], str);
-    {
-      PrepareArgs pa{sd, n, k64, w.tkey, w.tstart, w.totals, mode, timestamp,
-                     d_merge_min, d_merge_max, d_merge_clock, w.tm, w.tprior, w.tbuf, w.tsf,
-                     w.tpscale, w.st_clock, w.st_ls, w.st_min, w.st_max, w.err};
-      k_prepare<<<(int)((keys_max + 255) / 256), 256, 0, str>>>(pa);
-    }
-    // Level-0 arrays live in lv[0]; its scalars in totals[1] = (Ts, Tl, A1, M0)
-    // and totals[2].x = I0.
-    KdLevelDev l0 = w.lv[0];
-    l0.Ts = (int*)&w.totals[1] + 0;
-    l0.Tl = (int*)&w.totals[1] + 1;
-    l0.M = (int*)&w.totals[1] + 3;
-    l0.I = (int*)&w.totals[2] + 0;
-    int* a1 = (int*)&w.totals[1] + 2;
-    kd_scan(Plan0Src{w.totals, w.tm}, Plan0Dst{w.totals, w.tm, l0, w.lv[1], w.cap_work, w.cap_keys},
-            keys_max, w.partials, &w.totals[1], str);
-    {
-      InterArgs ia{a1, l0, w.lv[1], l0.I, w.cap_inter, w.needs, w.err};
-      k_inter0<<<1, 1024, 0, str>>>(ia);
-    }
-    {
-      MergeArgs ma{sd, n, k64, skey, sidx, d_wts, w.tkey, w.tmap, w.tstart, w.tprior, w.tbuf,
-                   w.tsf, w.tpscale, l0.base, w.totals, w.dx[0], w.dw[0], w.cap_merged, w.needs, w.err};
-      int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
-      k_merge_new<<<grid, 256, 0, str>>>(ma);
-      int pgrid = (int)std::min<long long>((keys_max * 32 + 255) / 256, (long long)s->num_sms * 16);
-      k_merge_prior<<<pgrid, 256, 0, str>>>(ma);
-    }
-    launches += 3 + 1 + 3 + 1 + 2;
-    mark(3);
-    auto launch_tiles = [&](const KdLevelDev& lv, const double* dx, const double* dw) {
-      TileArgs ta{sd, lv.Tl, lv.Ts, lv.I, lv, dx, dw, w.tkey, w.tbuf, w.st_count, w.scr_m,
-                  w.scr_w, w.tcount, w.cap_work, w.cap_inter, w.needs, s->force_exact, id_last,
-                  w.err};
-      k_tiles<KD_TILE><<<level_grid(s), 32, tile_smem(), str>>>(ta);
-      k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * 8, 128, tile_smem_small(), str>>>(ta);
-      launches += 2;
-    };
-    launch_tiles(l0, w.dx[0], w.dw[0]);
-    mark(4);
-    // Levels >= 1: run the number of levels the store needed last time, then
-    // commit; if keys remain above one tile, continue from where it stopped.
-    const int* curA = a1;
-    const int* Iprev = l0.I;
-    int L = 0;
-    int levels_goal = std::max(1, std::min(st->levels_hint, s->max_levels));
-    for (;;) {
-      for (; L < levels_goal; ) {
-        ++L;
-        KdLevelDev cur = w.lv[L & 1];
-        KdLevelDev nxt = w.lv[(L + 1) & 1];
-        cur.A = const_cast<int*>(curA);
-        PlanArgs pa{curA, Iprev, cur, nxt, w.tcount, w.doff, w.tkey, w.cap_work, w.cap_inter,
-                    w.cap_keys, w.cap_merged, w.needs, w.err};
-        k_plan<<<1, 1024, 0, str>>>(pa);
-        CompactArgs ca{Iprev, w.tcount, w.doff, w.scr_m, w.scr_w, w.dx[L & 1], w.dw[L & 1], w.err};
-        k_compact<<<s->num_sms * 4, 256, 0, str>>>(ca);
-        launches += 2;
-        launch_tiles(cur, w.dx[L & 1], w.dw[L & 1]);
-        curA = nxt.A;
-        Iprev = cur.I;
+  const bool with_idx = d_wts != nullptr;
+  // K0/K1 normalisers do not depend on the tile total, so the id of q == 1
+  // is one constant per launch (host FP64, same arithmetic as the device).
+  const int id_last = sd.scale <= KD_SCALE_K1
+                          ? (int)kd_bucket(sd.scale, 1.0, 1.0, kd_normalizer(sd.scale, sd.compression, 1.0))
+                          : 0;
+  // The per-call block; the status index starts at +inf so that the first
+  // offending sample wins the atomicMin.
+  KdCallArgs& c = *w.h_call;
+  c.keys = d_keys;
+  c.vals = d_vals;
+  c.wts = d_wts;
+  c.merge_min = d_merge_min;
+  c.merge_max = d_merge_max;
+  c.merge_clock = d_merge_clock;
+  c.timestamp = timestamp;
+  c.err = KdErrHost{0, 0, 0x7fffffffffffffffLL};
+  KdSortBufs sb = sort_bufs(w);
+  kd_rs_epoch_reserve(sb, str);
+  int L = std::max(1, std::min(st->levels_hint, s->max_levels));
+
+  KdGraphKey key;
+  key.n = n;
+  key.key_bits = key_bits_for(sd.K);
+  key.with_idx = with_idx;
+  key.mode = mode;
+  key.levels = L;
+  key.force_exact = s->force_exact;
+  key.timing = s->stats.enabled;
+  key.scale = sd.scale;
+  key.compression = sd.compression;
+  key.generation = w.generation;
+  KdStepView v;
+  bool ran = false;
+  if (s->use_graphs && w.generation != 0) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(str, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
+      KdGraphEntry* g = nullptr;
+      for (KdGraphEntry& e : st->graphs)
+        if (e.exec && e.key == key) g = &e;
+      if (!g && key == st->last_eager) {
+        // The same step shape twice in a row: capture it once, replay it after.
+        KdGraphEntry& slot = st->graphs[st->graph_next];
+        st->graph_next = (st->graph_next + 1) % KD_GRAPH_CACHE;
+        if (slot.exec) cudaGraphExecDestroy(slot.exec);
+        slot = KdGraphEntry();
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(str, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+          const KdStepView cv = enqueue_step(s, st, w, n, mode, with_idx, L, id_last);
+          const bool ended = cudaStreamEndCapture(str, &graph) == cudaSuccess;
+          if (ended && graph && cv.err == cudaSuccess) {
+            cudaGraphExec_t ex = nullptr;
+            if (cudaGraphInstantiate(&ex, graph, 0) == cudaSuccess) {
+              slot.key = key;
+              slot.exec = ex;
+              slot.curA = cv.curA;
+              slot.Iprev = cv.Iprev;
+              slot.launches = cv.launches;
+              g = &slot;
+            }
+          }
+          if (graph) cudaGraphDestroy(graph);
+        }
+        cudaGetLastError();  // a capture that failed leaves the eager path below
       }
-      mark(5);
-      {
-        CommitArgs ca{sd, w.totals, w.tkey, w.tbuf, w.st_count, w.st_clock, w.st_ls, w.st_min,
-                      w.st_max, curA, w.err};
-        k_commit<<<(int)((keys_max + 127) / 128), 128, 0, str>>>(ca);
-        launches += 1;
+      if (g) {
+        KD_CK(cudaGraphLaunch(g->exec, str));
+        v.curA = g->curA;
+        v.Iprev = g->Iprev;
+        v.launches = g->launches;
+        ran = true;
       }
-      mark(6);
-      KD_CK(cudaGetLastError());
-      KD_CK(cudaMemcpyAsync(w.h_err, w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, str));
-      KD_CK(cudaMemcpyAsync(w.h_scalars, w.needs, sizeof(int) * 4, cudaMemcpyDeviceToHost, str));
-      KD_CK(cudaStreamSynchronize(str));
-      if (w.h_err->code == KD_EMORE_LEVELS && L < s->max_levels) {
-        // keys still above one tile: reset the status word and run more levels
-        KdErrHost init{0, 0, 0x7fffffffffffffffLL};
-        *w.h_err = init;
-        KD_CK(cudaMemcpyAsync(w.err, w.h_err, sizeof(KdErrHost), cudaMemcpyHostToDevice, str));
-        levels_goal = std::min(s->max_levels, L + 2);
-        continue;
-      }
-      break;
     }
-    if (w.h_err->code == KD_EMORE_LEVELS) w.h_err->code = KD_ECONVERGE;
-    if (w.h_err->code == 0) st->levels_hint = std::max(1, L);
-    T.launches += launches;
-    T.ingests += 1;
-    if (T.enabled) {
-      for (int i = 0; i < KD_NSTAGES; ++i) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, T.ev[i], T.ev[i + 1]);
-        T.ms[i] += ms;
-      }
+  }
+  if (!ran) {
+    v = enqueue_step(s, st, w, n, mode, with_idx, L, id_last);
+    st->last_eager = key;
+    KD_CK(v.err);
+  }
+  KD_CK(cudaGetLastError());
+  KD_CK(cudaStreamSynchronize(str));
+  // Keys still above one tile after the planned levels: run more levels from
+  // where the step stopped, then commit again.
+  while (w.h_err->code == KD_EMORE_LEVELS && L < s->max_levels) {
+    *w.h_err = KdErrHost{0, 0, 0x7fffffffffffffffLL};
+    KD_CK(cudaMemcpyAsync(w.err, w.h_err, sizeof(KdErrHost), cudaMemcpyHostToDevice, str));
+    const int goal = std::min(s->max_levels, L + 2);
+    enqueue_levels(s, w, sd, L, goal, id_last, v);
+    L = goal;
+    enqueue_tail(s, w, sd, keys_max, v);
+    KD_CK(v.err);
+    KD_CK(cudaStreamSynchronize(str));
+  }
+  if (w.h_err->code == KD_EMORE_LEVELS) w.h_err->code = KD_ECONVERGE;
+  if (w.h_err->code == 0) st->levels_hint = std::max(1, L);
+  KdStageStats& T = s->stats;
+  T.launches += v.launches;
+  T.ingests += 1;
+  if (T.enabled) {
+    for (int i = 0; i < KD_NSTAGES; ++i) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, T.ev[i], T.ev[i + 1]) == cudaSuccess) T.ms[i] += ms;
+      else cudaGetLastError();  // timing is best effort; never fail the next call
     }
   }
   const KdErrHost e = *w.h_err;

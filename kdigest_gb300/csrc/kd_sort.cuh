@@ -26,19 +26,25 @@
 #define KD_RS_MAXPASS 12
 #define KD_RS_SPIN_LIMIT (1 << 22)
 
-// Look-back words: [63:48] epoch, [47:46] status (1 aggregate, 2 inclusive),
-// [45:0] count.
+// Look-back words: [63:34] epoch, [33:32] status (1 aggregate, 2 inclusive),
+// [31:0] count (counts never exceed n < 2^31).  The epoch of pass p of a sort is
+// (device epoch base) + p: the histogram kernel advances the base by
+// KD_RS_EPOCH_STRIDE per sort, so a replayed CUDA graph gets fresh epochs too,
+// and words left by earlier sorts never read as ready.
 #define KD_LB_AGG 1ull
 #define KD_LB_INC 2ull
+#define KD_RS_EPOCH_STRIDE 16u
+#define KD_RS_EPOCH_LIMIT ((1u << 30) - 2u * KD_RS_EPOCH_STRIDE)
 __device__ __forceinline__ unsigned long long lb_pack(unsigned epoch, unsigned long long st,
                                                       unsigned long long cnt) {
-  return ((unsigned long long)epoch << 48) | (st << 46) | cnt;
+  return ((unsigned long long)epoch << 34) | (st << 32) | cnt;
 }
 
 static __global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_hist_all(
     const uint64_t* __restrict__ k64, const uint32_t* __restrict__ key, long long n,
-    int key_passes, unsigned* __restrict__ ghist) {
+    int key_passes, unsigned* __restrict__ ghist, unsigned* __restrict__ epoch_base) {
   __shared__ unsigned h[KD_RS_MAXPASS][256];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *epoch_base += KD_RS_EPOCH_STRIDE;
   for (int t = threadIdx.x; t < KD_RS_MAXPASS * 256; t += KD_RS_THREADS) (&h[0][0])[t] = 0;
   __syncthreads();
   for (long long i = (long long)blockIdx.x * KD_RS_THREADS + threadIdx.x; i < n;
@@ -71,7 +77,8 @@ struct KdRsPass {
   unsigned long long* state;
   unsigned long long* ticket;
   unsigned long long ticket_base;
-  unsigned epoch;
+  const unsigned* epoch_base;  // device epoch base of this sort
+  int pass;                    // epoch = *epoch_base + pass
   int* err_code;  // device status word (KdErr.code)
 };
 
@@ -97,6 +104,7 @@ __global__ void __launch_bounds__(KD_RS_THREADS, 3) kd_rs_onesweep(KdRsPass a) {
   const long long base = tile0 + (long long)warp * KD_RS_PER_WARP;
   const unsigned lt_mask = (1u << lane) - 1u;
   const int shift = a.shift;
+  const unsigned epoch = *a.epoch_base + (unsigned)a.pass;
   // 1. stable rank of every element among the warp's elements of its digit;
   //    ranks (< 512) are packed two per register
   unsigned rank2[KD_RS_ROUNDS / 2];
@@ -154,9 +162,9 @@ __global__ void __launch_bounds__(KD_RS_THREADS, 3) kd_rs_onesweep(KdRsPass a) {
     volatile unsigned long long* st = a.state;
     unsigned long long excl = 0;
     if (b == 0) {
-      st[d] = lb_pack(a.epoch, KD_LB_INC, cnt_d);
+      st[d] = lb_pack(epoch, KD_LB_INC, cnt_d);
     } else {
-      st[(size_t)b * 256 + d] = lb_pack(a.epoch, KD_LB_AGG, cnt_d);
+      st[(size_t)b * 256 + d] = lb_pack(epoch, KD_LB_AGG, cnt_d);
       long long hi = b - 1;  // next predecessor to account for
       long long spins = 0;
       bool done = false, timed_out = false;
@@ -164,15 +172,15 @@ __global__ void __launch_bounds__(KD_RS_THREADS, 3) kd_rs_onesweep(KdRsPass a) {
         unsigned long long v[KD_LB_WINDOW];
 #pragma unroll
         for (int k = 0; k < KD_LB_WINDOW; ++k)
-          v[k] = hi - k >= 0 ? st[(size_t)(hi - k) * 256 + d] : lb_pack(a.epoch, KD_LB_INC, 0);
+          v[k] = hi - k >= 0 ? st[(size_t)(hi - k) * 256 + d] : lb_pack(epoch, KD_LB_INC, 0);
         // consume the window from hi downwards up to the first not-ready word
         int k = 0;
         for (; k < KD_LB_WINDOW; ++k) {
           const unsigned long long w = v[k];
-          const bool ready = (unsigned)(w >> 48) == a.epoch && ((w >> 46) & 3ull) != 0ull;
+          const bool ready = (unsigned)(w >> 34) == epoch && ((w >> 32) & 3ull) != 0ull;
           if (!ready) break;
-          excl += w & ((1ull << 46) - 1ull);
-          if (((w >> 46) & 3ull) == KD_LB_INC) {
+          excl += w & 0xffffffffull;
+          if (((w >> 32) & 3ull) == KD_LB_INC) {
             done = true;
             break;
           }
@@ -185,7 +193,7 @@ __global__ void __launch_bounds__(KD_RS_THREADS, 3) kd_rs_onesweep(KdRsPass a) {
         }
       }
       if (timed_out) atomicCAS(a.err_code, 0, KD_ETIMEOUT);
-      st[(size_t)b * 256 + d] = lb_pack(a.epoch, KD_LB_INC, excl + cnt_d);
+      st[(size_t)b * 256 + d] = lb_pack(epoch, KD_LB_INC, excl + cnt_d);
     }
     gpos[d] = (long long)gbase + (long long)excl;
   }
@@ -226,7 +234,8 @@ struct KdSortBufs {
   unsigned* ghist;                // KD_RS_MAXPASS * 256
   unsigned long long* state;      // 256 per tile
   unsigned long long* ticket;     // device ticket counter (reset per sort)
-  unsigned* epoch;                // host-side epoch of the look-back words
+  unsigned* epoch_base;           // device epoch base, advanced by every sort
+  unsigned long long* epochs_used;  // host: epochs consumed since the last clear
   long long state_tiles;          // tiles the look-back array holds
   int* err_code;
 };
@@ -236,7 +245,19 @@ static inline size_t kd_rs_smem(bool with_idx) {
   return (size_t)KD_RS_TILE * (8 + 4 + (with_idx ? 4 : 0));
 }
 
-// Sorts by (key, k64); returns the index (0/1) of the buffer set holding the result.
+// Host bookkeeping, once before every sort is enqueued or replayed: when the
+// epoch field would wrap, the look-back words and the base are cleared first.
+static inline void kd_rs_epoch_reserve(KdSortBufs& b, cudaStream_t st) {
+  if (*b.epochs_used + KD_RS_EPOCH_STRIDE >= KD_RS_EPOCH_LIMIT) {
+    cudaMemsetAsync(b.state, 0, sizeof(unsigned long long) * 256 * (size_t)b.state_tiles, st);
+    cudaMemsetAsync(b.epoch_base, 0, sizeof(unsigned), st);
+    *b.epochs_used = 0;
+  }
+  *b.epochs_used += KD_RS_EPOCH_STRIDE;
+}
+
+// Sorts by (key, k64); returns the index (0/1) of the buffer set holding the
+// result.  Enqueues device work only (no host state), so it can be captured.
 static inline int kd_radix_sort(KdSortBufs& b, long long n, int key_bits, bool with_idx,
                                 int num_sms, cudaStream_t st) {
   int src = 0;
@@ -246,16 +267,12 @@ static inline int kd_radix_sort(KdSortBufs& b, long long n, int key_bits, bool w
   cudaMemsetAsync(b.ghist, 0, sizeof(unsigned) * KD_RS_MAXPASS * 256, st);
   cudaMemsetAsync(b.ticket, 0, sizeof(unsigned long long), st);
   unsigned long long ticket_base = 0;
-  kd_rs_hist_all<<<num_sms * 8, KD_RS_THREADS, 0, st>>>(b.k64[0], b.key[0], n, key_passes, b.ghist);
+  kd_rs_hist_all<<<num_sms * 8, KD_RS_THREADS, 0, st>>>(b.k64[0], b.key[0], n, key_passes, b.ghist,
+                                                        b.epoch_base);
   auto pass = [&](int shift, int from_key, int pidx) {
     const int dst = src ^ 1;
-    *b.epoch += 1;
-    if (*b.epoch >= 65535u) {  // epochs wrap: clear the look-back words
-      cudaMemsetAsync(b.state, 0, sizeof(unsigned long long) * 256 * (size_t)b.state_tiles, st);
-      *b.epoch = 1;
-    }
     KdRsPass a{b.k64[src], b.key[src], b.idx[src], b.k64[dst], b.key[dst], b.idx[dst], n, shift,
-               from_key, b.ghist + pidx * 256, b.state, b.ticket, ticket_base, *b.epoch,
+               from_key, b.ghist + pidx * 256, b.state, b.ticket, ticket_base, b.epoch_base, pidx,
                b.err_code};
     if (with_idx)
       kd_rs_onesweep<true><<<nb, KD_RS_THREADS, kd_rs_smem(true), st>>>(a);
