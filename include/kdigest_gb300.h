@@ -133,6 +133,42 @@ KD_API int kd_store_stats(kd_store* st, int64_t* num_keys, int64_t* total_centro
  * for all keys at once (grouped.mojo:182-185). */
 KD_API int kd_store_counts(kd_store* st, int32_t* out, int flags);
 
+/* Serving loop over a resident store (no counterpart in the reference, which
+ * has none).  Client threads submit ingest and query requests with
+ * non-decreasing timestamps; a worker thread serves them by continuous
+ * batching in windows of `window_s` of the timestamp axis.  A window's queries
+ * see the store as it was before the window's ingests; the window's ingests are
+ * applied as one grouped batch (samples concatenated in arrival order, clocks
+ * moved to the window's last ingest timestamp).  Windows close when a later
+ * window's request arrives, on kd_server_advance past their end, or on flush, so
+ * every result depends only on the request stream.  Requests are validated at
+ * submit (KD_EINVAL: key out of range, non-finite value, q outside [0,1],
+ * decreasing timestamp or a closed window) and admitted while the bytes of
+ * buffered requests stay within budget_bytes (0 = 1 TiB); submit blocks until
+ * there is room.  The store's session belongs to the server until it is
+ * destroyed.  Query outputs are written to `out` (n doubles, kept valid until
+ * the request is waited for); a query of an empty digest completes with
+ * KD_EEMPTY and NaN. */
+#define KD_REQ_INGEST 0
+#define KD_REQ_QUANTILE 1
+#define KD_REQ_CDF 2
+typedef struct kd_server kd_server;
+KD_API int kd_server_create(kd_store* st, double window_s, size_t budget_bytes, kd_server** out);
+KD_API int kd_server_submit(kd_server* srv, int kind, double timestamp, const uint32_t* keys,
+                            const double* vals, int64_t n, double* out, int64_t* ticket);
+/* The client's clock reached now_ts: windows ending at or before it close. */
+KD_API int kd_server_advance(kd_server* srv, double now_ts);
+/* Waits for a request (timeout_s < 0: no limit; KD_ETIMEOUT when it runs out);
+ * *status receives the request's own status. */
+KD_API int kd_server_wait(kd_server* srv, int64_t ticket, double timeout_s, int* status);
+/* Closes every open window and waits until all submitted requests completed. */
+KD_API int kd_server_flush(kd_server* srv);
+/* Submit-to-completion latency percentiles in seconds (p50, p99, p999), requests
+ * completed, windows served and seconds the worker spent serving windows. */
+KD_API int kd_server_stats(kd_server* srv, double* lat3, int64_t* completed, int64_t* windows,
+                           double* busy_s);
+KD_API void kd_server_destroy(kd_server* srv);
+
 /* No counterpart in the reference.  kd_compress for callers that cannot call
  * cudaMalloc: a host program whose own pool owns all device memory (memory taken
  * behind its back is unaccounted and may not exist), or a latency-critical loop

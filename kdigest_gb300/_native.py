@@ -28,7 +28,10 @@ EXPORTED = (
     "kd_store_quantile", "kd_store_cdf", "kd_store_merge", "kd_store_get_digest",
     "kd_store_set_digest", "kd_store_to_bytes", "kd_store_from_bytes", "kd_store_stats",
     "kd_store_counts", "kd_compress_noalloc",
+    "kd_server_create", "kd_server_submit", "kd_server_advance", "kd_server_wait",
+    "kd_server_flush", "kd_server_stats", "kd_server_destroy",
 )
+KD_REQ_INGEST, KD_REQ_QUANTILE, KD_REQ_CDF = 0, 1, 2
 
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -83,6 +86,14 @@ def load(path: str = LIB_PATH):
     L.kd_store_to_bytes.argtypes = [_P, ctypes.c_uint32, _P, _I64, ctypes.POINTER(_I64)]
     L.kd_store_from_bytes.argtypes = [_P, ctypes.c_uint32, _P, _I64]
     L.kd_store_counts.argtypes = [_P, _P, ctypes.c_int]
+    L.kd_server_create.argtypes = [_P, _D, ctypes.c_size_t, ctypes.POINTER(_P)]
+    L.kd_server_submit.argtypes = [_P, ctypes.c_int, _D, _P, _P, _I64, _P, ctypes.POINTER(_I64)]
+    L.kd_server_advance.argtypes = [_P, _D]
+    L.kd_server_wait.argtypes = [_P, _I64, _D, ctypes.POINTER(ctypes.c_int)]
+    L.kd_server_flush.argtypes = [_P]
+    L.kd_server_stats.argtypes = [_P, _P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                                  ctypes.POINTER(_D)]
+    L.kd_server_destroy.argtypes = [_P]
     L.kd_compress_noalloc.argtypes = [ctypes.c_int, _D, _P, _P, _I64, ctypes.c_int, _P, _P, _I64,
                                       ctypes.POINTER(_I64), _P, ctypes.c_char_p, ctypes.c_int]
     L.kd_store_stats.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),

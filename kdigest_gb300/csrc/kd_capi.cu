@@ -15,12 +15,6 @@
 #include "kd_scan.cuh"
 #include "kd_sort.cuh"
 
-struct kd_session {
-  KdSession s;
-};
-struct kd_store {
-  KdStore st;
-};
 
 #define KD_CK(call)                                           \
   do {                                                        \

@@ -199,6 +199,14 @@ struct KdStore {
   KdGraphKey last_eager;
 };
 
+// The opaque handles of the C-ABI.
+struct kd_session {
+  KdSession s;
+};
+struct kd_store {
+  KdStore st;
+};
+
 // Pipeline entry points (kd_pipeline.cu).  All work is enqueued on sess->stream.
 // Return KD_* status; on error sess->last_error holds a message.
 enum KdIngestMode { KD_MODE_COUNT = 0, KD_MODE_TIME = 1, KD_MODE_REPLACE = 2, KD_MODE_MERGE = 3 };

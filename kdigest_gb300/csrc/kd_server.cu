@@ -1,0 +1,449 @@
+// kd_server.cu — serving loop over a resident store: ingest and query requests
+// arrive one by one from client threads and are served by continuous batching.
+//
+// Semantics (deterministic in the request stream, whatever the load):
+//   * requests carry non-decreasing timestamps; request r belongs to window
+//     floor(ts / window) of the timestamp axis;
+//   * a window's query requests are answered against the store as it was
+//     before that window's ingests (so a query sees every ingest of earlier
+//     windows and none of later ones);
+//   * a window's ingest requests are applied as one grouped batch: their
+//     samples concatenated in arrival order, every touched key's clock moving
+//     to the window's last ingest timestamp (add_at semantics, time decay).
+// A window closes when a request of a later window arrives, when the client
+// advances the clock past its end, or on flush — never on a wall-clock timer,
+// so the batches, and therefore every result, depend only on the request
+// stream.  Requests that arrive while earlier windows are on the GPU are
+// admitted (against the byte budget) into the open window; the next closed
+// window's host->device copy runs on a copy stream while the current window
+// computes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/kdigest_gb300.h"
+#include "kd_engine.h"
+#include "kd_math.h"
+
+namespace {
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Req {
+  int64_t id = 0;
+  int kind = 0;
+  double ts = 0.0;
+  long long window = 0;
+  std::vector<uint32_t> keys;
+  std::vector<double> vals;  // values, q or x
+  double* out = nullptr;     // caller's output (queries)
+  size_t bytes = 0;
+  int status = -1;  // -1 while pending
+  double t_submit = 0.0, t_done = 0.0;
+};
+
+// Pinned host and device buffers of one staged window (two alternate).
+struct Buf {
+  size_t cap_i = 0, cap_q = 0;
+  uint32_t *h_ik = nullptr, *d_ik = nullptr;
+  double *h_iv = nullptr, *d_iv = nullptr;
+  uint32_t *h_qk = nullptr, *d_qk = nullptr;
+  double *h_qv = nullptr, *d_qv = nullptr, *h_qo = nullptr, *d_qo = nullptr;
+  cudaEvent_t copied = nullptr;
+};
+
+struct Staged {
+  long long window = 0;
+  std::vector<std::shared_ptr<Req>> reqs;
+  long long n_ing = 0, n_qq = 0, n_qc = 0;  // ingest pairs, quantile pairs, cdf pairs
+  double ts = 0.0;                          // last ingest timestamp of the window
+  int buf = 0;
+};
+
+void free_buf(Buf& b) {
+  void* dv[] = {b.d_ik, b.d_iv, b.d_qk, b.d_qv, b.d_qo};
+  for (void* p : dv)
+    if (p) cudaFree(p);
+  void* hv[] = {b.h_ik, b.h_iv, b.h_qk, b.h_qv, b.h_qo};
+  for (void* p : hv)
+    if (p) cudaFreeHost(p);
+  if (b.copied) cudaEventDestroy(b.copied);
+  b = Buf();
+}
+
+bool grow_buf(Buf& b, size_t ni, size_t nq) {
+  if (!b.copied && cudaEventCreateWithFlags(&b.copied, cudaEventDisableTiming) != cudaSuccess) return false;
+  bool ok = true;
+  if (ni > b.cap_i) {
+    size_t c = std::max(ni, 2 * b.cap_i);
+    if (b.d_ik) cudaFree(b.d_ik);
+    if (b.d_iv) cudaFree(b.d_iv);
+    if (b.h_ik) cudaFreeHost(b.h_ik);
+    if (b.h_iv) cudaFreeHost(b.h_iv);
+    b.d_ik = nullptr, b.d_iv = nullptr, b.h_ik = nullptr, b.h_iv = nullptr;
+    ok = ok && cudaMalloc(&b.d_ik, c * 4) == cudaSuccess && cudaMalloc(&b.d_iv, c * 8) == cudaSuccess &&
+         cudaHostAlloc((void**)&b.h_ik, c * 4, cudaHostAllocDefault) == cudaSuccess &&
+         cudaHostAlloc((void**)&b.h_iv, c * 8, cudaHostAllocDefault) == cudaSuccess;
+    b.cap_i = ok ? c : 0;
+  }
+  if (ok && nq > b.cap_q) {
+    size_t c = std::max(nq, 2 * b.cap_q);
+    void* dv[] = {b.d_qk, b.d_qv, b.d_qo};
+    for (void* p : dv)
+      if (p) cudaFree(p);
+    void* hv[] = {b.h_qk, b.h_qv, b.h_qo};
+    for (void* p : hv)
+      if (p) cudaFreeHost(p);
+    ok = cudaMalloc(&b.d_qk, c * 4) == cudaSuccess && cudaMalloc(&b.d_qv, c * 8) == cudaSuccess &&
+         cudaMalloc(&b.d_qo, c * 8) == cudaSuccess &&
+         cudaHostAlloc((void**)&b.h_qk, c * 4, cudaHostAllocDefault) == cudaSuccess &&
+         cudaHostAlloc((void**)&b.h_qv, c * 8, cudaHostAllocDefault) == cudaSuccess &&
+         cudaHostAlloc((void**)&b.h_qo, c * 8, cudaHostAllocDefault) == cudaSuccess;
+    b.cap_q = ok ? c : 0;
+  }
+  if (!ok) cudaGetLastError();
+  return ok;
+}
+
+}  // namespace
+
+struct kd_server {
+  KdStore* st = nullptr;
+  KdSession* s = nullptr;
+  double window_s = 0.001;
+  size_t budget = 0;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<std::shared_ptr<Req>> pending;  // arrival order (= timestamp order)
+  std::unordered_map<int64_t, std::shared_ptr<Req>> live;  // submitted, not yet waited for
+  int64_t next_id = 1;
+  double last_ts = -std::numeric_limits<double>::infinity();
+  double clock_ts = -std::numeric_limits<double>::infinity();
+  long long newest_window = std::numeric_limits<long long>::min();
+  bool flushing = false, stop = false;
+  size_t buffered = 0;
+  std::vector<double> latencies;
+  long long completed = 0, windows_done = 0;
+  double busy_s = 0.0;
+  int fatal = 0;
+  char fatal_msg[256] = {0};
+  cudaStream_t copy_stream = nullptr;
+  Buf buf[2];
+  std::thread worker;
+
+  long long window_of(double ts) const { return (long long)std::floor(ts / window_s); }
+  // Whether the window of the oldest pending request may be processed.
+  bool front_closed() const {
+    if (pending.empty()) return false;
+    const long long w = pending.front()->window;
+    return flushing || stop || newest_window > w || clock_ts >= (double)(w + 1) * window_s;
+  }
+};
+
+namespace {
+
+// Takes the oldest closed window (caller holds the lock) and packs it into
+// buffer `bi`, then starts its host->device copy on the copy stream.
+std::unique_ptr<Staged> take_window(kd_server* v, int bi) {
+  auto sg = std::make_unique<Staged>();
+  sg->window = v->pending.front()->window;
+  sg->buf = bi;
+  while (!v->pending.empty() && v->pending.front()->window == sg->window) {
+    auto r = v->pending.front();
+    v->pending.pop_front();
+    const long long n = (long long)r->vals.size();
+    if (r->kind == KD_REQ_INGEST) {
+      sg->n_ing += n;
+      sg->ts = r->ts;
+    } else if (r->kind == KD_REQ_QUANTILE) {
+      sg->n_qq += n;
+    } else {
+      sg->n_qc += n;
+    }
+    sg->reqs.push_back(std::move(r));
+  }
+  return sg;
+}
+
+int stage_copy(kd_server* v, Staged& sg) {
+  Buf& b = v->buf[sg.buf];
+  if (!grow_buf(b, (size_t)sg.n_ing, (size_t)(sg.n_qq + sg.n_qc))) return KD_ENOMEM;
+  long long oi = 0, oq = 0, oc = sg.n_qq;  // quantile pairs first, then cdf pairs
+  for (auto& r : sg.reqs) {
+    const size_t n = r->vals.size();
+    if (r->kind == KD_REQ_INGEST) {
+      memcpy(b.h_ik + oi, r->keys.data(), n * 4);
+      memcpy(b.h_iv + oi, r->vals.data(), n * 8);
+      oi += (long long)n;
+    } else {
+      long long& o = r->kind == KD_REQ_QUANTILE ? oq : oc;
+      memcpy(b.h_qk + o, r->keys.data(), n * 4);
+      memcpy(b.h_qv + o, r->vals.data(), n * 8);
+      o += (long long)n;
+    }
+  }
+  cudaStream_t cs = v->copy_stream;
+  const long long nq = sg.n_qq + sg.n_qc;
+  if (sg.n_ing) {
+    cudaMemcpyAsync(b.d_ik, b.h_ik, (size_t)sg.n_ing * 4, cudaMemcpyHostToDevice, cs);
+    cudaMemcpyAsync(b.d_iv, b.h_iv, (size_t)sg.n_ing * 8, cudaMemcpyHostToDevice, cs);
+  }
+  if (nq) {
+    cudaMemcpyAsync(b.d_qk, b.h_qk, (size_t)nq * 4, cudaMemcpyHostToDevice, cs);
+    cudaMemcpyAsync(b.d_qv, b.h_qv, (size_t)nq * 8, cudaMemcpyHostToDevice, cs);
+  }
+  cudaEventRecord(b.copied, cs);
+  return cudaGetLastError() == cudaSuccess ? KD_OK : KD_ECUDA;
+}
+
+// Queries (against the state before the window's ingests), then the ingest.
+void run_window(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>* next) {
+  KdSession* s = v->s;
+  Buf& b = v->buf[sg.buf];
+  const double t0 = now_s();
+  int ing_rc = stage_rc;
+  const long long nq = sg.n_qq + sg.n_qc;
+  if (stage_rc == KD_OK) {
+    cudaStreamWaitEvent(s->stream, b.copied, 0);
+    if (sg.n_qq) kd_pipeline_quantile(s, v->st, b.d_qk, b.d_qv, sg.n_qq, b.d_qo, 0);
+    if (sg.n_qc) kd_pipeline_quantile(s, v->st, b.d_qk + sg.n_qq, b.d_qv + sg.n_qq, sg.n_qc, b.d_qo + sg.n_qq, 1);
+    if (nq) cudaMemcpyAsync(b.h_qo, b.d_qo, (size_t)nq * 8, cudaMemcpyDeviceToHost, s->stream);
+  }
+  // While this window's ingest runs, the next closed window is packed and its
+  // copy starts on the copy stream (into the other buffer).
+  {
+    std::unique_lock<std::mutex> lk(v->mu);
+    if (!*next && v->front_closed()) {
+      *next = take_window(v, sg.buf ^ 1);
+      lk.unlock();
+      const int rc = stage_copy(v, **next);
+      if (rc) (*next)->buf = -rc - 1;  // remember the failure for its turn
+    }
+  }
+  if (stage_rc == KD_OK && sg.n_ing)
+    ing_rc = kd_pipeline_ingest(s, v->st, b.d_ik, b.d_iv, nullptr, sg.n_ing, KD_MODE_TIME, sg.ts,
+                                nullptr, nullptr, nullptr);
+  if (stage_rc == KD_OK) cudaStreamSynchronize(s->stream);
+  const double t1 = now_s();
+  std::lock_guard<std::mutex> lk(v->mu);
+  long long oq = 0, oc = sg.n_qq;
+  for (auto& r : sg.reqs) {
+    const size_t n = r->vals.size();
+    if (r->kind == KD_REQ_INGEST) {
+      r->status = ing_rc;
+    } else {
+      long long& o = r->kind == KD_REQ_QUANTILE ? oq : oc;
+      int stt = stage_rc;
+      if (stage_rc == KD_OK) {
+        for (size_t i = 0; i < n; ++i)
+          if (std::isnan(b.h_qo[o + (long long)i])) stt = KD_EEMPTY;  // inputs were validated
+        if (r->out) memcpy(r->out, b.h_qo + o, n * 8);
+      }
+      o += (long long)n;
+      r->status = stt;
+    }
+    r->t_done = t1;
+    v->latencies.push_back(t1 - r->t_submit);
+    v->buffered -= std::min(v->buffered, r->bytes);
+    ++v->completed;
+  }
+  ++v->windows_done;
+  v->busy_s += t1 - t0;
+  v->cv.notify_all();
+}
+
+void worker_main(kd_server* v) {
+  cudaSetDevice(v->s->device);
+  std::unique_ptr<Staged> cur;
+  int bi = 0;
+  for (;;) {
+    if (!cur) {
+      std::unique_lock<std::mutex> lk(v->mu);
+      v->cv.wait(lk, [&] { return v->front_closed() || (v->stop && v->pending.empty()); });
+      if (v->pending.empty()) return;  // stopping
+      cur = take_window(v, bi);
+      lk.unlock();
+      const int rc = stage_copy(v, *cur);
+      if (rc) cur->buf = -rc - 1;
+    }
+    int stage_rc = KD_OK;
+    if (cur->buf < 0) {  // staging failed: report it on the window's requests
+      stage_rc = -cur->buf - 1;
+      cur->buf = bi;
+    }
+    std::unique_ptr<Staged> next;
+    run_window(v, *cur, stage_rc, &next);
+    bi = cur->buf ^ 1;
+    cur = std::move(next);
+  }
+}
+
+int srv_fail(char* dst, const char* msg, int code) {
+  if (dst) snprintf(dst, 256, "%s", msg);
+  return code;
+}
+
+}  // namespace
+
+extern "C" {
+
+KD_API int kd_server_create(kd_store* store, double window_s, size_t budget_bytes, kd_server** out) {
+  if (!store || !out) return KD_EINVAL;
+  *out = nullptr;
+  KdSession* s = store->st.sess;
+  if (!(window_s > 0.0) || !kd_isfinite(window_s)) return srv_fail(s->last_error, "window must be positive", KD_EINVAL);
+  kd_server* v = new (std::nothrow) kd_server();
+  if (!v) return KD_ENOMEM;
+  v->st = &store->st;
+  v->s = s;
+  v->window_s = window_s;
+  v->budget = budget_bytes ? budget_bytes : ((size_t)1 << 40);
+  cudaSetDevice(s->device);
+  int rc = kd_pipeline_prepare_device(s);
+  if (rc == KD_OK && cudaStreamCreateWithFlags(&v->copy_stream, cudaStreamNonBlocking) != cudaSuccess) rc = KD_ECUDA;
+  if (rc) {
+    delete v;
+    return rc;
+  }
+  v->worker = std::thread(worker_main, v);
+  *out = v;
+  return KD_OK;
+}
+
+KD_API int kd_server_submit(kd_server* v, int kind, double timestamp, const uint32_t* keys,
+                            const double* vals, int64_t n, double* out, int64_t* ticket) {
+  if (!v || !ticket) return KD_EINVAL;
+  *ticket = 0;
+  if (kind != KD_REQ_INGEST && kind != KD_REQ_QUANTILE && kind != KD_REQ_CDF) return KD_EINVAL;
+  if (n < 0 || (n > 0 && !vals) || (kind != KD_REQ_INGEST && n > 0 && !out)) return KD_EINVAL;
+  if (!kd_isfinite(timestamp)) return KD_EINVAL;
+  const long long K = v->st->d.K;
+  // validate before admission: a bad request never reaches a batch
+  for (int64_t i = 0; i < n; ++i) {
+    if (keys && (long long)keys[i] >= K) return KD_EINVAL;
+    const double x = vals[i];
+    if (!kd_isfinite(x)) return KD_EINVAL;
+    if (kind == KD_REQ_QUANTILE && !(x >= 0.0 && x <= 1.0)) return KD_EINVAL;
+  }
+  auto r = std::make_shared<Req>();
+  r->kind = kind;
+  r->ts = timestamp;
+  r->window = v->window_of(timestamp);
+  r->keys.assign((size_t)n, 0u);
+  if (keys && n) memcpy(r->keys.data(), keys, (size_t)n * 4);
+  if (n) r->vals.assign(vals, vals + n);
+  r->out = out;
+  r->bytes = (size_t)n * (kind == KD_REQ_INGEST ? 12 : 20) + 64;
+  if (r->bytes > v->budget) return KD_ENOMEM;
+  std::unique_lock<std::mutex> lk(v->mu);
+  if (v->stop) return KD_EINVAL;
+  if (timestamp < v->last_ts) return KD_EINVAL;  // timestamps must not decrease
+  if (r->window < v->newest_window || (double)(r->window + 1) * v->window_s <= v->clock_ts)
+    return KD_EINVAL;  // its window is already closed
+  // admission: wait until the buffered requests leave room for this one
+  v->cv.wait(lk, [&] { return v->buffered + r->bytes <= v->budget || v->stop; });
+  if (v->stop) return KD_EINVAL;
+  r->id = v->next_id++;
+  r->t_submit = now_s();
+  v->last_ts = timestamp;
+  v->newest_window = std::max(v->newest_window, r->window);
+  v->buffered += r->bytes;
+  v->live[r->id] = r;
+  v->pending.push_back(r);
+  *ticket = r->id;
+  v->cv.notify_all();
+  return KD_OK;
+}
+
+KD_API int kd_server_advance(kd_server* v, double now_ts) {
+  if (!v || !kd_isfinite(now_ts)) return KD_EINVAL;
+  std::lock_guard<std::mutex> lk(v->mu);
+  v->clock_ts = std::max(v->clock_ts, now_ts);
+  v->cv.notify_all();
+  return KD_OK;
+}
+
+KD_API int kd_server_wait(kd_server* v, int64_t ticket, double timeout_s, int* status) {
+  if (!v || !status) return KD_EINVAL;
+  std::unique_lock<std::mutex> lk(v->mu);
+  auto it = v->live.find(ticket);
+  if (it == v->live.end()) return KD_EINVAL;
+  auto r = it->second;
+  auto done = [&] { return r->status >= 0; };
+  if (timeout_s < 0) {
+    v->cv.wait(lk, done);
+  } else if (!v->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), done)) {
+    return KD_ETIMEOUT;
+  }
+  *status = r->status;
+  v->live.erase(ticket);
+  return KD_OK;
+}
+
+KD_API int kd_server_flush(kd_server* v) {
+  if (!v) return KD_EINVAL;
+  std::unique_lock<std::mutex> lk(v->mu);
+  v->flushing = true;
+  v->cv.notify_all();
+  v->cv.wait(lk, [&] { return v->pending.empty() && v->buffered == 0; });
+  v->flushing = false;
+  // later requests open new windows after the flushed ones
+  v->clock_ts = std::max(v->clock_ts, (double)(v->newest_window + 1) * v->window_s);
+  return KD_OK;
+}
+
+KD_API int kd_server_stats(kd_server* v, double* lat3, int64_t* completed, int64_t* windows,
+                           double* busy_s) {
+  if (!v) return KD_EINVAL;
+  std::lock_guard<std::mutex> lk(v->mu);
+  if (lat3) {
+    std::vector<double> l = v->latencies;
+    std::sort(l.begin(), l.end());
+    const double ps[3] = {0.50, 0.99, 0.999};
+    for (int i = 0; i < 3; ++i) {
+      if (l.empty()) {
+        lat3[i] = 0.0;
+        continue;
+      }
+      size_t k = (size_t)std::ceil(ps[i] * (double)l.size());  // nearest rank
+      lat3[i] = l[std::min(l.size() - 1, k == 0 ? 0 : k - 1)];
+    }
+  }
+  if (completed) *completed = v->completed;
+  if (windows) *windows = v->windows_done;
+  if (busy_s) *busy_s = v->busy_s;
+  return KD_OK;
+}
+
+KD_API void kd_server_destroy(kd_server* v) {
+  if (!v) return;
+  {
+    std::lock_guard<std::mutex> lk(v->mu);
+    v->stop = true;  // remaining windows are processed before the worker exits
+    v->cv.notify_all();
+  }
+  if (v->worker.joinable()) v->worker.join();
+  cudaSetDevice(v->s->device);
+  cudaStreamSynchronize(v->s->stream);
+  for (Buf& b : v->buf) free_buf(b);
+  if (v->copy_stream) cudaStreamDestroy(v->copy_stream);
+  delete v;
+}
+
+}  // extern "C"

@@ -469,3 +469,83 @@ class GroupedTDigest:
         """Batched merge_into: key g of this store becomes the P-path merge of
         src keys parts[group_offsets[g]:group_offsets[g+1]] (in order)."""
         self._store.merge_from(src._store, group_offsets, parts)
+
+
+class Server:
+    """Serving loop over a resident digest store (no reference counterpart):
+    requests with non-decreasing timestamps are batched per window of the
+    timestamp axis by a native worker thread.  A window's queries see the store
+    before the window's ingests; the window's ingests are one grouped batch.
+    The store's session belongs to the server until close()."""
+
+    def __init__(self, digests, window: float = 1e-3, budget_bytes: int = 0):
+        self._digests = digests
+        store = digests._store
+        self.session = store.session
+        h = ctypes.c_void_p()
+        rc = N.load().kd_server_create(store._h, float(window), int(budget_bytes), ctypes.byref(h))
+        _check(self.session.handle, rc)
+        self._h = h.value
+        self._outs = {}  # ticket -> output array kept alive until waited
+
+    def _submit(self, kind, timestamp, keys, vals, out=None):
+        v = np.ascontiguousarray(vals, dtype=np.float64)
+        k = None if keys is None else np.ascontiguousarray(keys, dtype=np.uint32)
+        if k is not None and len(k) != len(v):
+            raise ValueError("keys and values must have equal length")
+        t = ctypes.c_int64(0)
+        rc = N.load().kd_server_submit(self._h, kind, float(timestamp), N.ptr(k), N.ptr(v), len(v),
+                                       N.ptr(out), ctypes.byref(t))
+        if rc:
+            raise KdError(rc, "request rejected (invalid input, closed window or over budget)")
+        return t.value
+
+    def submit_ingest(self, timestamp: float, keys, values) -> int:
+        return self._submit(N.KD_REQ_INGEST, timestamp, keys, values)
+
+    def submit_quantiles(self, timestamp: float, keys, qs) -> int:
+        out = np.empty(len(qs))
+        t = self._submit(N.KD_REQ_QUANTILE, timestamp, keys, qs, out)
+        self._outs[t] = out
+        return t
+
+    def submit_cdfs(self, timestamp: float, keys, xs) -> int:
+        out = np.empty(len(xs))
+        t = self._submit(N.KD_REQ_CDF, timestamp, keys, xs, out)
+        self._outs[t] = out
+        return t
+
+    def advance(self, now: float):
+        N.load().kd_server_advance(self._h, float(now))
+
+    def wait(self, ticket: int, timeout: float = -1.0):
+        """(status, outputs or None) of a request."""
+        st = ctypes.c_int(0)
+        rc = N.load().kd_server_wait(self._h, int(ticket), float(timeout), ctypes.byref(st))
+        if rc:
+            raise KdError(rc, "wait failed (unknown ticket or timeout)")
+        return st.value, self._outs.pop(ticket, None)
+
+    def flush(self):
+        N.load().kd_server_flush(self._h)
+
+    def stats(self) -> dict:
+        lat = np.zeros(3)
+        done = ctypes.c_int64(0)
+        wins = ctypes.c_int64(0)
+        busy = ctypes.c_double(0.0)
+        N.load().kd_server_stats(self._h, N.ptr(lat), ctypes.byref(done), ctypes.byref(wins),
+                                 ctypes.byref(busy))
+        return {"p50_s": lat[0], "p99_s": lat[1], "p999_s": lat[2], "completed": done.value,
+                "windows": wins.value, "busy_s": busy.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().kd_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

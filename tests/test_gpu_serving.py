@@ -1,0 +1,205 @@
+"""Serving loop: every request's result is the same alone and in the mix.
+
+"In the mix": the requests are submitted back to back by a client while the
+server batches them per window and overlaps the next window's copy with the
+current window's compute.  "Alone": each query request is evaluated by itself
+against the state its window defines, and each window's ingests are applied
+as one batch, one step at a time with no server.  Results are compared bit for
+bit (tolerance 0, inside the 1e-9 quantile/cdf tolerance), as is the final
+state of every digest.
+"""
+import math
+import threading
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NK = 400
+LAMBDA = math.log(2.0) / 60.0  # 60 s half-life on the timestamp axis
+
+
+def _trace(seed, n_req, gap, nk=NK):
+    rng = np.random.default_rng(seed)
+    ts = 0.002 + np.cumsum(rng.exponential(gap, n_req))
+    reqs = []
+    # the first request, alone in the first window, touches every key so that
+    # no later query meets an empty digest
+    reqs.append(("ingest", 0.0, np.arange(nk, dtype=np.uint32), rng.lognormal(0, 2, nk)))
+    for t in ts:
+        u = rng.random()
+        if u < 0.7:
+            n = int(min(2000, rng.lognormal(math.log(200), 1.0))) + 1
+            keys = (rng.zipf(1.2, n) - 1) % nk
+            reqs.append(("ingest", float(t), keys.astype(np.uint32), rng.lognormal(0, 2, n)))
+        elif u < 0.85:
+            n = int(rng.integers(1, 40))
+            qs = np.where(rng.random(n) < 0.5, rng.random(n), 10 ** rng.uniform(-6, -2, n))
+            reqs.append(("quantile", float(t), rng.integers(0, nk, n).astype(np.uint32), qs))
+        else:
+            n = int(rng.integers(1, 40))
+            reqs.append(("cdf", float(t), rng.integers(0, nk, n).astype(np.uint32),
+                         rng.lognormal(0, 2, n)))
+    return reqs
+
+
+def _store(kd):
+    return kd.GroupedTDigest(NK, 200.0, decay=kd.Decay.rate(LAMBDA), scale=kd.K2,
+                             session=kd.GpuSession())
+
+
+def _serve(kd, reqs, window, budget=0):
+    g = _store(kd)
+    srv = kd.Server(g, window=window, budget_bytes=budget)
+    tickets = []
+    for kind, t, k, v in reqs:
+        if kind == "ingest":
+            tickets.append(srv.submit_ingest(t, k, v))
+        elif kind == "quantile":
+            tickets.append(srv.submit_quantiles(t, k, v))
+        else:
+            tickets.append(srv.submit_cdfs(t, k, v))
+    srv.flush()
+    res = [srv.wait(tk, 30.0) for tk in tickets]
+    stats = srv.stats()
+    srv.close()
+    return g, res, stats
+
+
+def _alone(kd, reqs, window):
+    """Window semantics executed step by step, each query request by itself."""
+    g = _store(kd)
+    res = []
+    i = 0
+    while i < len(reqs):
+        w = math.floor(reqs[i][1] / window)
+        j = i
+        while j < len(reqs) and math.floor(reqs[j][1] / window) == w:
+            j += 1
+        ing_k, ing_v, ts = [], [], None
+        for kind, t, k, v in reqs[i:j]:
+            if kind == "ingest":
+                ing_k.append(k)
+                ing_v.append(v)
+                ts = t
+                res.append((0, None))
+            else:
+                out = g.quantiles(k, v) if kind == "quantile" else g.cdfs(k, v)
+                res.append((0, out))
+        if ing_k:
+            g.add_batch_at(np.concatenate(ing_k), np.concatenate(ing_v), ts)
+        i = j
+    return g, res
+
+
+def _compare(kd, ga, ra, gb, rb):
+    assert len(ra) == len(rb)
+    for (sa, oa), (sb, ob) in zip(ra, rb):
+        assert sa == sb == 0
+        if oa is None:
+            assert ob is None
+        else:
+            assert np.array_equal(oa, ob)
+    assert np.array_equal(ga.centroid_counts(), gb.centroid_counts())
+    for k in range(0, NK, 7):
+        ma, wa = ga.centroids(k)
+        mb, wb = gb.centroids(k)
+        assert np.array_equal(ma, mb) and np.array_equal(wa, wb)
+        assert ga.state(k) == gb.state(k)
+
+
+def test_results_same_alone_and_in_the_mix(kd):
+    reqs = _trace(11, 600, 2e-4)
+    window = 1e-3
+    ga, ra, st = _serve(kd, reqs, window)
+    gb, rb = _alone(kd, reqs, window)
+    _compare(kd, ga, ra, gb, rb)
+    assert st["completed"] == len(reqs)
+    assert st["windows"] < len(reqs) // 2  # requests were batched
+    assert 0.0 < st["p50_s"] <= st["p99_s"] <= st["p999_s"]
+
+
+def test_one_request_per_window_is_request_by_request(kd):
+    reqs = _trace(12, 150, 1e-3)
+    window = 1e-7  # gaps of ~1 ms: every request is alone in its window
+    assert len({math.floor(t / window) for _, t, _, _ in reqs}) == len(reqs)
+    ga, ra, _ = _serve(kd, reqs, window)
+    gb = _store(kd)
+    rb = []
+    for kind, t, k, v in reqs:
+        if kind == "ingest":
+            gb.add_batch_at(k, v, t)
+            rb.append((0, None))
+        else:
+            rb.append((0, gb.quantiles(k, v) if kind == "quantile" else gb.cdfs(k, v)))
+    _compare(kd, ga, ra, gb, rb)
+
+
+def test_budget_backpressure_keeps_results(kd):
+    reqs = _trace(13, 300, 2e-4)
+    window = 1e-3
+    ga, ra, _ = _serve(kd, reqs, window, budget=80_000)  # a few requests at a time
+    gb, rb = _alone(kd, reqs, window)
+    _compare(kd, ga, ra, gb, rb)
+
+
+def test_concurrent_waiters(kd):
+    """Waiters on other threads see their own results while the client submits."""
+    reqs = _trace(14, 200, 2e-4)
+    window = 1e-3
+    g = _store(kd)
+    srv = kd.Server(g, window=window)
+    results = {}
+
+    def waiter(tk):
+        results[tk] = srv.wait(tk, 30.0)
+
+    threads = []
+    for kind, t, k, v in reqs:
+        if kind == "ingest":
+            tk = srv.submit_ingest(t, k, v)
+        elif kind == "quantile":
+            tk = srv.submit_quantiles(t, k, v)
+        else:
+            tk = srv.submit_cdfs(t, k, v)
+        th = threading.Thread(target=waiter, args=(tk,))
+        th.start()
+        threads.append(th)
+    srv.advance(reqs[-1][1] + 1.0)
+    for th in threads:
+        th.join(60)
+    srv.close()
+    assert len(results) == len(reqs) and all(s == 0 for s, _ in results.values())
+
+
+def test_rejections_and_empty_digest(kd):
+    from kdigest_gb300 import KdError
+
+    g = _store(kd)
+    srv = kd.Server(g, window=1e-3, budget_bytes=10_000)
+    k = np.array([1, 2], dtype=np.uint32)
+    with pytest.raises(KdError):
+        srv.submit_ingest(0.5, np.array([NK], dtype=np.uint32), [1.0])  # key out of range
+    with pytest.raises(KdError):
+        srv.submit_ingest(0.5, k, [1.0, float("nan")])
+    with pytest.raises(KdError):
+        srv.submit_quantiles(0.5, k, [0.5, 1.5])
+    with pytest.raises(KdError):
+        srv.submit_ingest(0.5, np.zeros(2000, np.uint32), np.ones(2000))  # over budget
+    t0 = srv.submit_quantiles(0.5, k, [0.5, 0.5])  # empty digests
+    t1 = srv.submit_ingest(0.6, k, [3.0, 4.0])
+    with pytest.raises(KdError):
+        srv.submit_ingest(0.4, k, [1.0, 1.0])  # timestamps must not decrease
+    srv.advance(0.7)
+    with pytest.raises(KdError):
+        srv.submit_ingest(0.65, k, [1.0, 1.0])  # its window [0.650, 0.651) closed
+    st0, out0 = srv.wait(t0, 30.0)
+    st1, _ = srv.wait(t1, 30.0)
+    assert st0 == 2 and np.isnan(out0).all()  # KD_EEMPTY
+    assert st1 == 0
+    t2 = srv.submit_quantiles(0.8, k, [0.5, 0.5])
+    srv.flush()
+    st2, out2 = srv.wait(t2, 30.0)
+    assert st2 == 0 and np.array_equal(out2, [3.0, 4.0])
+    srv.close()
