@@ -209,6 +209,119 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------------------
+# Serving (config 5): 1,000,000 resident K2 (compression 200) digests with a
+# 60 s half-life on simulated monotone timestamps; Poisson arrivals; 70% ingest
+# requests of lognormal size (median 4096, sigma 1, capped at 2^20 pairs) with
+# Zipf(1.2) keys and lognormal(0, 2) values, 30% query requests of 1..1024
+# uniform (key, q) pairs; a 100 GB admission budget.
+# ----------------------------------------------------------------------------
+SERVE_KEYS = 1_000_000
+SERVE_RATE = 20_000.0
+SERVE_POOL = 1 << 25
+
+
+def make_serve_pool(seed: int = SEED + 5, num_keys: int = SERVE_KEYS, size: int = SERVE_POOL):
+    """Pairs that ingest requests take slices of (keys Zipf(1.2) over a seeded
+    rank->id permutation, values lognormal(0, 2))."""
+    rng = np.random.default_rng(seed)
+    p = 1.0 / np.arange(1, num_keys + 1, dtype=np.float64) ** 1.2
+    cdf = np.cumsum(p)
+    cdf /= cdf[-1]
+    perm = rng.permutation(num_keys).astype(np.uint32)
+    keys = np.empty(size, np.uint32)
+    vals = np.empty(size, np.float64)
+    parts = max(1, min(32, size >> 20))
+    seeds = np.random.SeedSequence(seed + 1).spawn(parts)
+    bounds = np.linspace(0, size, parts + 1).astype(np.int64)
+
+    def fill(i):
+        r = np.random.default_rng(seeds[i])
+        lo, hi = bounds[i], bounds[i + 1]
+        u = r.random(hi - lo)
+        keys[lo:hi] = perm[np.minimum(np.searchsorted(cdf, u, side="right"), num_keys - 1)]
+        vals[lo:hi] = r.lognormal(0.0, 2.0, hi - lo)
+
+    th = [threading.Thread(target=fill, args=(i,)) for i in range(parts)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    return keys, vals
+
+
+def make_serve_trace(seconds: float, rate: float = SERVE_RATE, seed: int = SEED + 7,
+                     num_keys: int = SERVE_KEYS, pool: int = SERVE_POOL):
+    """Arrival times (Poisson), kinds, sizes, pool offsets and query pairs."""
+    rng = np.random.default_rng(seed)
+    n = int(rate * seconds * 1.1) + 16
+    arr = np.cumsum(rng.exponential(1.0 / rate, n))
+    arr = arr[arr < seconds]
+    m = len(arr)
+    ingest = rng.random(m) < 0.7
+    sizes = np.where(ingest, np.minimum(1 << 20, np.maximum(1, np.rint(
+        rng.lognormal(np.log(4096.0), 1.0, m)))), rng.integers(1, 1025, m)).astype(np.int64)
+    offs = (rng.random(m) * (pool - sizes)).astype(np.int64)
+    nq = int(sizes[~ingest].sum())
+    qkeys = rng.integers(0, num_keys, nq).astype(np.uint32)
+    qvals = rng.random(nq)
+    return arr, ingest, sizes, offs, qkeys, qvals
+
+
+def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
+    """Open-loop client at `rate` requests/s against the serving loop; returns
+    latency percentiles (submit -> completion) and throughput."""
+    import kdigest_gb300 as kd
+
+    sess = kd.GpuSession()
+    store = kd.GroupedTDigest(SERVE_KEYS, 200.0, decay=kd.Decay.half_life(60.0), scale=kd.K2,
+                              session=sess)
+    srv = kd.Server(store, window=window, budget_bytes=100 << 30)
+    pk, pv = make_serve_pool()
+    arr, ingest, sizes, offs, qkeys, qvals = make_serve_trace(seconds, rate)
+    tickets = []
+    lag = 0.0
+    qo = 0
+    t0 = time.perf_counter()
+    for i in range(len(arr)):
+        target = t0 + arr[i]
+        now = time.perf_counter()
+        while now < target:
+            now = time.perf_counter()
+        lag = max(lag, now - target)
+        n = int(sizes[i])
+        if ingest[i]:
+            o = int(offs[i])
+            tickets.append(srv.submit_ingest(arr[i], pk[o:o + n], pv[o:o + n]))
+        else:
+            tickets.append(srv.submit_quantiles(arr[i], qkeys[qo:qo + n], qvals[qo:qo + n]))
+            qo += n
+        # nothing earlier than the next arrival can come: windows ending by then close
+        srv.advance(arr[i + 1] if i + 1 < len(arr) else arr[i] + window)
+    t_sub = time.perf_counter() - t0
+    srv.flush()
+    t_all = time.perf_counter() - t0
+    st = srv.stats()
+    statuses = {}
+    for tk in tickets:
+        s, _ = srv.wait(tk, 60.0)
+        statuses[s] = statuses.get(s, 0) + 1
+    srv.close()
+    ing_pairs = int(sizes[ingest].sum())
+    q_pairs = int(sizes[~ingest].sum())
+    return {
+        "p50_ms": round(st["p50_s"] * 1e3, 3), "p99_ms": round(st["p99_s"] * 1e3, 3),
+        "p999_ms": round(st["p999_s"] * 1e3, 3), "requests": len(arr),
+        "seconds": seconds, "window_ms": window * 1e3, "offered_req_per_s": rate,
+        "achieved_req_per_s": round(len(arr) / t_all, 1),
+        "ingest_pairs_per_s": round(ing_pairs / t_all, 1),
+        "query_pairs_per_s": round(q_pairs / t_all, 1),
+        "windows": st["windows"], "gpu_worker_busy_frac": round(st["busy_s"] / t_all, 3),
+        "client_max_lag_ms": round(lag * 1e3, 3), "submit_seconds": round(t_sub, 3),
+        "status_counts": {str(k): v for k, v in sorted(statuses.items())},
+    }
+
+
+# ----------------------------------------------------------------------------
 # Replicas (N > 1): every rank ingests its own copy of the stream on its own
 # GPU; no collective touches the data path.
 # ----------------------------------------------------------------------------
@@ -424,6 +537,10 @@ def run_gpu(args):
         cpu = {"value": v, "unit": "samples/s", "cores": threads, "kind": "port",
                "sample": f"first {done} batches of 2^22 pairs ({t:.1f} s, C oracle P-path, key-partitioned threads)"}
 
+    serving = None
+    if not args.no_serve and rank == 0 and world == 1:
+        serving = run_serve(args.serve_seconds or 3.0, args.serve_window, args.serve_rate)
+
     line = {
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
@@ -442,6 +559,7 @@ def run_gpu(args):
         "e2e": e2e,
         "gpu_launches": st["launches"],
         "clocks": clocks,
+        "serving": serving,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -462,12 +580,30 @@ def main():
     ap.add_argument("--plain-seconds", type=float, default=30.0)
     ap.add_argument("--total", type=int, default=TOTAL,
                     help="stream length (samples); smaller values are for profiling only")
+    ap.add_argument("--serve", action="store_true",
+                    help="run only the serving benchmark (config 5) and print its line")
+    ap.add_argument("--serve-seconds", type=float, default=None)
+    ap.add_argument("--serve-window", type=float, default=1e-3)
+    ap.add_argument("--serve-rate", type=float, default=SERVE_RATE)
+    ap.add_argument("--no-serve", action="store_true")
     args = ap.parse_args()
     TOTAL = args.total
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.serve:
+        import torch  # noqa: F401  (CUDA context before the worker thread)
+
+        r = run_serve(args.serve_seconds or 10.0, args.serve_window, args.serve_rate)
+        line = {"metric": "serving p99 latency (1M K2 d200 keys, 60 s half-life, Poisson arrivals)",
+                "value": r["p99_ms"], "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+                "dtype": "f64", "data": "synthetic (seeded numpy trace, open-loop client)",
+                "config": {"workload": "serving loop, config 5", "keys": SERVE_KEYS,
+                           "scale": "K2", "compression": 200.0, "half_life_s": 60.0,
+                           "budget_bytes": 100 << 30}, **r}
+        print(json.dumps(line), flush=True)
+        return 0
     if not os.path.exists(os.path.join(ROOT, "kdigest_gb300", "libkdigest_gb300.so")):
         from kdigest_gb300 import build as kb
 

@@ -259,6 +259,8 @@ void run_window(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>*
       r->status = stt;
     }
     r->t_done = t1;
+    std::vector<uint32_t>().swap(r->keys);  // the data is consumed: release it now
+    std::vector<double>().swap(r->vals);
     v->latencies.push_back(t1 - r->t_submit);
     v->buffered -= std::min(v->buffered, r->bytes);
     ++v->completed;
