@@ -57,6 +57,11 @@ extern "C" {
 #define KD_OPT_MAX_LEVELS 2    /* cap on tile-hierarchy levels per ingest (default 32) */
 #define KD_OPT_STAGE_TIMING 3  /* record CUDA events between ingest stages */
 #define KD_OPT_GRAPHS 4        /* capture repeated ingest steps as CUDA graphs (default on) */
+/* Launch tuning; results never depend on it (kdigest_gb300/tuning/ holds the
+ * autotuner's record for GB300, whose choice is the default). */
+#define KD_OPT_SMALL_TILE_CAP 5       /* largest tile for the small-tile kernel, 1..128 */
+#define KD_OPT_LARGE_BLOCKS_PER_SM 6  /* grid of the large-tile kernel, blocks per SM */
+#define KD_OPT_SMALL_BLOCKS_PER_SM 7  /* grid of the small-tile kernel, blocks per SM */
 
 typedef struct kd_session kd_session;
 typedef struct kd_store kd_store;

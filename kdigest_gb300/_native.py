@@ -18,6 +18,7 @@ KD_K0, KD_K1, KD_K2, KD_K3 = 0, 1, 2, 3
 KD_CLOCK_COUNT, KD_CLOCK_TIME = 0, 1
 KD_PTR_DEVICE = 1
 KD_OPT_FORCE_EXACT_K, KD_OPT_MAX_LEVELS, KD_OPT_STAGE_TIMING, KD_OPT_GRAPHS = 1, 2, 3, 4
+KD_OPT_SMALL_TILE_CAP, KD_OPT_LARGE_BLOCKS_PER_SM, KD_OPT_SMALL_BLOCKS_PER_SM = 5, 6, 7
 STAGES = ("prep", "sort", "plan", "level0", "levels", "commit")
 
 EXPORTED = (

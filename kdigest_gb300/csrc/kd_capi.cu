@@ -428,6 +428,15 @@ KD_API int kd_session_set_option(kd_session* h, int option, int value) {
     s->max_levels = value;
   } else if (option == KD_OPT_GRAPHS) {
     s->use_graphs = value ? 1 : 0;
+  } else if (option == KD_OPT_SMALL_TILE_CAP) {
+    if (value < 1 || value > KD_SERIAL_TILE_MAX) return fail(s, KD_EINVAL, "small tile cap must be in [1, 128]");
+    s->small_cap = value;
+  } else if (option == KD_OPT_LARGE_BLOCKS_PER_SM) {
+    if (value < 1 || value > 64) return fail(s, KD_EINVAL, "blocks per SM must be in [1, 64]");
+    s->large_bps = value;
+  } else if (option == KD_OPT_SMALL_BLOCKS_PER_SM) {
+    if (value < 1 || value > 64) return fail(s, KD_EINVAL, "blocks per SM must be in [1, 64]");
+    s->small_bps = value;
   } else {
     return fail(s, KD_EINVAL, "unknown option");
   }

@@ -157,6 +157,12 @@ struct KdSession {
   int force_exact = 0;
   int max_levels = 32;
   int use_graphs = 1;  // capture repeated ingest steps as CUDA graphs
+  // Launch tuning (results never depend on these): the largest partial tile
+  // sent to the small-tile kernel, and resident blocks per SM of the two tile
+  // kernels.  Defaults are the committed autotuner choice for GB300.
+  int small_cap = 128;
+  int large_bps = 7;
+  int small_bps = 12;
   char last_error[256] = {0};  // fixed buffer: reporting an error never allocates
   KdWorkspace ws;
   KdStageStats stats;
@@ -169,12 +175,14 @@ struct KdGraphKey {
   long long n = -1;
   int key_bits = 0, with_idx = 0, mode = 0, levels = 0, force_exact = 0, timing = 0;
   int scale = 0;
+  int tuning = 0;
   double compression = 0.0;
   unsigned long long generation = 0;
   bool operator==(const KdGraphKey& o) const {
     return n == o.n && key_bits == o.key_bits && with_idx == o.with_idx && mode == o.mode &&
            levels == o.levels && force_exact == o.force_exact && timing == o.timing &&
-           scale == o.scale && compression == o.compression && generation == o.generation;
+           scale == o.scale && tuning == o.tuning && compression == o.compression &&
+           generation == o.generation;
   }
 };
 struct KdGraphEntry {

@@ -567,25 +567,29 @@ __global__ void k_prepare(PrepareArgs a) {
 }
 
 // Tiles of a key with m input elements: floor(m/1024) full tiles plus a partial
-// tile of r = m mod 1024 elements; only that partial tile can be small.
+// tile of r = m mod 1024 elements; only that partial tile can be small.  A
+// small tile (r <= cap, cap <= KD_SERIAL_TILE_MAX) goes to the small-tile
+// kernel, every other tile to the large-tile kernel.  The split only chooses
+// the kernel: both compute a tile in the same canonical order, so cap is a
+// tuning parameter that never changes a result.
 struct TileSplit {
   int small, large;
 };
-__device__ __forceinline__ TileSplit tile_split(int m) {
+__device__ __forceinline__ TileSplit tile_split(int m, int cap) {
   const int full = m / KD_TILE, r = m - full * KD_TILE;
   TileSplit t;
-  t.small = (r > 0 && r <= KD_SERIAL_TILE_MAX) ? 1 : 0;
-  t.large = full + (r > KD_SERIAL_TILE_MAX ? 1 : 0);
+  t.small = (r > 0 && r <= cap) ? 1 : 0;
+  t.large = full + (r > cap ? 1 : 0);
   return t;
 }
 __device__ __forceinline__ void write_work(const KdLevelDev& lv, int a, int m, int s_off, int l_off,
-                                           long long cap_work) {
+                                           long long cap_work, int cap) {
   const int full = m / KD_TILE, r = m - full * KD_TILE;
   int nl = full;
-  if (r > KD_SERIAL_TILE_MAX) ++nl;
+  if (r > cap) ++nl;
   for (int lt = 0; lt < nl; ++lt)
     if (l_off + lt < cap_work) lv.work_l[l_off + lt] = make_int2(a, lt);
-  if (r > 0 && r <= KD_SERIAL_TILE_MAX && s_off < cap_work) lv.work_s[s_off] = make_int2(a, full);
+  if (r > 0 && r <= cap && s_off < cap_work) lv.work_s[s_off] = make_int2(a, full);
 }
 
 // Level-0 plan over the touched keys: small / large tiles, multi-tile keys and
@@ -593,10 +597,11 @@ __device__ __forceinline__ void write_work(const KdLevelDev& lv, int a, int m, i
 struct Plan0Src {
   const int4* totals;
   const int* tm;
+  int small_cap;
   __device__ int4 operator()(long long j) const {
     if (j >= totals[0].x) return make_int4(0, 0, 0, 0);
     const int m = tm[j];
-    const TileSplit t = tile_split(m);
+    const TileSplit t = tile_split(m, small_cap);
     return make_int4(t.small, t.large, m > KD_TILE ? 1 : 0, m);
   }
 };
@@ -607,12 +612,13 @@ struct Plan0Dst {
   KdLevelDev nxt;
   long long cap_work;
   long long cap_keys;
+  int small_cap;
   __device__ void operator()(long long j, int4 excl, int4 v) const {
     if (j >= totals[0].x) return;
     cur.j[j] = (int)j;
     cur.m[j] = v.w;
     cur.base[j] = excl.w;
-    write_work(cur, (int)j, v.w, excl.x, excl.y, cap_work);
+    write_work(cur, (int)j, v.w, excl.x, excl.y, cap_work, small_cap);
     if (v.z && excl.z < cap_keys) {
       nxt.j[excl.z] = (int)j;
       nxt.src_tiles[excl.z] = v.x + v.y;
@@ -869,6 +875,7 @@ struct PlanArgs {
   long long cap_inter;
   long long cap_keys;
   long long cap_merged;
+  int small_cap;
   int* needs;
   KdErrHost* err;
 };
@@ -920,7 +927,7 @@ __global__ void __launch_bounds__(1024) k_plan(PlanArgs p) {
     p.cur.base[a] = base;
     p.cur.m[a] = m;
     if (m >= p.cur.mprev[a]) kd_err_set(p.err, KD_ECONVERGE, (long long)p.tkey[p.cur.j[a]]);
-    const TileSplit t = tile_split(m);
+    const TileSplit t = tile_split(m, p.small_cap);
     const bool fin = m <= KD_TILE;
     acc = i4add(acc, make_int4(t.small, t.large, fin ? 0 : 1, m));
     acc_inter += fin ? 0 : t.small + t.large;
@@ -932,10 +939,10 @@ __global__ void __launch_bounds__(1024) k_plan(PlanArgs p) {
   int run_inter = incl2.x - acc_inter;
   for (int a = a0; a < a1; ++a) {
     const int m = p.cur.m[a];
-    const TileSplit t = tile_split(m);
+    const TileSplit t = tile_split(m, p.small_cap);
     const bool fin = m <= KD_TILE;
     p.cur.inter_off[a] = run_inter;
-    write_work(p.cur, a, m, run.x, run.y, p.cap_work);
+    write_work(p.cur, a, m, run.x, run.y, p.cap_work, p.small_cap);
     if (!fin && run.z < p.cap_keys) {
       p.nxt.j[run.z] = p.cur.j[a];
       p.nxt.src_base[run.z] = run_inter;
@@ -1291,7 +1298,6 @@ static const char* err_text(int code) {
   }
 }
 
-static int level_grid(KdSession* s) { return s->num_sms * 6; }
 
 static size_t tile_smem() { return sizeof(WarpTile); }
 static size_t tile_smem_small() { return sizeof(WarpTileSmall) * 4; }
@@ -1350,8 +1356,8 @@ static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, co
   TileArgs ta{sd, lv.Tl, lv.Ts, lv.I, lv, dx, dw, w.tkey, w.tbuf, w.st_count, w.scr_m,
               w.scr_w, w.tcount, w.cap_work, w.cap_inter, w.needs, s->force_exact, id_last,
               w.err};
-  k_tiles<KD_TILE><<<level_grid(s), 32, tile_smem(), str>>>(ta);
-  k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * 8, 128, tile_smem_small(), str>>>(ta);
+  k_tiles<KD_TILE><<<s->num_sms * s->large_bps, 32, tile_smem(), str>>>(ta);
+  k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * s->small_bps, 128, tile_smem_small(), str>>>(ta);
   v.launches += 2;
 }
 
@@ -1365,7 +1371,7 @@ static void enqueue_levels(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, i
     KdLevelDev nxt = w.lv[(L + 1) & 1];
     cur.A = const_cast<int*>(v.curA);
     PlanArgs pa{v.curA, v.Iprev, cur, nxt, w.tcount, w.doff, w.tkey, w.cap_work, w.cap_inter,
-                w.cap_keys, w.cap_merged, w.needs, w.err};
+                w.cap_keys, w.cap_merged, s->small_cap, w.needs, w.err};
     k_plan<<<1, 1024, 0, str>>>(pa);
     CompactArgs ca{v.Iprev, w.tcount, w.doff, w.scr_m, w.scr_w, w.dx[L & 1], w.dw[L & 1], w.err};
     k_compact<<<s->num_sms * 4, 256, 0, str>>>(ca);
@@ -1434,8 +1440,9 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   l0.M = (int*)&w.totals[1] + 3;
   l0.I = (int*)&w.totals[2] + 0;
   int* a1 = (int*)&w.totals[1] + 2;
-  kd_scan(Plan0Src{w.totals, w.tm}, Plan0Dst{w.totals, w.tm, l0, w.lv[1], w.cap_work, w.cap_keys},
-          keys_max, w.partials, &w.totals[1], str);
+  kd_scan(Plan0Src{w.totals, w.tm, s->small_cap},
+          Plan0Dst{w.totals, w.tm, l0, w.lv[1], w.cap_work, w.cap_keys, s->small_cap}, keys_max,
+          w.partials, &w.totals[1], str);
   {
     InterArgs ia{a1, l0, w.lv[1], l0.I, w.cap_inter, w.needs, w.err};
     k_inter0<<<1, 1024, 0, str>>>(ia);
@@ -1498,6 +1505,7 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
   key.scale = sd.scale;
   key.compression = sd.compression;
   key.generation = w.generation;
+  key.tuning = s->small_cap | (s->large_bps << 8) | (s->small_bps << 16);
   KdStepView v;
   bool ran = false;
   if (s->use_graphs && w.generation != 0) {

@@ -71,7 +71,7 @@ class Decay:
 class GpuSession:
     """One device, one CUDA stream, reusable workspaces (gpu/session.mojo)."""
 
-    def __init__(self, device: int = 0, mem_budget: int = 0):
+    def __init__(self, device: int = 0, mem_budget: int = 0, tuned: bool = True):
         L = N.load()
         h = ctypes.c_void_p()
         rc = L.kd_session_create(device, mem_budget, ctypes.byref(h))
@@ -79,6 +79,10 @@ class GpuSession:
             raise KdError(rc, f"kd_session_create failed ({L.kd_status_string(rc).decode()})")
         self._h = h.value
         self.device = device
+        if tuned:  # launch parameters chosen by the committed autotuner run
+            from .tune import apply_tuning, load_tuning
+
+            apply_tuning(self, load_tuning())
 
     @property
     def handle(self):

@@ -1,0 +1,171 @@
+"""Autotuner for the launch parameters of the grouped ingest step.
+
+The tile hierarchy sends every tile to one of two kernels: a small-tile kernel
+(four warps per block, one tile of at most KD_OPT_SMALL_TILE_CAP elements per
+warp) and a large-tile kernel (one warp per tile).  Which kernel takes a
+partial tile, and how many blocks per SM each kernel's grid holds, only move
+work between kernels: both compute a tile in the same canonical order, so the
+results are identical for every setting (the tuner checks this).
+
+The tuner builds a store in the steady state of a Zipf-keyed grouped ingest
+(65,536 K3 keys, compression 100, 2^22-sample batches: digests have filled
+up), then runs a coordinate descent over
+    small tile cap   in {32, 64, 96, 128}
+    large blocks/SM  in {4, 5, 6, 7, 8}
+    small blocks/SM  in {4, 6, 8, 12, 16}
+timing each candidate as the median device time (CUDA events on the session
+stream) of several ingest steps, and writes the measurements and the choice to
+tuning/gb300.json.  GpuSession applies that file's choice; the library's
+built-in defaults (KdSession in csrc/kd_engine.h) are set to it.
+
+    python -m kdigest_gb300.tune [--out kdigest_gb300/tuning/gb300.json]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TUNING_FILE = os.path.join(HERE, "tuning", "gb300.json")
+PARAMS = (("small_tile_cap", 5, (32, 64, 96, 128)),
+          ("large_blocks_per_sm", 6, (4, 5, 6, 7, 8)),
+          ("small_blocks_per_sm", 7, (4, 6, 8, 12, 16)))
+# the starting point of the search (the launch shapes before tuning)
+DEFAULTS = {"small_tile_cap": 128, "large_blocks_per_sm": 6, "small_blocks_per_sm": 8}
+
+
+def load_tuning(path: str = TUNING_FILE) -> dict:
+    """The committed choice ({} when there is none)."""
+    try:
+        with open(path) as f:
+            return dict(json.load(f).get("choice", {}))
+    except (OSError, ValueError):
+        return {}
+
+
+def apply_tuning(session, choice: dict):
+    for name, opt, _ in PARAMS:
+        if name in choice:
+            session.set_option(opt, int(choice[name]))
+
+
+def _stream(seed: int, num_keys: int, batch: int, batches: int):
+    rng = np.random.default_rng(seed)
+    p = 1.0 / np.arange(1, num_keys + 1, dtype=np.float64) ** 1.1
+    cdf = np.cumsum(p)
+    cdf /= cdf[-1]
+    perm = rng.permutation(num_keys).astype(np.uint32)
+    mu = rng.uniform(-100.0, 100.0, num_keys)
+    out = []
+    for _ in range(batches):
+        k = perm[np.minimum(np.searchsorted(cdf, rng.random(batch), side="right"), num_keys - 1)]
+        out.append((k, rng.standard_normal(batch) + mu[k]))
+    return out
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=TUNING_FILE)
+    ap.add_argument("--keys", type=int, default=65536)
+    ap.add_argument("--batch", type=int, default=1 << 22)
+    ap.add_argument("--steps", type=int, default=5)
+    args = ap.parse_args(argv)
+
+    import torch
+
+    import kdigest_gb300 as kd
+    from kdigest_gb300 import _native as N
+
+    dev = torch.device("cuda", 0)
+    batches = _stream(7, args.keys, args.batch, 16)
+    d_batches = [(torch.from_numpy(k).to(dev), torch.from_numpy(v).to(dev)) for k, v in batches]
+    sess = kd.GpuSession(0, tuned=False)
+    ext = torch.cuda.ExternalStream(sess.stream, device=dev)
+    store = kd.GroupedTDigest(args.keys, 100.0, scale=kd.K3, session=sess)
+    L = N.load()
+    h = store._store._h
+    step_no = [0]
+
+    def step():
+        k, v = d_batches[step_no[0] % len(d_batches)]
+        step_no[0] += 1
+        rc = L.kd_store_ingest(h, k.data_ptr(), v.data_ptr(), args.batch, N.KD_CLOCK_COUNT, 0.0,
+                               N.KD_PTR_DEVICE)
+        if rc:
+            raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+
+    for _ in range(2 * len(d_batches)):  # steady state: digests filled up
+        step()
+    torch.cuda.synchronize()
+
+    def measure(cfg: dict) -> float:
+        apply_tuning(sess, cfg)
+        step()  # first step of a new shape runs eagerly, the second captures
+        step()
+        times = []
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            step()
+            e1.record(ext)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return statistics.median(times)
+
+    cur = dict(DEFAULTS)
+    log = []
+    best = measure(cur)
+    log.append({**cur, "ms": best})
+    for _round in range(2):
+        for name, _, values in PARAMS:
+            for val in values:
+                if val == cur[name]:
+                    continue
+                cand = {**cur, name: val}
+                ms = measure(cand)
+                log.append({**cand, "ms": ms})
+                if ms < best * 0.99:  # keep a change only for a clear gain
+                    best, cur = ms, cand
+    default_ms = measure(DEFAULTS)
+    chosen_ms = measure(cur)
+
+    # The choice must not change results: same stream, two fresh stores.
+    same = True
+    stores = []
+    for cfg in (DEFAULTS, cur):
+        s2 = kd.GpuSession(0, tuned=False)
+        apply_tuning(s2, cfg)
+        g = kd.GroupedTDigest(args.keys, 100.0, scale=kd.K3, session=s2)
+        for k, v in batches[:6]:
+            g.add_batch(k, v)
+        stores.append(g)
+    same = bool(np.array_equal(stores[0].centroid_counts(), stores[1].centroid_counts()))
+    for key in range(0, args.keys, 997):
+        ma, wa = stores[0].centroids(key)
+        mb, wb = stores[1].centroids(key)
+        same = same and np.array_equal(ma, mb) and np.array_equal(wa, wb)
+
+    rec = {
+        "device": torch.cuda.get_device_name(0),
+        "sms": torch.cuda.get_device_properties(0).multi_processor_count,
+        "workload": f"grouped ingest, {args.keys} Zipf(1.1) K3 keys, compression 100, "
+                    f"batches of {args.batch} in steady state",
+        "timing": f"median of {args.steps} steps, CUDA events on the session stream",
+        "default": DEFAULTS, "default_ms": default_ms,
+        "choice": cur, "choice_ms": chosen_ms, "results_identical": same,
+        "measurements": log,
+    }
+    os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+    with open(args.out, "w") as f:
+        json.dump(rec, f, indent=1)
+    print(json.dumps({k: rec[k] for k in ("choice", "choice_ms", "default_ms", "results_identical")}))
+    return 0 if same else 1
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -119,3 +119,23 @@ def test_replays_with_stage_timing(kd):
     assert st["ingests"] == 6 and st["launches"] > 6 * 20
     assert all(v > 0.0 for v in st["stage_ms"].values()), st
     _same(g, e, nk)
+
+
+def test_launch_tuning_never_changes_results(kd):
+    """Every tile-kernel split and grid gives the same digests."""
+    nk, n = 500, 60000
+    rng = np.random.default_rng(7)
+    batches = [(rng.zipf(1.2, n) % nk, rng.standard_normal(n) * 3.0) for _ in range(4)]
+    ref = None
+    for cap, lb, sb in ((128, 6, 8), (32, 4, 16), (64, 8, 4), (1, 1, 1)):
+        s = kd.GpuSession(tuned=False)
+        s.set_option(5, cap)
+        s.set_option(6, lb)
+        s.set_option(7, sb)
+        g = kd.GroupedTDigest(nk, 100.0, scale=kd.K3, session=s)
+        for k, v in batches:
+            g.add_batch(k, v)
+        if ref is None:
+            ref = g
+        else:
+            _same(g, ref, nk)
