@@ -26,6 +26,8 @@ import sys
 import threading
 import time
 
+import math
+
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -203,6 +205,321 @@ def run_reference(args):
         "cpu_baseline": {"value": v, "unit": "samples/s", "cores": threads, "kind": "port",
                          "sample": f"{k} batches of 2^22 pairs of the stream (C oracle, P-path, key-partitioned threads)"},
         "e2e": {"value": v, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# Accuracy: rank error against an exact FP64 sort
+# ----------------------------------------------------------------------------
+def rank_error_ppm(values_sorted: np.ndarray, estimates: np.ndarray, qs, weights_cum=None):
+    """|F(estimate) - q| in ppm, F the empirical CDF of the sorted values with
+    ties counted half (weights_cum: cumulative weights of the sorted values
+    for a weighted distribution)."""
+    lo = np.searchsorted(values_sorted, estimates, side="left")
+    hi = np.searchsorted(values_sorted, estimates, side="right")
+    if weights_cum is None:
+        f = (lo + hi) / 2.0 / len(values_sorted)
+    else:
+        wc = np.concatenate([[0.0], weights_cum])
+        f = (wc[lo] + wc[hi]) / 2.0 / wc[-1]
+    return np.abs(f - np.asarray(qs, dtype=np.float64)) * 1e6
+
+
+def grouped_rank_error(store, keys, vals, ingested_batches, batch, num_keys, nsample=256):
+    """Per-quantile rank error (ppm) of `nsample` keys spread over the
+    frequency ranks, against the exact sort of everything they ingested."""
+    sel_b = [(b * batch, (b + 1) * batch) for b in ingested_batches]
+    counts = np.zeros(num_keys, np.int64)
+    for lo, hi in sel_b:
+        counts += np.bincount(keys[lo:hi], minlength=num_keys)
+    order = np.argsort(-counts, kind="stable")
+    pos = np.unique(np.round(np.logspace(0, np.log10(num_keys), nsample)).astype(np.int64)) - 1
+    sel = order[pos]
+    sel = sel[counts[sel] >= 2]
+    lut = np.zeros(num_keys, bool)
+    lut[sel] = True
+    kk = np.concatenate([keys[lo:hi][lut[keys[lo:hi]]] for lo, hi in sel_b])
+    vv = np.concatenate([vals[lo:hi][lut[keys[lo:hi]]] for lo, hi in sel_b])
+    o = np.argsort(kk, kind="stable")
+    kk, vv = kk[o], vv[o]
+    starts = np.searchsorted(kk, sel, side="left")
+    ends = np.searchsorted(kk, sel, side="right")
+    qs = np.array(QUANTILES)
+    est = store.quantiles(np.repeat(sel, len(qs)), np.tile(qs, len(sel))).reshape(len(sel), len(qs))
+    errs = np.stack([rank_error_ppm(np.sort(vv[a:b]), est[i], qs) for i, (a, b) in
+                     enumerate(zip(starts, ends))])
+    return {"q": list(QUANTILES), "mean_ppm": [round(x, 1) for x in errs.mean(0)],
+            "max_ppm": [round(x, 1) for x in errs.max(0)], "keys": int(len(sel)),
+            "samples_per_key": [int((ends - starts).min()), int(np.median(ends - starts)),
+                                int((ends - starts).max())],
+            "oracle": "identical (the digests equal the oracle's bit for bit)"}
+
+
+# ----------------------------------------------------------------------------
+# Config 2: one K2 digest (compression 200), Decay.half_life(1e6 samples),
+# 2^26 lognormal(mu_t, 1.5) samples with mu_t drifting 0 -> 2, batches of 2^20,
+# then 4096 quantiles (2048 uniform, 1024 log-uniform in [1e-6, 1e-2] and their
+# mirrors).  This is the plain single-digest form.
+# ----------------------------------------------------------------------------
+C2_TOTAL = 1 << 26
+C2_BATCH = 1 << 20
+
+
+def c2_queries(seed: int = SEED + 2):
+    r = np.random.default_rng(seed)
+    tails = 10 ** r.uniform(-6, -2, 1024)
+    return np.concatenate([r.random(2048), tails, 1.0 - tails])
+
+
+def run_config2(args) -> int:
+    import torch
+
+    import kdigest_gb300 as kd
+    from kdigest_gb300 import _native as N
+
+    dev = torch.device("cuda", 0)
+    gen = torch.Generator(device=dev).manual_seed(SEED + 22)
+    t = torch.arange(C2_TOTAL, dtype=torch.float64, device=dev)
+    mu = 2.0 * t / (C2_TOTAL - 1)
+    vals = torch.exp(mu + 1.5 * torch.randn(C2_TOTAL, dtype=torch.float64, device=dev,
+                                            generator=gen)).contiguous()
+    del t, mu
+    nb = C2_TOTAL // C2_BATCH
+    sess = kd.GpuSession()
+    ext = torch.cuda.ExternalStream(sess.stream, device=dev)
+    d = kd.TDigest(200.0, kd.K2, decay=kd.Decay.half_life(1e6), session=sess)
+    L = N.load()
+    h = d._store._h
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def ingest(b):
+        rc = L.kd_store_ingest(h, None, vals.data_ptr() + b * C2_BATCH * 8, C2_BATCH,
+                               N.KD_CLOCK_COUNT, 0.0, N.KD_PTR_DEVICE)
+        if rc:
+            raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+
+    steps = min(args.steps if args.steps_given else nb - args.warmup, nb - args.warmup)
+    for b in range(args.warmup):
+        ingest(b)
+    torch.cuda.synchronize()
+    sess.reset_stats()
+    times = []
+    sampler = ClockSampler(0)
+    sampler.start()
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        ingest(args.warmup + i)
+        e1.record(ext)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clocks = sampler.stop()
+    launches = sess.stats()["launches"]
+    done_batches = args.warmup + steps
+    for b in range(done_batches, nb):  # the rest of the stream, untimed
+        ingest(b)
+    torch.cuda.synchronize()
+    value = steps * C2_BATCH / (sum(times) / 1e3)
+
+    qs = c2_queries()
+    dq = torch.from_numpy(qs).to(dev)
+    dout = torch.empty_like(dq)
+    q_times = []
+    for r in range(6):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        rc = L.kd_store_quantile(h, None, dq.data_ptr(), len(qs), dout.data_ptr(), N.KD_PTR_DEVICE)
+        e1.record(ext)
+        e1.synchronize()
+        if rc:
+            raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+        if r >= 3:
+            q_times.append(e0.elapsed_time(e1))
+    est = dout.cpu().numpy()
+
+    # exact weighted distribution: a sample of batch b carries the decay weight
+    # of the clock after that batch, 2^((b + 1) * batch / 1e6), here relative to
+    # the last batch
+    w_b = torch.pow(2.0, (torch.arange(nb, dtype=torch.float64, device=dev) + 1 - nb) * C2_BATCH / 1e6)
+    w = w_b.repeat_interleave(C2_BATCH)
+    sv, order = torch.sort(vals)
+    wc = torch.cumsum(w[order], 0)
+    sv_h = sv.cpu().numpy()
+    wc_h = wc.cpu().numpy()
+    del sv, order, wc, w
+    q7 = np.array(QUANTILES)
+    est7 = d.quantiles(q7)
+    err7 = rank_error_ppm(sv_h, est7, q7, wc_h)
+    err_all = rank_error_ppm(sv_h, est, qs, wc_h)
+
+    cpu = None
+    if not args.no_cpu:
+        from oracle import pyoracle as po
+
+        po.build()
+        od = po.Digest(po.K2, 200.0, math.log(2.0) / 1e6)
+        host = vals.cpu().numpy()
+        t0 = time.perf_counter()
+        k = 0
+        while k < nb and time.perf_counter() - t0 < 20.0:
+            od.add_batch_p(host[k * C2_BATCH:(k + 1) * C2_BATCH])
+            k += 1
+        dt = time.perf_counter() - t0
+        cpu = {"value": k * C2_BATCH / dt, "unit": "samples/s", "cores": 1, "kind": "port",
+               "sample": f"first {k} batches of 2^20 ({dt:.1f} s, C oracle P-path, one digest)"}
+        if k == nb:  # the oracle saw the whole stream: full-size parity of the answers
+            cpu["quantiles_bit_identical"] = bool(
+                np.array_equal(np.array([od.quantile(q) for q in qs]), est))
+            om, ow = od.centroids()
+            gm, gw = d.centroids()
+            cpu["centroids_bit_identical"] = bool(np.array_equal(om, gm) and np.array_equal(ow, gw))
+
+    line = {
+        "metric": "single-digest ingest samples/s (K2 d200, 1e6-sample half-life)",
+        "value": value, "unit": "samples/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (torch device RNG, seeded), resident in HBM",
+        "config": {"workload": "config 2: 2^26 lognormal(mu_t, 1.5) samples, mu_t 0 -> 2, "
+                               "one TDigest[K2] d200, half-life 1e6 samples, batches of 2^20",
+                   "batch": C2_BATCH, "total": C2_TOTAL,
+                   "l2": "flushed (256 MiB write) between timed steps"},
+        "queries_per_s": len(qs) / (statistics.median(q_times) / 1e3),
+        "centroids": len(d),
+        "rank_error": {"q": list(QUANTILES), "ppm": [round(x, 1) for x in err7],
+                       "queries_4096_mean_ppm": round(float(err_all.mean()), 1),
+                       "queries_4096_max_ppm": round(float(err_all.max()), 1),
+                       "reference": "exact sort of all 2^26 samples with their decay weights"},
+        "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# Config 4: 2^20 small K2 digests (compression 50), digest i built from
+# U{64..4096} samples of N(mu_i, sigma_i), mu_i ~ U(-10, 10), sigma_i ~ U(0.1, 5);
+# merged 32-way into 2^15 and again into 1024 group digests (compression 200);
+# then 2^24 quantile queries (group uniform, q half uniform, half log-uniform
+# tails mirrored) and 2^24 cdf queries (x uniform in the group's [min, max]).
+# ----------------------------------------------------------------------------
+C4_DIGESTS = 1 << 20
+C4_BUILD_BATCH = 1 << 24
+C4_QUERIES = 1 << 24
+
+
+def run_config4(args) -> int:
+    import torch
+
+    import kdigest_gb300 as kd
+    from kdigest_gb300 import _native as N
+
+    dev = torch.device("cuda", 0)
+    r = np.random.default_rng(SEED + 4)
+    n_i = r.integers(64, 4097, C4_DIGESTS)
+    mu = torch.from_numpy(r.uniform(-10.0, 10.0, C4_DIGESTS)).to(dev)
+    sg = torch.from_numpy(r.uniform(0.1, 5.0, C4_DIGESTS)).to(dev)
+    offs = np.concatenate([[0], np.cumsum(n_i)])
+    total = int(offs[-1])
+    sess = kd.GpuSession()
+    src = kd.GroupedTDigest(C4_DIGESTS, 50.0, scale=kd.K2, session=sess)
+    L = N.load()
+    # build: batches of whole digests (each digest is one ingest of its samples)
+    cuts = [0]
+    while cuts[-1] < C4_DIGESTS:
+        nxt = int(np.searchsorted(offs, offs[cuts[-1]] + C4_BUILD_BATCH, side="right")) - 1
+        cuts.append(max(nxt, cuts[-1] + 1))
+    gen = torch.Generator(device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for bi in range(len(cuts) - 1):
+        d0, d1 = cuts[bi], min(cuts[bi + 1], C4_DIGESTS)
+        cnt = torch.from_numpy(n_i[d0:d1]).to(dev)
+        keys = torch.repeat_interleave(torch.arange(d0, d1, device=dev, dtype=torch.int32), cnt)
+        gen.manual_seed(SEED + 400 + bi)
+        kl = keys.long()
+        vals = mu[kl] + sg[kl] * torch.randn(len(keys), dtype=torch.float64, device=dev, generator=gen)
+        rc = L.kd_store_ingest(src._store._h, keys.data_ptr(), vals.data_ptr(), len(keys),
+                               N.KD_CLOCK_COUNT, 0.0, N.KD_PTR_DEVICE)
+        if rc:
+            raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+
+    lvl1 = kd.GroupedTDigest(C4_DIGESTS // 32, 200.0, scale=kd.K2, session=sess)
+    lvl2 = kd.GroupedTDigest(1024, 200.0, scale=kd.K2, session=sess)
+    t0 = time.perf_counter()
+    lvl1.merge_groups(src, np.arange(0, C4_DIGESTS + 1, 32), np.arange(C4_DIGESTS, dtype=np.uint32))
+    torch.cuda.synchronize()
+    m1 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    lvl2.merge_groups(lvl1, np.arange(0, C4_DIGESTS // 32 + 1, 32),
+                      np.arange(C4_DIGESTS // 32, dtype=np.uint32))
+    torch.cuda.synchronize()
+    m2 = time.perf_counter() - t0
+    cent_in = int(src.centroid_counts().sum())
+
+    # queries, device-resident inputs and outputs
+    rq = np.random.default_rng(SEED + 44)
+    ids = rq.integers(0, 1024, C4_QUERIES).astype(np.int32)
+    tails = 10 ** rq.uniform(-6, -2, C4_QUERIES // 4)
+    qs = np.concatenate([rq.random(C4_QUERIES // 2), tails, 1.0 - tails])
+    rq.shuffle(qs)
+    mins = np.array([lvl2.state(k)["min"] for k in range(1024)])
+    maxs = np.array([lvl2.state(k)["max"] for k in range(1024)])
+    cids = rq.integers(0, 1024, C4_QUERIES).astype(np.int32)
+    xs = mins[cids] + rq.random(C4_QUERIES) * (maxs[cids] - mins[cids])
+    dk, dq = torch.from_numpy(ids).to(dev), torch.from_numpy(qs).to(dev)
+    dck, dx = torch.from_numpy(cids).to(dev), torch.from_numpy(xs).to(dev)
+    out_q = torch.empty_like(dq)
+    out_c = torch.empty_like(dx)
+    ext = torch.cuda.ExternalStream(sess.stream, device=dev)
+    h2 = lvl2._store._h
+    tq, tc = [], []
+    for rep in range(6):
+        for fn, k, x, o, acc in ((L.kd_store_quantile, dk, dq, out_q, tq),
+                                 (L.kd_store_cdf, dck, dx, out_c, tc)):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            rc = fn(h2, k.data_ptr(), x.data_ptr(), C4_QUERIES, o.data_ptr(), N.KD_PTR_DEVICE)
+            e1.record(ext)
+            e1.synchronize()
+            if rc:
+                raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+            if rep >= 3:
+                acc.append(e0.elapsed_time(e1))
+    ms_q, ms_c = statistics.median(tq), statistics.median(tc)
+    qps = 2 * C4_QUERIES / ((ms_q + ms_c) / 1e3)
+    peaks = measured_peaks()
+    qbytes = 20 * C4_QUERIES  # key 4 B + q 8 B + result 8 B per query
+    achieved = qbytes / (ms_q / 1e3) / 1e9
+    line = {
+        "metric": "batched queries/s after a 2^20-digest 32-way merge (K2)",
+        "value": qps, "unit": "queries/s", "n_gpus": 1, "steps": 3, "warmup": 3,
+        "ms_per_step": ms_q + ms_c, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (torch device RNG for samples, seeded numpy for shapes and queries)",
+        "config": {"workload": "config 4: 2^20 K2 d50 digests of U{64..4096} normal samples, "
+                               "merged 32-way twice into 1024 d200 groups, 2^24 quantile + 2^24 cdf queries",
+                   "samples": total, "digests": C4_DIGESTS, "groups": 1024},
+        "build": {"samples_per_s": total / build_s, "seconds": round(build_s, 3),
+                  "batches": len(cuts) - 1},
+        "merge": {"level1_s": round(m1, 4), "level2_s": round(m2, 4),
+                  "digests_per_s": (C4_DIGESTS + C4_DIGESTS // 32) / (m1 + m2),
+                  "centroids_in_level1": cent_in},
+        "queries": {"quantile_ms": round(ms_q, 4), "cdf_ms": round(ms_c, 4),
+                    "launches": "one kernel per call"},
+        "roofline": {"bound": "hbm", "kernel": "k_query (quantile)", "achieved": round(achieved, 1),
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                     "algorithmic_bytes": qbytes},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -445,6 +762,9 @@ def run_gpu(args):
             q_times.append(e0.elapsed_time(e1))
     qps = qq.numel() / (statistics.median(q_times) / 1e3)
 
+    ingested = [i % nb for i in range(args.warmup + args.steps)]
+    accuracy = grouped_rank_error(store, keys, vals, ingested, BATCH, NUM_KEYS)
+
     comp_bytes = sum(compulsory) / len(compulsory)
     peaks = measured_peaks()
     step_gbs = sum(compulsory) / (sum(times) / 1e3) / 1e9
@@ -457,8 +777,9 @@ def run_gpu(args):
     dom = max(stage_ms, key=stage_ms.get)
     passes = 8 + 2  # 64 value bits + 16 key bits, 8-bit digits
     alg = {
-        # radix passes: histogram read of the digit source + scatter read/write of 12 B pairs
-        "sort": passes * BATCH * (8 + 24) - 2 * BATCH * 4,
+        # one histogram read of the 12 B pairs for all passes, then per pass a
+        # read and a write of every pair
+        "sort": (12 + passes * 24) * BATCH,
         "level0": 8 * BATCH + touched_avg * 16 * 2 * prior_avg,
         "prep": 12 * BATCH + 12 * BATCH,
     }
@@ -559,6 +880,7 @@ def run_gpu(args):
         "e2e": e2e,
         "gpu_launches": st["launches"],
         "clocks": clocks,
+        "rank_error": accuracy,
         "serving": serving,
     }
     if rank == 0:
@@ -572,7 +894,7 @@ def main():
     global TOTAL
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=29)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-plain", action="store_true")
@@ -586,12 +908,22 @@ def main():
     ap.add_argument("--serve-window", type=float, default=1e-3)
     ap.add_argument("--serve-rate", type=float, default=SERVE_RATE)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--config", type=int, default=3, choices=[2, 3, 4],
+                    help="2: single decayed digest; 3: grouped ingest (the headline); "
+                         "4: batched merge and query")
     args = ap.parse_args()
+    args.steps_given = args.steps is not None
+    if args.steps is None:
+        args.steps = 29
     TOTAL = args.total
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == 2:
+        return run_config2(args)
+    if args.config == 4:
+        return run_config4(args)
     if args.serve:
         import torch  # noqa: F401  (CUDA context before the worker thread)
 
