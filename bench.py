@@ -258,6 +258,85 @@ def grouped_rank_error(store, keys, vals, ingested_batches, batch, num_keys, nsa
 
 
 # ----------------------------------------------------------------------------
+# Config 1: one K1 digest (compression 100, no decay), 1,000,000 N(0, 1) samples
+# (seed 0) in batches of 4096, then quantiles at 7 q and cdf at 5 x.  The
+# reference serves batches this small with its sequential CPU S-path; here
+# every batch takes the GPU P-path (a different clustering, so both paths'
+# rank errors are reported against the exact sort).
+# ----------------------------------------------------------------------------
+C1_TOTAL = 1_000_000
+C1_BATCH = 4096
+C1_X = (-3.0, -1.0, 0.0, 1.0, 3.0)
+
+
+def run_config1(args) -> int:
+    import torch
+
+    import kdigest_gb300 as kd
+    from kdigest_gb300 import _native as N
+
+    dev = torch.device("cuda", 0)
+    vals_h = np.random.default_rng(0).standard_normal(C1_TOTAL)
+    vals = torch.from_numpy(vals_h).to(dev)
+    sess = kd.GpuSession()
+    ext = torch.cuda.ExternalStream(sess.stream, device=dev)
+    L = N.load()
+    nb = (C1_TOTAL + C1_BATCH - 1) // C1_BATCH
+    reps = []
+    for rep in range(args.warmup + 3):  # whole-stream passes; the first ones warm up
+        d = kd.TDigest(100.0, kd.K1, session=sess)
+        h = d._store._h
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for b in range(nb):
+            n = min(C1_BATCH, C1_TOTAL - b * C1_BATCH)
+            rc = L.kd_store_ingest(h, None, vals.data_ptr() + b * C1_BATCH * 8, n, N.KD_CLOCK_COUNT,
+                                   0.0, N.KD_PTR_DEVICE)
+            if rc:
+                raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+        e1.record(ext)
+        e1.synchronize()
+        if rep >= args.warmup:
+            reps.append(e0.elapsed_time(e1))
+    ms = statistics.median(reps)
+    q7 = np.array(QUANTILES)
+    sv = np.sort(vals_h)
+    gq = d.quantiles(q7)
+    gc = d.cdfs(np.array(C1_X))
+    out = {"gpu_p_path": {"rank_error_ppm": [round(x, 1) for x in rank_error_ppm(sv, gq, q7)],
+                          "centroids": len(d), "quantiles": gq.tolist(), "cdf": gc.tolist()}}
+    cpu = None
+    if not args.no_cpu:
+        from oracle import pyoracle as po
+
+        po.build()
+        od = po.Digest(po.K1, 100.0, 0.0)
+        t0 = time.perf_counter()
+        od.add_many(vals_h)
+        od.merge()
+        dt = time.perf_counter() - t0
+        oq = np.array([od.quantile(q) for q in q7])
+        out["cpu_s_path"] = {"rank_error_ppm": [round(x, 1) for x in rank_error_ppm(sv, oq, q7)],
+                             "centroids": len(od.centroids()[0]), "quantiles": oq.tolist()}
+        cpu = {"value": C1_TOTAL / dt, "unit": "samples/s", "cores": 1, "kind": "port",
+               "sample": f"the whole stream through the oracle's sequential add loop in C "
+                         f"({dt:.2f} s)"}
+    line = {
+        "metric": "single-digest ingest samples/s (K1 d100, batches of 4096)",
+        "value": C1_TOTAL / (ms / 1e3), "unit": "samples/s", "n_gpus": 1, "steps": 3,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic N(0,1), seed 0, resident in HBM",
+        "config": {"workload": "config 1: 1e6 N(0,1) samples into one TDigest[K1] d100 in "
+                               "batches of 4096 (a step is the whole stream)", "batch": C1_BATCH},
+        "accuracy": out, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
 # Config 2: one K2 digest (compression 200), Decay.half_life(1e6 samples),
 # 2^26 lognormal(mu_t, 1.5) samples with mu_t drifting 0 -> 2, batches of 2^20,
 # then 4096 quantiles (2048 uniform, 1024 log-uniform in [1e-6, 1e-2] and their
@@ -783,11 +862,17 @@ def run_gpu(args):
         "level0": 8 * BATCH + touched_avg * 16 * 2 * prior_avg,
         "prep": 12 * BATCH + 12 * BATCH,
     }
+    # DRAM bytes of one sort stage (histogram + 10 passes) of a 2^22-pair batch,
+    # from `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum` on GB300
+    # (profiles/launches_dram_grouped_ingest_65536keys_batch2p22.md): below the
+    # algorithmic bytes because the ping-pong buffers largely stay in L2.
+    traffic = {"sort": 599.0e6 * BATCH / (1 << 22)}
     dom_bytes = alg.get(dom, comp_bytes)
     achieved = dom_bytes / (stage_ms[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
                 "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                "frac": round(achieved / peaks["hbm_gbs"], 4),
+                "traffic": int(traffic[dom]) if dom in traffic else None,
                 "peak_source": peaks["source"], "algorithmic_bytes": int(dom_bytes),
                 "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()}}
 
@@ -908,9 +993,9 @@ def main():
     ap.add_argument("--serve-window", type=float, default=1e-3)
     ap.add_argument("--serve-rate", type=float, default=SERVE_RATE)
     ap.add_argument("--no-serve", action="store_true")
-    ap.add_argument("--config", type=int, default=3, choices=[2, 3, 4],
-                    help="2: single decayed digest; 3: grouped ingest (the headline); "
-                         "4: batched merge and query")
+    ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4],
+                    help="1: single digest, small batches; 2: single decayed digest; "
+                         "3: grouped ingest (the headline); 4: batched merge and query")
     args = ap.parse_args()
     args.steps_given = args.steps is not None
     if args.steps is None:
@@ -920,6 +1005,8 @@ def main():
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == 1:
+        return run_config1(args)
     if args.config == 2:
         return run_config2(args)
     if args.config == 4:

@@ -473,6 +473,16 @@ int kdo_add(kdo_digest* d, double value, double weight) { /* tdigest.mojo:153-16
   return KDO_OK;
 }
 
+/* The reference's add loop over an array of unit-weight samples (what
+ * TDigest.add_batch runs below its GPU crossover, tdigest.mojo:199-202). */
+int kdo_add_many(kdo_digest* d, const double* values, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) {
+    int e = kdo_add(d, values[i], 1.0);
+    if (e) return e;
+  }
+  return KDO_OK;
+}
+
 int kdo_add_at(kdo_digest* d, double value, double timestamp, double weight) {
   int e = validate(value, weight); /* tdigest.mojo:163-175 */
   if (e) return e;

@@ -54,6 +54,7 @@ void kdo_digest_free(kdo_digest* d);
 /* S-path (sequential greedy sweep) API — tdigest.mojo:153-175, 391-458. */
 int kdo_add(kdo_digest* d, double value, double weight);
 int kdo_add_at(kdo_digest* d, double value, double timestamp, double weight);
+int kdo_add_many(kdo_digest* d, const double* values, int64_t n);
 void kdo_merge(kdo_digest* d);
 int kdo_merge_into(kdo_digest* d, kdo_digest* other);
 

@@ -52,6 +52,7 @@ def lib():
         L.kdo_digest_free.argtypes = [_P]
         L.kdo_add.argtypes = [_P, _D, _D]
         L.kdo_add_at.argtypes = [_P, _D, _D, _D]
+        L.kdo_add_many.argtypes = [_P, _P, ctypes.c_int64]
         L.kdo_merge.argtypes = [_P]
         L.kdo_merge_into.argtypes = [_P, _P]
         L.kdo_add_batch_p.argtypes = [_P, _P, _I64]
@@ -144,6 +145,11 @@ class Digest:
 
     def add(self, v: float, w: float = 1.0):
         self._check(lib().kdo_add(self._h, v, w), "add")
+
+    def add_many(self, values):
+        """The sequential add loop over unit-weight samples, in C."""
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        self._check(lib().kdo_add_many(self._h, v.ctypes.data_as(ctypes.c_void_p), len(v)), "add_many")
 
     def add_at(self, v: float, t: float, w: float = 1.0):
         self._check(lib().kdo_add_at(self._h, v, t, w), "add_at")

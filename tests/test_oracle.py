@@ -363,3 +363,17 @@ def test_grouped_rejects_bad_batch_before_mutation():
     with pytest.raises(o.OracleError):
         o.grouped_add_batch(g, [0, 5], [1.0, 2.0])
     assert [d.total_weight() for d in g] == before
+
+
+def test_add_many_is_the_add_loop(oracle):
+    """The C add loop equals one add() per sample (tdigest.mojo:199-202)."""
+    v = np.random.default_rng(9).standard_normal(5000)
+    a = oracle.Digest(oracle.K2, 100.0, 0.0)
+    b = oracle.Digest(oracle.K2, 100.0, 0.0)
+    a.add_many(v)
+    for x in v:
+        b.add(float(x))
+    a.merge()
+    b.merge()
+    for ca, cb in zip(a.centroids(), b.centroids()):
+        assert np.array_equal(ca, cb)
