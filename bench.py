@@ -854,19 +854,18 @@ def run_gpu(args):
     # Dominant stage (kernel group) from the stage events on the launching stream.
     stage_ms = {k: v / max(1, st["ingests"]) for k, v in st["stage_ms"].items()}
     dom = max(stage_ms, key=stage_ms.get)
-    passes = 8 + 2  # 64 value bits + 16 key bits, 8-bit digits
+    passes = 8  # (16-bit key, top 48 value bits) packed into 64 bits, 8-bit digits
     alg = {
-        # one histogram read of the 12 B pairs for all passes, then per pass a
-        # read and a write of every pair
-        "sort": (12 + passes * 24) * BATCH,
+        # one histogram read of the 12 B pairs for all passes, per pass a read
+        # and a write of every pair, then the unpack (read + write)
+        "sort": (12 + passes * 24 + 24) * BATCH,
         "level0": 8 * BATCH + touched_avg * 16 * 2 * prior_avg,
         "prep": 12 * BATCH + 12 * BATCH,
     }
-    # DRAM bytes of one sort stage (histogram + 10 passes) of a 2^22-pair batch,
-    # from `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum` on GB300
-    # (profiles/launches_dram_grouped_ingest_65536keys_batch2p22.md): below the
-    # algorithmic bytes because the ping-pong buffers largely stay in L2.
-    traffic = {"sort": 599.0e6 * BATCH / (1 << 22)}
+    # DRAM bytes of one sort stage of a 2^22-pair batch from an ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum), filled in from the
+    # committed profile of the current sort
+    traffic = {}
     dom_bytes = alg.get(dom, comp_bytes)
     achieved = dom_bytes / (stage_ms[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),

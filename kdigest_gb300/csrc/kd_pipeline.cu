@@ -29,6 +29,7 @@
 
 #define KD_ERANGE_SCRATCH KD_ERANGE_SCRATCH_INTERNAL  // scratch too small (index = needed)
 #define KD_EMORE_LEVELS 101    // internal: keys still above one tile after the levels run
+#define KD_ERESORT 102         // internal: the packed sort left an inversion; sort in full
 
 __device__ __forceinline__ size_t slot_base(long long K, int buf, long long key) {
   return ((size_t)buf * (size_t)K + (size_t)key) * KD_TILE;
@@ -422,7 +423,14 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
 // ---------------------------------------------------------------------------
 // Stage kernels
 // ---------------------------------------------------------------------------
-__global__ void k_prep(long long n, const KdCallArgs* __restrict__ call, long long K,
+// Sort keys.  Full form: k64 = order key of the value, kout = digest key (the
+// sort then runs 8 value passes and ceil(kb / 8) key passes).  Packed form
+// (kb > 0): k64 = digest key in the top kb bits above the top 64 - kb bits of
+// the order key, kout = the order key's low kb bits; 8 passes sort it, and
+// k_unpack restores the full form.  Samples of one key whose order keys agree
+// in the top 64 - kb bits keep their input order, so the packed order can
+// only be wrong between such samples; k_merge_new checks it.
+__global__ void k_prep(long long n, const KdCallArgs* __restrict__ call, long long K, int kb,
                        uint64_t* __restrict__ k64, uint32_t* __restrict__ kout,
                        uint32_t* __restrict__ idx, KdErrHost* err) {
   const uint32_t* __restrict__ keys = call->keys;
@@ -441,8 +449,14 @@ __global__ void k_prep(long long n, const KdCallArgs* __restrict__ call, long lo
       atomicMin((unsigned long long*)&err->index, (unsigned long long)i);
       atomicCAS(&err->code, 0, KD_EINVAL);
     }
-    k64[i] = kd_order_key(v);
-    kout[i] = key;
+    const uint64_t ok = kd_order_key(v);
+    if (kb > 0) {
+      k64[i] = ((uint64_t)key << (64 - kb)) | (ok >> kb);
+      kout[i] = (uint32_t)(ok & ((1ull << kb) - 1ull));
+    } else {
+      k64[i] = ok;
+      kout[i] = key;
+    }
     if (idx) idx[i] = (uint32_t)i;
   }
 }
@@ -493,6 +507,49 @@ struct PrepareArgs {
 
 // _gpu_batch_prepare per touched key (tdigest.mojo:236-296), _advance_clock
 // (:324-332), _renormalize (:359-371), _scale_factor (:352-357).
+// Packed sort keys back to (order key, digest key), from the sort's last
+// buffers into the free ones, repairing the order where the packed sort could
+// not see it: samples of one key with equal packed bits form a run still in
+// input order; the run's first element copies the run, sorts it by the low
+// bits (insertion sort, stable) and unpacks it.  Runs longer than
+// KD_PACK_RUN_MAX (adversarial data only) send the step to the full sort.
+// Sources are read-only and every destination run has one writer.
+#define KD_PACK_RUN_MAX 64
+__global__ void k_unpack(long long n, int kb, const uint64_t* __restrict__ sk,
+                         const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx,
+                         uint64_t* __restrict__ dk, uint32_t* __restrict__ dkey,
+                         uint32_t* __restrict__ didx, KdErrHost* err) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const uint64_t p = sk[i];
+    if (i > 0 && sk[i - 1] == p) continue;  // inside a run: its first element owns it
+    long long e = i + 1;
+    while (e < n && e - i <= KD_PACK_RUN_MAX && sk[e] == p) ++e;
+    if (e - i > KD_PACK_RUN_MAX) {
+      kd_err_set(err, KD_ERESORT, i);
+      continue;
+    }
+    const uint32_t kid = (uint32_t)(p >> (64 - kb));
+    for (long long a = i; a < e; ++a) {  // stable insertion sort by the low bits
+      const uint32_t lv = skey[a];
+      const uint32_t iv = sidx ? sidx[a] : 0u;
+      long long b = a;
+      while (b > i && dkey[b - 1] > lv) {
+        dkey[b] = dkey[b - 1];
+        if (didx) didx[b] = didx[b - 1];
+        --b;
+      }
+      dkey[b] = lv;
+      if (didx) didx[b] = iv;
+    }
+    for (long long a = i; a < e; ++a) {
+      const uint32_t low = dkey[a];
+      dkey[a] = kid;
+      dk[a] = (p << kb) | (uint64_t)low;
+    }
+  }
+}
+
 __global__ void k_prepare(PrepareArgs a) {
   const int U = a.totals[0].x;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -709,6 +766,9 @@ __global__ void k_merge_new(MergeArgs a) {
     const int jn = (int)(i - a.tstart[j]);
     const int np = a.tprior[j];
     const uint64_t vk = a.k64[i];
+    // the packed sort is exact unless two samples of a key shared the packed
+    // bits and their low bits came out of order: then sort again in full
+    if (i > 0 && a.skey[i - 1] == k && a.k64[i - 1] > vk) kd_err_set(a.err, KD_ERESORT, i);
     int lo = 0;
     if (np > 0) {
       const double* pm = a.s.slot_m + slot_base(a.s.K, a.tbuf[j] ^ 1, k);
@@ -1401,7 +1461,7 @@ static void enqueue_tail(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, lon
 // per-call block, prep, sort, planning, level 0, `levels` hierarchy levels,
 // commit and readback.
 static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long long n, int mode,
-                               bool with_idx, int levels, int id_last) {
+                               bool with_idx, int levels, int id_last, bool full_sort) {
   cudaStream_t str = s->stream;
   const KdStoreDev sd = st->d;
   const long long keys_max = std::min<long long>(n, sd.K);
@@ -1413,14 +1473,23 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   stage_mark(s, 0);
   {
     int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
-    k_prep<<<grid, 256, 0, str>>>(n, w.d_call, sd.K, w.k64[0], w.key[0],
+    k_prep<<<grid, 256, 0, str>>>(n, w.d_call, sd.K, full_sort ? 0 : key_bits, w.k64[0], w.key[0],
                                   with_idx ? w.idx[0] : nullptr, w.err);
     v.launches += 1;
   }
   stage_mark(s, 1);
   KdSortBufs sb = sort_bufs(w);
-  const int r = kd_radix_sort(sb, n, key_bits, with_idx, s->num_sms, str);
-  v.launches += kd_radix_sort_launches(n, key_bits);
+  const int sort_bits = full_sort ? key_bits : 0;  // packed keys need no key passes
+  int r = kd_radix_sort(sb, n, sort_bits, with_idx, s->num_sms, str);
+  v.launches += kd_radix_sort_launches(n, sort_bits);
+  if (!full_sort && key_bits > 0) {
+    const int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
+    k_unpack<<<grid, 256, 0, str>>>(n, key_bits, w.k64[r], w.key[r], with_idx ? w.idx[r] : nullptr,
+                                    w.k64[r ^ 1], w.key[r ^ 1], with_idx ? w.idx[r ^ 1] : nullptr,
+                                    w.err);
+    v.launches += 1;
+    r ^= 1;
+  }
   stage_mark(s, 2);
   const uint64_t* k64 = w.k64[r];
   const uint32_t* skey = w.key[r];
@@ -1522,7 +1591,7 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
         slot = KdGraphEntry();
         cudaGraph_t graph = nullptr;
         if (cudaStreamBeginCapture(str, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-          const KdStepView cv = enqueue_step(s, st, w, n, mode, with_idx, L, id_last);
+          const KdStepView cv = enqueue_step(s, st, w, n, mode, with_idx, L, id_last, false);
           const bool ended = cudaStreamEndCapture(str, &graph) == cudaSuccess;
           if (ended && graph && cv.err == cudaSuccess) {
             cudaGraphExec_t ex = nullptr;
@@ -1549,12 +1618,21 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
     }
   }
   if (!ran) {
-    v = enqueue_step(s, st, w, n, mode, with_idx, L, id_last);
+    v = enqueue_step(s, st, w, n, mode, with_idx, L, id_last, false);
     st->last_eager = key;
     KD_CK(v.err);
   }
   KD_CK(cudaGetLastError());
   KD_CK(cudaStreamSynchronize(str));
+  if (w.h_err->code == KD_ERESORT) {
+    // Two samples of one key agreed in the packed bits and came out of order:
+    // nothing was committed; run the step again with the full sort.
+    c.err = KdErrHost{0, 0, 0x7fffffffffffffffLL};
+    kd_rs_epoch_reserve(sb, str);
+    v = enqueue_step(s, st, w, n, mode, with_idx, L, id_last, true);
+    KD_CK(v.err);
+    KD_CK(cudaStreamSynchronize(str));
+  }
   // Keys still above one tile after the planned levels: run more levels from
   // where the step stopped, then commit again.
   while (w.h_err->code == KD_EMORE_LEVELS && L < s->max_levels) {

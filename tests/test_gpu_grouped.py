@@ -244,3 +244,51 @@ def test_serde_round_trip(kd, oracle):
         kd.TDigest.from_bytes(bytes([99]))
     with pytest.raises(ValueError):
         kd.TDigest.from_bytes(b[:-16], scale=kd.K2)
+
+
+@pytest.mark.parametrize("num_keys", [300, 70000])
+def test_packed_sort_inversion_falls_back_to_full_sort(kd, oracle, num_keys):
+    """Samples of one key whose order keys differ only in the bits the packed
+    sort leaves out arrive larger-first: the step must detect the inversion,
+    commit nothing from the packed order, and sort in full."""
+    rng = np.random.default_rng(17)
+    base = rng.standard_normal(2000) * 10
+    ulp = np.spacing(np.abs(base))
+    keys = np.repeat(rng.integers(0, num_keys, 2000), 2)
+    vals = np.stack([base + 3 * ulp, base], axis=1).reshape(-1)  # larger first, same top bits
+    more_k = rng.integers(0, num_keys, 30000)
+    more_v = rng.standard_normal(30000)
+    keys = np.concatenate([keys, more_k])
+    vals = np.concatenate([vals, more_v])
+    g = kd.GroupedTDigest(num_keys, 100.0, scale=kd.K2)
+    for step in range(2):
+        g.add_batch(keys, vals)
+    used = np.unique(keys)
+    ref = [oracle.Digest(oracle.K2, 100.0, 0.0) for _ in range(len(used))]
+    pos = {k: i for i, k in enumerate(used)}
+    sub = np.array([pos[k] for k in keys])
+    for step in range(2):
+        oracle.grouped_add_batch(ref, sub, vals)
+    for k in used[:: max(1, len(used) // 50)]:
+        gm, gw = g.centroids(int(k))
+        om, ow = ref[pos[k]].centroids()
+        assert np.array_equal(gm, om) and np.array_equal(gw, ow)
+
+
+def test_packed_sort_long_run_falls_back(kd, oracle):
+    """200 samples of one key equal in their packed bits (1 + j ulp, shuffled):
+    a run too long to repair in place, so the step sorts in full."""
+    rng = np.random.default_rng(23)
+    nk = 1000
+    vals = 1.0 + rng.permutation(200) * np.spacing(1.0)
+    keys = np.full(200, 7)
+    keys = np.concatenate([keys, rng.integers(0, nk, 5000)])
+    vals = np.concatenate([vals, rng.standard_normal(5000)])
+    g = kd.GroupedTDigest(nk, 100.0, scale=kd.K1)
+    g.add_batch(keys, vals)
+    refs = [oracle.Digest(oracle.K1, 100.0, 0.0) for _ in range(nk)]
+    oracle.grouped_add_batch(refs, keys, vals)
+    for k in [7] + list(range(0, nk, 97)):
+        gm, gw = g.centroids(k)
+        om, ow = refs[k].centroids()
+        assert np.array_equal(gm, om) and np.array_equal(gw, ow)
