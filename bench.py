@@ -862,10 +862,11 @@ def run_gpu(args):
         "level0": 8 * BATCH + touched_avg * 16 * 2 * prior_avg,
         "prep": 12 * BATCH + 12 * BATCH,
     }
-    # DRAM bytes of one sort stage of a 2^22-pair batch from an ncu capture
-    # (dram__bytes_read.sum + dram__bytes_write.sum), filled in from the
-    # committed profile of the current sort
-    traffic = {}
+    # DRAM bytes of one sort stage (histogram, 8 packed passes, unpack) of a
+    # 2^22-pair batch: `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum`
+    # on GB300 (profiles/launches_dram_grouped_ingest_65536keys_batch2p22.md).
+    # Below the algorithmic bytes: the ping-pong buffers largely stay in L2.
+    traffic = {"sort": 528.3e6 * BATCH / (1 << 22)}
     dom_bytes = alg.get(dom, comp_bytes)
     achieved = dom_bytes / (stage_ms[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),

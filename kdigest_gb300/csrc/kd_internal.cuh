@@ -48,9 +48,11 @@ __device__ __forceinline__ void kd_set_error(KdErr* e, int code, long long index
 //
 // floor(k64) is needed where k64 = kd_k(scale, cum/tot, nrm64) is evaluated in
 // FP64 with the shared kd_math.h functions.  The filter evaluates k in FP32
-// together with a rigorous bound B on |k32 - k64| (worst-case relative errors
-// of the FP32 conversions, division, logf/asinf/sqrtf (<= 2 ulp each) and of the
-// FP64 reference itself, all multiplied by a safety factor of 8).  When
+// together with a rigorous bound B on |k32 - k64| (worst-case errors of the
+// FP32 conversions, of q = cum * rcp(total) (<= 3 ulp with the truncations),
+// of asinf/sqrtf (<= 2 ulp), of the __logf intrinsic (<= 2^-21.41 absolute on
+// [0.5, 2], <= 3 ulp elsewhere, documented by CUDA) and of the FP64 reference
+// itself, with margins of 5x or more on every term).  When
 // floor(k32 - B) == floor(k32 + B) the id is exact; otherwise, and outside the
 // domain where the bound holds (q or 1-q below 2^-40, non-finite values), the
 // caller evaluates the FP64 path.  The filter never changes a result: it only
@@ -83,6 +85,7 @@ struct KFilterTile {
   float nrm;      // FP32 normaliser
   float nrm_rel;  // bound on its relative error (already includes safety)
   float t32;      // tile total in FP32 (truncated)
+  float inv32;    // its reciprocal (round to nearest): q = cum * inv32
   int ok;         // 0 -> the tile must use the exact path for every element
 };
 
@@ -90,6 +93,7 @@ __device__ __forceinline__ KFilterTile kfilter_tile(int scale, double compressio
   KFilterTile f;
   float c32 = kd_d2f_trunc(compression);
   f.t32 = t32;
+  f.inv32 = __frcp_rn(t32);
   f.ok = isfinite(t32) && t32 > 0.f && c32 > 0.f && isfinite(c32);
   const float u = 5.9604645e-08f;  // 2^-24
   if (scale == KD_SCALE_K0) {
@@ -145,7 +149,7 @@ __device__ __forceinline__ int kfilter_id(int scale, const KFilterTile& ft, floa
     k = ft.nrm * a;
     b = fabsf(ft.nrm) * (64.f * u) + fabsf(k) * (ft.nrm_rel + 64.f * u);
   } else if (scale == KD_SCALE_K2) {
-    float lq = logf(q), l1 = logf(r);
+    float lq = __logf(q), l1 = __logf(r);
     float g = lq - l1;
     k = ft.nrm * g;
     // 2^-50 / r: the FP64 reference forms 1 - q64, whose absolute error
@@ -154,8 +158,8 @@ __device__ __forceinline__ int kfilter_id(int scale, const KFilterTile& ft, floa
         fabsf(k) * (ft.nrm_rel + 64.f * u);
   } else {
     float g;
-    if (q <= 0.5f) g = logf(2.f * q);
-    else g = -logf(2.f * r);
+    if (q <= 0.5f) g = __logf(2.f * q);
+    else g = -__logf(2.f * r);
     k = ft.nrm * g;
     b = fabsf(ft.nrm) * (64.f * u + 32.f * u * fabsf(g) + 8.881784e-16f / r) +
         fabsf(k) * (ft.nrm_rel + 64.f * u);

@@ -229,8 +229,8 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
           id = id_last;
           ok = true;
         } else {
-          const float q = A::to_f(cum) / ft.t32;
-          const float r = q > 0.25f ? A::to_f(A::sub(tot, cum)) / ft.t32 : 1.f - q;
+          const float q = A::to_f(cum) * ft.inv32;
+          const float r = q > 0.25f ? A::to_f(A::sub(tot, cum)) * ft.inv32 : 1.f - q;
           ok = kfilter_id(scale, ft, q, r, rz, &id);
         }
       }

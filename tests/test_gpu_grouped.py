@@ -292,3 +292,26 @@ def test_packed_sort_long_run_falls_back(kd, oracle):
         gm, gw = g.centroids(k)
         om, ow = refs[k].centroids()
         assert np.array_equal(gm, om) and np.array_equal(gw, ow)
+
+
+@pytest.mark.parametrize("scale", [0, 1, 2, 3])
+def test_grouped_filter_matches_exact_path(kd, scale):
+    """Grouped ingest (integral weights) with the FP32 bucket filter gives the
+    same digests as every id evaluated in FP64."""
+    nk, n = 3000, 200000
+    rng = np.random.default_rng(31 + scale)
+    batches = [(rng.zipf(1.15, n) % nk, rng.standard_normal(n) * 5 + rng.integers(0, 3, n))
+               for _ in range(3)]
+    out = []
+    for exact in (0, 1):
+        s = kd.GpuSession()
+        s.set_option(1, exact)  # KD_OPT_FORCE_EXACT_K
+        g = kd.GroupedTDigest(nk, 100.0, scale=scale, session=s)
+        for k, v in batches:
+            g.add_batch(k, v)
+        out.append(g)
+    assert np.array_equal(out[0].centroid_counts(), out[1].centroid_counts())
+    for k in range(0, nk, 41):
+        ma, wa = out[0].centroids(k)
+        mb, wb = out[1].centroids(k)
+        assert np.array_equal(ma, mb) and np.array_equal(wa, wb)
