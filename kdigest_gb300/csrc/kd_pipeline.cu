@@ -421,6 +421,308 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
 }
 
 // ---------------------------------------------------------------------------
+// Block-cooperative compress of one tile above the small-tile cap: the same
+// canonical order as warp_compress (the chunk-serial prefix and segment sums
+// stay on warp 0), with the element-parallel stages - bucket ids, the FP64
+// fallback list, head detection and the mean divisions - spread over the
+// block's KD_TILE_WARPS warps.  Results are identical to warp_compress.
+// ---------------------------------------------------------------------------
+#define KD_TILE_WARPS 4
+struct BlockScr {
+  double totb;          // tile total (int64 bits in the integral path)
+  double totd;
+  KFilterTile ft;
+  int nneed, ndiv, nout, stop;
+  int rc[32];           // heads per round of 32 elements (then their offsets)
+  unsigned hb[32];      // head ballot per round
+};
+
+template <bool kInt>
+__device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, double compression,
+                              int force_exact, int32_t id_last, double* __restrict__ om,
+                              double* __restrict__ ow) {
+  typedef TileAcc<kInt> A;
+  typedef typename A::T T;
+  constexpr int NT = KD_TILE_WARPS * 32;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int E = tile_chunk(n);
+  const int SE = E | 1;
+  const unsigned inv = tile_inv(E);
+  const unsigned lt_mask = (1u << lane) - 1u;
+
+  // 1-2. In-chunk prefix (serial per lane) and Kogge-Stone over chunk totals.
+  if (warp == 0) {
+    const int lo = lane * E;
+    const int cnt = max(0, min(E, n - lo));
+    const int sb = lane * SE;
+    T acc = 0;
+    for (int j = 0; j < cnt; ++j) {
+      const T wv = A::from_w(t.w[sb + j]);
+      acc = j == 0 ? wv : A::add(acc, wv);
+      t.L[sb + j] = A::store(acc);
+    }
+    T I = cnt > 0 ? acc : (T)0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T v = A::shfl_up(I, o);
+      if (lane >= o) I = A::add(I, v);
+    }
+    t.P[lane] = A::store(A::shfl_up(I, 1));
+    const int cl = (n - 1) / E;
+    T last_cum = 0;
+    if (cnt > 0) last_cum = lane == 0 ? acc : A::add(A::load(t.P[lane]), acc);
+    T tot = A::shfl(last_cum, cl);
+    double totd = A::to_d(tot);
+    if (!(totd > 0.0)) {  // add_batch.mojo:98-100
+      totd = 1.0;
+      tot = (T)1;
+    }
+    if (lane == 0) {
+      bs.totb = A::store(tot);
+      bs.totd = totd;
+      bs.ft = kfilter_tile(scale, compression, kInt ? A::to_f(tot) : kd_d2f_trunc(totd));
+      bs.nneed = 0;
+      bs.ndiv = 0;
+    }
+  }
+  __syncthreads();
+  const T tot = A::load(bs.totb);
+  const double totd = bs.totd;
+  const KFilterTile ft = bs.ft;
+
+  // 3a. Bucket ids; warp w takes rounds w, w + KD_TILE_WARPS, ...
+  int* const ids = t.ids();
+  unsigned short* const plist = t.poslist();
+  for (int r0 = warp * 32; r0 < n; r0 += NT) {
+    const int p = r0 + lane;
+    bool need = false;
+    if (p < n) {
+      const int c = (int)(((unsigned)p * inv) >> 16);
+      const int slot = c * SE + (p - c * E);
+      const T Lp = A::load(t.L[slot]);
+      const T cum = c == 0 ? Lp : A::add(A::load(t.P[c]), Lp);
+      int32_t id = 0;
+      bool ok = false;
+      if (!force_exact) {
+        const bool rz = A::eq(cum, tot);
+        if (scale != KD_SCALE_K0 && A::is_half(cum, tot)) {
+          ok = true;
+        } else if (rz && scale <= KD_SCALE_K1) {
+          id = id_last;
+          ok = true;
+        } else {
+          const float q = A::to_f(cum) * ft.inv32;
+          const float r = q > 0.25f ? A::to_f(A::sub(tot, cum)) * ft.inv32 : 1.f - q;
+          ok = kfilter_id(scale, ft, q, r, rz, &id);
+        }
+      }
+      ids[p] = id;
+      need = !ok;
+    }
+    const unsigned nb = __ballot_sync(0xffffffffu, need);
+    if (nb) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(&bs.nneed, __popc(nb));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (need) plist[base + __popc(nb & lt_mask)] = (unsigned short)p;
+    }
+  }
+  __syncthreads();
+  // 3b. The FP64 path for the listed positions.
+  const int nneed = bs.nneed;
+  if (nneed > 0) {
+    const double nrm64 = kd_normalizer(scale, compression, totd);
+    for (int k = tid; k < nneed; k += NT) {
+      const int p = plist[k];
+      const int c = (int)(((unsigned)p * inv) >> 16);
+      const int slot = c * SE + (p - c * E);
+      const T Lp = A::load(t.L[slot]);
+      const T cum = c == 0 ? Lp : A::add(A::load(t.P[c]), Lp);
+      ids[p] = kd_bucket(scale, A::to_d(cum), totd, nrm64);
+    }
+  }
+  __syncthreads();
+  // 3c. Heads: flags per round, offsets by a scan over the rounds, then the
+  //     positions (the ids are all read before any position is written).
+  const int rounds = (n + 31) >> 5;
+  for (int r = warp; r < rounds; r += KD_TILE_WARPS) {
+    const int p = r * 32 + lane;
+    const bool act = p < n;
+    const int32_t id = act ? ids[p] : 0;
+    const int32_t prev = (act && p > 0) ? ids[p - 1] : 0;
+    const unsigned hb = __ballot_sync(0xffffffffu, act && (p == 0 || id != prev));
+    if (lane == 0) {
+      bs.hb[r] = hb;
+      bs.rc[r] = __popc(hb);
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int v = lane < rounds ? bs.rc[lane] : 0;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    bs.rc[lane] = incl - v;
+    if (lane == 31) bs.nout = incl;
+  }
+  __syncthreads();
+  for (int r = warp; r < rounds; r += KD_TILE_WARPS) {
+    const unsigned hb = bs.hb[r];
+    if ((hb >> lane) & 1u) t.headpos[bs.rc[r] + __popc(hb & lt_mask)] = (unsigned short)(r * 32 + lane);
+  }
+  __syncthreads();
+  const int total_out = bs.nout;
+
+  // 4. Segment sums, parked at each segment's end element.
+  if (n <= KD_SERIAL_TILE_MAX) {
+    for (int sI = tid; sI < total_out; sI += NT) {  // one chunk: serial, thread per segment
+      const int h = t.headpos[sI];
+      const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
+      t.endpos[sI] = (unsigned short)e;
+      if (h == e) {
+        t.L[e] = A::store(A::from_w(t.w[e]));
+        continue;
+      }
+      T aw = A::from_w(t.w[h]);
+      double awx = KD_MUL(t.w[h], t.x[h]);
+      for (int i = h + 1; i <= e; ++i) {
+        const double wi = t.w[i];
+        aw = A::add(aw, A::from_w(wi));
+        awx = KD_ADD(awx, KD_MUL(wi, t.x[i]));
+      }
+      t.L[e] = A::store(aw);
+      t.w[e] = awx;
+    }
+  } else {
+    for (int q = tid; q < n; q += NT) {
+      const int sl = tile_slot(q, E, SE, inv);
+      t.hf[sl] = 0;
+      t.ef[sl] = 0;
+    }
+    __syncthreads();
+    for (int sI = tid; sI < total_out; sI += NT) {
+      const int h = t.headpos[sI];
+      t.hf[tile_slot(h, E, SE, inv)] = 1;
+      const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
+      t.ef[tile_slot(e, E, SE, inv)] = 1;
+      t.endpos[sI] = (unsigned short)e;
+    }
+    __syncthreads();
+    if (warp == 0) {  // chunk-serial pieces and the segmented carry across lanes
+      const int lo = lane * E;
+      const int cnt = max(0, min(E, n - lo));
+      const int sb = lane * SE;
+      T aw = 0;
+      double awx = 0.0;
+      bool head_seen = false;
+      bool pend = false;
+      T pend_w = 0;
+      double pend_wx = 0.0;
+      int pend_se = 0;
+      for (int j = 0; j < cnt; ++j) {
+        const double wi = t.w[sb + j], xi = t.x[sb + j];
+        const double wx = KD_MUL(wi, xi);
+        const T wv = A::from_w(wi);
+        const bool hd = t.hf[sb + j];
+        if (hd || j == 0) {
+          aw = wv;
+          awx = wx;
+        } else {
+          aw = A::add(aw, wv);
+          awx = KD_ADD(awx, wx);
+        }
+        if (hd) head_seen = true;
+        if (t.ef[sb + j]) {
+          if (head_seen) {
+            t.L[sb + j] = A::store(aw);
+            t.w[sb + j] = awx;
+          } else {
+            pend = true;
+            pend_w = aw;
+            pend_wx = awx;
+            pend_se = sb + j;
+          }
+        }
+      }
+      T Vw = aw;
+      double Vwx = awx;
+      int F = head_seen ? 1 : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const T tw = A::shfl_up(Vw, o);
+        const double twx = shfl_up_d(Vwx, o);
+        const int tf = __shfl_up_sync(0xffffffffu, F, o);
+        if (lane >= o) {
+          if (!F) {
+            Vw = A::add(Vw, tw);
+            Vwx = KD_ADD(Vwx, twx);
+          }
+          F |= tf;
+        }
+      }
+      const T cw = A::shfl_up(Vw, 1);
+      const double cwx = shfl_up_d(Vwx, 1);
+      if (pend) {
+        t.L[pend_se] = A::store(A::add(cw, pend_w));
+        t.w[pend_se] = KD_ADD(cwx, pend_wx);
+      }
+    }
+  }
+  __syncthreads();
+
+  // 5. Centroids; the means that need a division are listed and divided with
+  //    every thread busy.
+  unsigned short* const dlist = t.poslist();
+  for (int s0 = warp * 32; s0 < total_out; s0 += NT) {
+    const int sI = s0 + lane;
+    bool div = false;
+    if (sI < total_out) {
+      const int e = t.endpos[sI];
+      const int h = t.headpos[sI];
+      const int se = tile_slot(e, E, SE, inv), sh = tile_slot(h, E, SE, inv);
+      const double sw = A::to_d(A::load(t.L[se]));
+      const double lo_v = t.x[sh], hi_v = t.x[se];
+      ow[sI] = sw;
+      if (__double_as_longlong(lo_v) == __double_as_longlong(hi_v)) {
+        om[sI] = lo_v;
+      } else if (!(__double_as_longlong(sw) > 0)) {  // zero weight: 0, clamped
+        const uint64_t k0 = kd_order_key(0.0);
+        om[sI] = k0 < kd_order_key(lo_v) ? lo_v : (k0 > kd_order_key(hi_v) ? hi_v : 0.0);
+      } else {
+        div = true;
+      }
+    }
+    const unsigned db = __ballot_sync(0xffffffffu, div);
+    if (db) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(&bs.ndiv, __popc(db));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (div) dlist[base + __popc(db & lt_mask)] = (unsigned short)sI;
+    }
+  }
+  __syncthreads();
+  const int ndiv = bs.ndiv;
+  for (int k = tid; k < ndiv; k += NT) {
+    const int sI = dlist[k];
+    const int e = t.endpos[sI];
+    const int h = t.headpos[sI];
+    const int se = tile_slot(e, E, SE, inv), sh = tile_slot(h, E, SE, inv);
+    const double sw = A::to_d(A::load(t.L[se]));
+    const double lo_v = t.x[sh], hi_v = t.x[se];
+    double mean = KD_DIV(t.w[se], sw);
+    const uint64_t km = kd_order_key(mean);
+    if (km < kd_order_key(lo_v)) mean = lo_v;
+    else if (km > kd_order_key(hi_v)) mean = hi_v;
+    om[sI] = mean;
+  }
+  __syncthreads();  // the tile staging is reused by the block's next tile
+  return total_out;
+}
+
+// ---------------------------------------------------------------------------
 // Stage kernels
 // ---------------------------------------------------------------------------
 // Sort keys.  Full form: k64 = order key of the value, kout = digest key (the
@@ -923,6 +1225,46 @@ __global__ void __launch_bounds__(32 * (CAP == KD_TILE ? 1 : 4)) k_tiles(TileArg
   }
 }
 
+// One block of KD_TILE_WARPS warps per tile above the small-tile cap (the large
+// work list): coalesced load into the slot layout, then block_compress.
+__global__ void __launch_bounds__(KD_TILE_WARPS * 32) k_tiles_blk(TileArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpTile& t = *reinterpret_cast<WarpTile*>(smem_raw);
+  __shared__ BlockScr bs;
+  if (threadIdx.x == 0) bs.stop = kd_err_get(a.err);  // one read, so the block exits as one
+  __syncthreads();
+  if (bs.stop) return;
+  const int T = *a.Tl;
+  if (!tiles_fit(a, T)) return;
+  const KdStoreDev& s = a.s;
+  for (int wi = blockIdx.x; wi < T; wi += gridDim.x) {
+    const int2 wk = a.lv.work_l[wi];
+    const int ai = wk.x, lt = wk.y;
+    const int j = a.lv.j[ai];
+    const int m = a.lv.m[ai];
+    const long long src = (long long)a.lv.base[ai] + (long long)lt * KD_TILE;
+    const int n = min(KD_TILE, m - lt * KD_TILE);
+    const int E = tile_chunk(n), SE = E | 1;
+    const unsigned inv = tile_inv(E);
+    bool integral = true;
+    for (int p = threadIdx.x; p < n; p += blockDim.x) {
+      const int slot = tile_slot(p, E, SE, inv);
+      const double wv = a.dw[src + p];
+      t.x[slot] = a.dx[src + p];
+      t.w[slot] = wv;
+      integral = integral && kd_is_small_int(wv);
+    }
+    integral = __syncthreads_and(integral);
+    const TileOut o = tile_out(a, ai, lt, j, m);
+    const int c = integral
+                      ? block_compress<true>(t, bs, n, s.scale, s.compression, a.force_exact,
+                                             a.id_last, o.m, o.w)
+                      : block_compress<false>(t, bs, n, s.scale, s.compression, a.force_exact,
+                                              a.id_last, o.m, o.w);
+    if (threadIdx.x == 0) *o.count = c;
+  }
+}
+
 struct PlanArgs {
   const int* A;
   const int* Iprev;  // intermediate tiles written by the previous level
@@ -1368,7 +1710,7 @@ int kd_pipeline_prepare_device(KdSession* s) {
   static std::atomic<bool> done[64];
   std::atomic<bool>* flag = (s->device >= 0 && s->device < 64) ? &done[s->device] : nullptr;
   if (flag && flag->load(std::memory_order_acquire)) return KD_OK;
-  KD_CK(cudaFuncSetAttribute(k_tiles<KD_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem()));
+  KD_CK(cudaFuncSetAttribute(k_tiles_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem()));
   KD_CK(cudaFuncSetAttribute(kd_rs_onesweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kd_rs_smem(true)));
   KD_CK(cudaFuncSetAttribute(kd_rs_onesweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1416,7 +1758,7 @@ static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, co
   TileArgs ta{sd, lv.Tl, lv.Ts, lv.I, lv, dx, dw, w.tkey, w.tbuf, w.st_count, w.scr_m,
               w.scr_w, w.tcount, w.cap_work, w.cap_inter, w.needs, s->force_exact, id_last,
               w.err};
-  k_tiles<KD_TILE><<<s->num_sms * s->large_bps, 32, tile_smem(), str>>>(ta);
+  k_tiles_blk<<<s->num_sms * s->large_bps, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
   k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * s->small_bps, 128, tile_smem_small(), str>>>(ta);
   v.launches += 2;
 }
