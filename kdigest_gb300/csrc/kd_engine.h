@@ -161,8 +161,8 @@ struct KdSession {
   // sent to the small-tile kernel, and resident blocks per SM of the two tile
   // kernels.  Defaults are the committed autotuner choice for GB300.
   int small_cap = 128;
-  int large_bps = 7;
-  int small_bps = 12;
+  int large_bps = 6;
+  int small_bps = 8;
   char last_error[256] = {0};  // fixed buffer: reporting an error never allocates
   KdWorkspace ws;
   KdStageStats stats;
