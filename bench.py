@@ -854,7 +854,9 @@ def run_gpu(args):
     # Dominant stage (kernel group) from the stage events on the launching stream.
     stage_ms = {k: v / max(1, st["ingests"]) for k, v in st["stage_ms"].items()}
     dom = max(stage_ms, key=stage_ms.get)
-    passes = 8  # (16-bit key, top 48 value bits) packed into 64 bits, 8-bit digits
+    # (16-bit key, value bits) packed into 64 bits; the sort orders the key and
+    # the top 40 value bits in 8-bit digits (7 passes), the unpack repairs the rest
+    passes = 7
     alg = {
         # one histogram read of the 12 B pairs for all passes, per pass a read
         # and a write of every pair, then the unpack (read + write)
@@ -866,7 +868,7 @@ def run_gpu(args):
     # 2^22-pair batch: `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum`
     # on GB300 (profiles/launches_dram_grouped_ingest_65536keys_batch2p22.md).
     # Below the algorithmic bytes: the ping-pong buffers largely stay in L2.
-    traffic = {"sort": 528.3e6 * BATCH / (1 << 22)}
+    traffic = {}  # re-measured for the 7-pass sort in the next capture
     dom_bytes = alg.get(dom, comp_bytes)
     achieved = dom_bytes / (stage_ms[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),

@@ -62,7 +62,7 @@ void kd_ws_free(KdWorkspace& w) {
                   w.tkey, w.tstart, w.tm, w.tprior, w.tbuf, w.tsf, w.tpscale, w.tmap,
                   w.st_clock, w.st_ls, w.st_min, w.st_max, w.st_count, w.lv_storage,
                   w.work[0], w.work[1], w.work[2], w.work[3], w.dx[0], w.dx[1], w.dw[0], w.dw[1], w.scr_m, w.scr_w,
-                  w.tcount, w.doff, w.needs, w.totals, w.d_call, w.rs_epoch_base};
+                  w.tcount, w.doff, w.needs, w.totals, w.d_call, w.rs_epoch_base, w.fix};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (w.h_call) cudaFreeHost(w.h_call);
@@ -87,7 +87,7 @@ static size_t ws_bytes(long long n, long long keys, long long inter, long long w
   b += (size_t)work * 8 * 4;
   b += (size_t)merged * 16 * 2;
   b += (size_t)inter * (KD_TILE * 16 + 8);
-  b += sizeof(KdCallArgs) + sizeof(unsigned);
+  b += sizeof(KdCallArgs) + sizeof(unsigned) + sizeof(int) * (KD_FIX_CAP + 1);
   return b;
 }
 
@@ -169,6 +169,7 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
   ok &= A((void**)&w.tcount, sizeof(int) * ii);
   ok &= A((void**)&w.doff, sizeof(int) * (ii + 1));
   ok &= A((void**)&w.needs, sizeof(int) * 4);
+  ok &= A((void**)&w.fix, sizeof(int) * (KD_FIX_CAP + 1));
   ok &= A((void**)&w.totals, sizeof(int4) * 8);
   ok &= A((void**)&w.d_call, sizeof(KdCallArgs));
   ok &= cudaHostAlloc((void**)&w.h_call, sizeof(KdCallArgs), cudaHostAllocDefault) == cudaSuccess;
@@ -209,6 +210,7 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
   w.cap_merged = mm;
   w.cap_tmap = tt;
   w.cap_partials = parts;
+  w.cap_fix = KD_FIX_CAP;
   s->mem_used += need;
   return KD_OK;
 }

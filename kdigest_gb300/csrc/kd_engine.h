@@ -73,6 +73,8 @@ struct KdLevelDev {
   int* M;          // dense elements (device scalar)
 };
 
+#define KD_FIX_CAP 65536  // repair-list capacity of the packed sort (a full list re-sorts)
+
 struct KdWorkspace {
   long long cap_n = 0;     // elements
   long long cap_keys = 0;  // touched-key capacity
@@ -123,6 +125,8 @@ struct KdWorkspace {
   int* tcount = nullptr;
   int* doff = nullptr;
   int* needs = nullptr;  // device: required (work, merged, inter) capacities
+  int* fix = nullptr;    // repair list of the packed sort: count, then positions
+  long long cap_fix = 0;
   // scalars: U, T0, I0, A1 ... (int4 totals)
   int4* totals = nullptr;
   KdCallArgs* d_call = nullptr;  // device per-call block (err lives inside it)

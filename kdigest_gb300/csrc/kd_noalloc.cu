@@ -107,6 +107,8 @@ size_t carve(uintptr_t base, KdWorkspace& w, KdStoreDev& d, double** stage) {
   w.tcount = c.take<int>(kInter);
   w.doff = c.take<int>(kInter + 1);
   w.needs = c.take<int>(4);
+  w.cap_fix = 2048;  // a fuller list falls back to the full sort
+  w.fix = c.take<int>(w.cap_fix + 1);
   w.totals = c.take<int4>(8);
   w.d_call = c.take<KdCallArgs>(1);
   w.err = &w.d_call->err;

@@ -30,6 +30,7 @@
 #define KD_ERANGE_SCRATCH KD_ERANGE_SCRATCH_INTERNAL  // scratch too small (index = needed)
 #define KD_EMORE_LEVELS 101    // internal: keys still above one tile after the levels run
 #define KD_ERESORT 102         // internal: the packed sort left an inversion; sort in full
+#define KD_PACK_VALUE_BITS 40  // value bits the packed sort orders at least
 
 __device__ __forceinline__ size_t slot_base(long long K, int buf, long long key) {
   return ((size_t)buf * (size_t)K + (size_t)key) * KD_TILE;
@@ -809,45 +810,77 @@ struct PrepareArgs {
 
 // _gpu_batch_prepare per touched key (tdigest.mojo:236-296), _advance_clock
 // (:324-332), _renormalize (:359-371), _scale_factor (:352-357).
-// Packed sort keys back to (order key, digest key), from the sort's last
-// buffers into the free ones, repairing the order where the packed sort could
-// not see it: samples of one key with equal packed bits form a run still in
-// input order; the run's first element copies the run, sorts it by the low
-// bits (insertion sort, stable) and unpacks it.  Runs longer than
-// KD_PACK_RUN_MAX (adversarial data only) send the step to the full sort.
-// Sources are read-only and every destination run has one writer.
-#define KD_PACK_RUN_MAX 64
-__global__ void k_unpack(long long n, int kb, const uint64_t* __restrict__ sk,
+// After the packed sort (digest key and the top value bits, sorted on all but
+// the lowest `shift` bits): the sort keys back to (order key, digest key),
+// from the sort's last buffers into the free ones, one element per thread.
+// Samples of one key that agree in the sorted bits form a run in input order;
+// an element smaller than its left neighbour inside such a run is recorded in
+// the repair list (fix[0] = count, fix[1..cap]).  Runs of equal values record
+// nothing.  A full list sends the step to the full sort.
+__global__ void k_unpack(long long n, int kb, int shift, const uint64_t* __restrict__ sk,
                          const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx,
                          uint64_t* __restrict__ dk, uint32_t* __restrict__ dkey,
-                         uint32_t* __restrict__ didx, KdErrHost* err) {
+                         uint32_t* __restrict__ didx, int* __restrict__ fix, int cap_fix,
+                         KdErrHost* err) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const uint64_t p = sk[i];
-    if (i > 0 && sk[i - 1] == p) continue;  // inside a run: its first element owns it
-    long long e = i + 1;
-    while (e < n && e - i <= KD_PACK_RUN_MAX && sk[e] == p) ++e;
-    if (e - i > KD_PACK_RUN_MAX) {
+    const uint64_t ok = (p << kb) | (uint64_t)skey[i];
+    dk[i] = ok;
+    dkey[i] = kb > 0 ? (uint32_t)(p >> (64 - kb)) : 0u;
+    if (didx) didx[i] = sidx[i];
+    if (i > 0) {
+      const uint64_t pp = sk[i - 1];
+      if ((pp >> shift) == (p >> shift) && ((pp << kb) | (uint64_t)skey[i - 1]) > ok) {
+        const int slot = atomicAdd(&fix[0], 1);
+        if (slot < cap_fix) fix[1 + slot] = (int)i;
+        else kd_err_set(err, KD_ERESORT, i);
+      }
+    }
+  }
+}
+
+// Repairs the runs that hold a recorded inversion: the run's first inversion
+// owns it (runs are disjoint, so every run has one writer), finds its ends and
+// sorts it by order key, stably, carrying the input indices.  Runs longer
+// than KD_PACK_RUN_MAX with an inversion (adversarial data) send the step to
+// the full sort.  Source arrays are read-only; only owners write.
+#define KD_PACK_RUN_MAX 64
+__global__ void k_repair(long long n, int kb, int shift, const uint64_t* __restrict__ sk,
+                         const uint32_t* __restrict__ skey, uint64_t* __restrict__ dk,
+                         uint32_t* __restrict__ didx, const int* __restrict__ fix, int cap_fix,
+                         KdErrHost* err) {
+  const int nf = min(fix[0], cap_fix);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x) {
+    const long long i = fix[1 + t];
+    const uint64_t top = sk[i] >> shift;
+    long long s = i;
+    while (s > 0 && i - s < KD_PACK_RUN_MAX && (sk[s - 1] >> shift) == top) --s;
+    if (s > 0 && (sk[s - 1] >> shift) == top) {
       kd_err_set(err, KD_ERESORT, i);
       continue;
     }
-    const uint32_t kid = (uint32_t)(p >> (64 - kb));
-    for (long long a = i; a < e; ++a) {  // stable insertion sort by the low bits
-      const uint32_t lv = skey[a];
-      const uint32_t iv = sidx ? sidx[a] : 0u;
+    bool owner = true;  // no inversion before i in the run
+    for (long long a = s + 1; a < i && owner; ++a)
+      owner = !(((sk[a - 1] << kb) | (uint64_t)skey[a - 1]) > ((sk[a] << kb) | (uint64_t)skey[a]));
+    if (!owner) continue;
+    long long e = i + 1;
+    while (e < n && e - s <= KD_PACK_RUN_MAX && (sk[e] >> shift) == top) ++e;
+    if (e - s > KD_PACK_RUN_MAX) {
+      kd_err_set(err, KD_ERESORT, i);
+      continue;
+    }
+    for (long long a = s + 1; a < e; ++a) {  // stable insertion sort by order key
+      const uint64_t v = dk[a];
+      const uint32_t iv = didx ? didx[a] : 0u;
       long long b = a;
-      while (b > i && dkey[b - 1] > lv) {
-        dkey[b] = dkey[b - 1];
+      while (b > s && dk[b - 1] > v) {
+        dk[b] = dk[b - 1];
         if (didx) didx[b] = didx[b - 1];
         --b;
       }
-      dkey[b] = lv;
+      dk[b] = v;
       if (didx) didx[b] = iv;
-    }
-    for (long long a = i; a < e; ++a) {
-      const uint32_t low = dkey[a];
-      dkey[a] = kid;
-      dk[a] = (p << kb) | (uint64_t)low;
     }
   }
 }
@@ -1812,6 +1845,7 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   v.note(cudaMemcpyAsync(w.d_call, w.h_call, sizeof(KdCallArgs), cudaMemcpyHostToDevice, str));
   v.note(cudaMemsetAsync(w.totals, 0, sizeof(int4) * 8, str));
   v.note(cudaMemsetAsync(w.needs, 0, sizeof(int) * 4, str));
+  v.note(cudaMemsetAsync(w.fix, 0, sizeof(int), str));  // repair-list count
   stage_mark(s, 0);
   {
     int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
@@ -1821,15 +1855,22 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   }
   stage_mark(s, 1);
   KdSortBufs sb = sort_bufs(w);
+  // Packed form: the sort covers the key bits and at least KD_PACK_VALUE_BITS
+  // value bits; lower digits are left to the repair (runs of near-equal values).
+  const int first_digit = full_sort ? 0 : std::max(0, (64 - key_bits - KD_PACK_VALUE_BITS) / 8);
   const int sort_bits = full_sort ? key_bits : 0;  // packed keys need no key passes
-  int r = kd_radix_sort(sb, n, sort_bits, with_idx, s->num_sms, str);
-  v.launches += kd_radix_sort_launches(n, sort_bits);
-  if (!full_sort && key_bits > 0) {
+  int r = kd_radix_sort(sb, n, sort_bits, with_idx, s->num_sms, str, first_digit);
+  v.launches += kd_radix_sort_launches(n, sort_bits, first_digit);
+  if (!full_sort) {  // also for n == 1: the key is still packed
     const int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
-    k_unpack<<<grid, 256, 0, str>>>(n, key_bits, w.k64[r], w.key[r], with_idx ? w.idx[r] : nullptr,
-                                    w.k64[r ^ 1], w.key[r ^ 1], with_idx ? w.idx[r ^ 1] : nullptr,
-                                    w.err);
-    v.launches += 1;
+    const int shift = 8 * first_digit;
+    k_unpack<<<grid, 256, 0, str>>>(n, key_bits, shift, w.k64[r], w.key[r],
+                                    with_idx ? w.idx[r] : nullptr, w.k64[r ^ 1], w.key[r ^ 1],
+                                    with_idx ? w.idx[r ^ 1] : nullptr, w.fix, (int)w.cap_fix, w.err);
+    k_repair<<<s->num_sms, 256, 0, str>>>(n, key_bits, shift, w.k64[r], w.key[r], w.k64[r ^ 1],
+                                          with_idx ? w.idx[r ^ 1] : nullptr, w.fix, (int)w.cap_fix,
+                                          w.err);
+    v.launches += 2;
     r ^= 1;
   }
   stage_mark(s, 2);

@@ -259,7 +259,7 @@ static inline void kd_rs_epoch_reserve(KdSortBufs& b, cudaStream_t st) {
 // Sorts by (key, k64); returns the index (0/1) of the buffer set holding the
 // result.  Enqueues device work only (no host state), so it can be captured.
 static inline int kd_radix_sort(KdSortBufs& b, long long n, int key_bits, bool with_idx,
-                                int num_sms, cudaStream_t st) {
+                                int num_sms, cudaStream_t st, int first_digit = 0) {
   int src = 0;
   if (n <= 1) return src;
   const int nb = kd_rs_blocks(n);
@@ -281,11 +281,11 @@ static inline int kd_radix_sort(KdSortBufs& b, long long n, int key_bits, bool w
     ticket_base += (unsigned long long)nb;
     src = dst;
   };
-  for (int p = 0; p < 8; ++p) pass(8 * p, 0, p);
+  for (int p = first_digit; p < 8; ++p) pass(8 * p, 0, p);  // digits below first_digit unsorted
   for (int p = 0; p < key_passes; ++p) pass(8 * p, 1, 8 + p);
   return src;
 }
 
-static inline int kd_radix_sort_launches(long long n, int key_bits) {
-  return n > 1 ? 1 + 8 + (key_bits + 7) / 8 : 0;
+static inline int kd_radix_sort_launches(long long n, int key_bits, int first_digit = 0) {
+  return n > 1 ? 1 + (8 - first_digit) + (key_bits + 7) / 8 : 0;
 }
