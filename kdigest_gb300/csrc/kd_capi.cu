@@ -482,6 +482,20 @@ KD_API void kd_store_destroy(kd_store* st) {
   delete st;
 }
 
+// Kernel-addressable view of a host pointer, or null.  Page-locked (pinned)
+// host memory is mapped into the device address space: on GB300 the kernels
+// read it in place over the coherent host link, so an ingest from pinned
+// buffers needs no staging copy (the bytes still cross the link once, inside
+// the call).  Pageable memory returns null and is staged.
+static const void* mapped_view(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 KD_API int kd_store_ingest(kd_store* h, const uint32_t* keys, const double* values, int64_t n,
                            int clock_mode, double timestamp, int flags) {
   if (!h) return KD_EINVAL;
@@ -494,7 +508,12 @@ KD_API int kd_store_ingest(kd_store* h, const uint32_t* keys, const double* valu
   cudaSetDevice(s->device);
   const uint32_t* dk = keys;
   const double* dv = values;
-  if (!(flags & KD_PTR_DEVICE)) {
+  const void* mk = (flags & KD_PTR_DEVICE) || !keys ? nullptr : mapped_view(keys);
+  const void* mv = (flags & KD_PTR_DEVICE) ? nullptr : mapped_view(values);
+  if (!(flags & KD_PTR_DEVICE) && mv && (!keys || mk)) {  // pinned: read in place
+    dk = (const uint32_t*)mk;
+    dv = (const double*)mv;
+  } else if (!(flags & KD_PTR_DEVICE)) {
     size_t kb = keys ? ((size_t)n * 4 + 15) / 16 * 16 : 0;
     int rc = stage_in(s, kb + (size_t)n * 8);
     if (rc) return rc;

@@ -315,3 +315,40 @@ def test_grouped_filter_matches_exact_path(kd, scale):
         ma, wa = out[0].centroids(k)
         mb, wb = out[1].centroids(k)
         assert np.array_equal(ma, mb) and np.array_equal(wa, wb)
+
+
+def test_ingest_from_pinned_host_buffers(kd):
+    """Pinned host inputs are read in place by the kernels; pageable ones are
+    staged; device pointers are used as they are: the same digests."""
+    torch = pytest.importorskip("torch")
+    from kdigest_gb300 import _native as N
+
+    nk, n = 777, 300000
+    rng = np.random.default_rng(41)
+    k = (rng.zipf(1.2, n) % nk).astype(np.uint32)
+    v = rng.standard_normal(n) * 4
+    pk = torch.from_numpy(k.view(np.int32)).pin_memory()
+    pv = torch.from_numpy(v).pin_memory()
+    dk = pk.cuda()
+    dv = pv.cuda()
+    L = N.load()
+    stores = []
+    for mode in ("pinned", "pageable", "device"):
+        g = kd.GroupedTDigest(nk, 100.0, scale=kd.K2)
+        for _ in range(2):
+            if mode == "pinned":
+                rc = L.kd_store_ingest(g._store._h, pk.data_ptr(), pv.data_ptr(), n, 0, 0.0, 0)
+            elif mode == "pageable":
+                rc = L.kd_store_ingest(g._store._h, N.ptr(k), N.ptr(v), n, 0, 0.0, 0)
+            else:
+                torch.cuda.synchronize()
+                rc = L.kd_store_ingest(g._store._h, dk.data_ptr(), dv.data_ptr(), n, 0, 0.0,
+                                       N.KD_PTR_DEVICE)
+            assert rc == 0
+        stores.append(g)
+    for g in stores[1:]:
+        assert np.array_equal(g.centroid_counts(), stores[0].centroid_counts())
+        for key in range(0, nk, 37):
+            ma, wa = g.centroids(key)
+            mb, wb = stores[0].centroids(key)
+            assert np.array_equal(ma, mb) and np.array_equal(wa, wb)
