@@ -864,11 +864,11 @@ def run_gpu(args):
         "level0": 8 * BATCH + touched_avg * 16 * 2 * prior_avg,
         "prep": 12 * BATCH + 12 * BATCH,
     }
-    # DRAM bytes of one sort stage (histogram, 8 packed passes, unpack) of a
+    # DRAM bytes of one sort stage (histogram, 7 packed passes, unpack, repair) of a
     # 2^22-pair batch: `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum`
     # on GB300 (profiles/launches_dram_grouped_ingest_65536keys_batch2p22.md).
     # Below the algorithmic bytes: the ping-pong buffers largely stay in L2.
-    traffic = {}  # re-measured for the 7-pass sort in the next capture
+    traffic = {"sort": 473.1e6 * BATCH / (1 << 22)}
     dom_bytes = alg.get(dom, comp_bytes)
     achieved = dom_bytes / (stage_ms[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
