@@ -174,12 +174,31 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
   const int cnt = max(0, min(E, n - lo));
   const int sb = lane * SE;
 
-  // 1. In-chunk inclusive prefix of the weights, serial per lane.
+  // 1. In-chunk inclusive prefix of the weights, serial per lane.  A one-chunk
+  //    tile with integral weights (exact int64 sums, any order gives the same
+  //    values) is scanned by the whole warp, 32 elements per round.
   T acc = 0;
-  for (int j = 0; j < cnt; ++j) {
-    const T wv = A::from_w(t.w[sb + j]);
-    acc = j == 0 ? wv : A::add(acc, wv);
-    t.L[sb + j] = A::store(acc);
+  if (kInt && CAP <= KD_SERIAL_TILE_MAX) {
+    T carry = 0;
+    for (int r0 = 0; r0 < n; r0 += 32) {
+      const int p = r0 + lane;  // one chunk: slot p holds element p
+      T v = p < n ? A::from_w(t.w[p]) : (T)0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const T u = A::shfl_up(v, o);
+        if (lane >= o) v = A::add(v, u);
+      }
+      v = A::add(v, carry);
+      if (p < n) t.L[p] = A::store(v);
+      carry = A::shfl(v, 31);
+    }
+    acc = carry;  // lane 0 owns the single chunk: its total
+  } else {
+    for (int j = 0; j < cnt; ++j) {
+      const T wv = A::from_w(t.w[sb + j]);
+      acc = j == 0 ? wv : A::add(acc, wv);
+      t.L[sb + j] = A::store(acc);
+    }
   }
   // 2. Chunk totals -> Kogge-Stone over lanes -> exclusive chunk prefix.
   T I = cnt > 0 ? acc : (T)0;
