@@ -4,7 +4,9 @@
 // One ingest (grouped add_batch, grouped.mojo:60-162 with gpu/grouped.mojo:415-643
 // semantics per key) runs entirely on the device:
 //   prep     validate (key range, finite values) and map values to order keys
-//   sort     stable LSD radix sort by (key, value)            (gpu/sort.mojo)
+//   sort     stable LSD radix sort by (key, value)            (gpu/sort.mojo):
+//            the key and the top value bits packed into 64 bits, the low
+//            value bits restored and their runs repaired by unpack / repair
 //   touched  compact the keys present in the batch
 //   prepare  per key: clock / decay / renormalise / min-max   (tdigest.mojo:236-296)
 //   level 0  per 1024 tile of (prior centroids ++ new samples): merge-path load
@@ -746,12 +748,12 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
 // Stage kernels
 // ---------------------------------------------------------------------------
 // Sort keys.  Full form: k64 = order key of the value, kout = digest key (the
-// sort then runs 8 value passes and ceil(kb / 8) key passes).  Packed form
-// (kb > 0): k64 = digest key in the top kb bits above the top 64 - kb bits of
-// the order key, kout = the order key's low kb bits; 8 passes sort it, and
-// k_unpack restores the full form.  Samples of one key whose order keys agree
-// in the top 64 - kb bits keep their input order, so the packed order can
-// only be wrong between such samples; k_merge_new checks it.
+// sort then runs 8 value passes and ceil(kb / 8) key passes).  Packed form:
+// k64 = digest key in the top kb bits above the top 64 - kb bits of the order
+// key, kout = the order key's low kb bits.  The sort orders the key and at
+// least KD_PACK_VALUE_BITS value bits; samples of one key that agree in the
+// sorted bits keep their input order, and k_unpack / k_repair restore the full
+// form and the exact order among them.
 __global__ void k_prep(long long n, const KdCallArgs* __restrict__ call, long long K, int kb,
                        uint64_t* __restrict__ k64, uint32_t* __restrict__ kout,
                        uint32_t* __restrict__ idx, KdErrHost* err) {
@@ -1073,107 +1075,6 @@ __global__ void __launch_bounds__(1024) k_inter0(InterArgs p) {
   }
 }
 
-struct MergeArgs {
-  KdStoreDev s;
-  long long n;
-  const uint64_t* k64;
-  const uint32_t* skey;
-  const uint32_t* sidx;
-  const KdCallArgs* call;  // per-sample weights (or null: unit weights)
-  const uint32_t* tkey;
-  const uint32_t* tmap;
-  const int* tstart;
-  const int* tprior;
-  const unsigned char* tbuf;
-  const double* tsf;
-  const double* tpscale;
-  const int* base;
-  const int4* totals;
-  double* dx;
-  double* dw;
-  long long cap_merged;
-  int* needs;
-  KdErrHost* err;
-};
-
-__device__ __forceinline__ bool merged_fits(const MergeArgs& a) {
-  const int M0 = a.totals[1].w;
-  if (M0 > a.cap_merged) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      atomicMax(&a.needs[1], M0);
-      kd_err_set(a.err, KD_ERANGE_SCRATCH, M0);
-    }
-    return false;
-  }
-  return true;
-}
-
-// New samples: merged position = rank among the key's new samples + number of
-// prior centroids with mean <= value (priors precede new samples on ties, their
-// indices being lower, gpu/grouped.mojo:489-538).
-__global__ void k_merge_new(MergeArgs a) {
-  if (kd_err_get(a.err) || !merged_fits(a)) return;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const uint32_t k = a.skey[i];
-    const int j = (int)a.tmap[k];
-    const int jn = (int)(i - a.tstart[j]);
-    const int np = a.tprior[j];
-    const uint64_t vk = a.k64[i];
-    // the packed sort is exact unless two samples of a key shared the packed
-    // bits and their low bits came out of order: then sort again in full
-    if (i > 0 && a.skey[i - 1] == k && a.k64[i - 1] > vk) kd_err_set(a.err, KD_ERESORT, i);
-    int lo = 0;
-    if (np > 0) {
-      const double* pm = a.s.slot_m + slot_base(a.s.K, a.tbuf[j] ^ 1, k);
-      int hi = np;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (kd_order_key(pm[mid]) <= vk) lo = mid + 1;
-        else hi = mid;
-      }
-    }
-    const long long pos = (long long)a.base[j] + jn + lo;
-    a.dx[pos] = kd_from_order_key(vk);
-    const double* wts = a.call->wts;
-    a.dw[pos] = wts ? wts[a.sidx[i]] : a.tsf[j];
-  }
-}
-
-// Prior centroids: merged position = prior index + number of new samples with
-// value < mean.  One warp per touched key.
-__global__ void k_merge_prior(MergeArgs a) {
-  if (kd_err_get(a.err) || !merged_fits(a)) return;
-  const int U = a.totals[0].x;
-  const int lane = threadIdx.x & 31;
-  for (int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < U;
-       j += (gridDim.x * blockDim.x) >> 5) {
-    const int np = a.tprior[j];
-    if (np == 0) continue;
-    const uint32_t k = a.tkey[j];
-    const int s0 = a.tstart[j];
-    const int nn = (j + 1 < U ? a.tstart[j + 1] : (int)a.n) - s0;
-    const int live = a.tbuf[j] ^ 1;
-    const double* pm = a.s.slot_m + slot_base(a.s.K, live, k);
-    const double* pw = a.s.slot_w + slot_base(a.s.K, live, k);
-    const double pscale = a.tpscale[j];
-    const bool rescale = pscale != 1.0;
-    const uint64_t* nk = a.k64 + s0;
-    for (int i = lane; i < np; i += 32) {
-      const uint64_t pk = kd_order_key(pm[i]);
-      int lo = 0, hi = nn;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (nk[mid] < pk) lo = mid + 1;
-        else hi = mid;
-      }
-      const long long pos = (long long)a.base[j] + i + lo;
-      a.dx[pos] = kd_from_order_key(pk);
-      a.dw[pos] = rescale ? KD_MUL(pw[i], pscale) : pw[i];
-    }
-  }
-}
-
 struct TileArgs {
   KdStoreDev s;
   const int* Tl;
@@ -1194,7 +1095,62 @@ struct TileArgs {
   int force_exact;
   int id_last;  // bucket id at q == 1 for K0/K1 (a launch constant)
   KdErrHost* err;
+  // Level 0 reads no dense input: each tile is merged on the fly from the
+  // key's prior centroids (live slot) and its sorted new samples.
+  int level0;
+  const uint64_t* k64;    // sorted order keys of the new samples
+  const uint32_t* sidx;   // their input positions (per-sample weights), or null
+  const KdCallArgs* call;
+  const int* tstart;
+  const int* tprior;
+  const double* tsf;
+  const double* tpscale;
+  const int4* totals;
+  long long n;
 };
+
+// Elements [d0 + q0, d0 + q1) of the merged input of touched key j: its prior
+// centroids (weights rescaled by the renormalisation factor) and its new
+// samples (their own weight, or the key's decay weight), ordered by value with
+// priors first on equal values (gpu/sort.mojo:38-41).  A merge-path binary
+// search finds where the range starts, then the range is merged in order;
+// put(q, value, weight) receives every element.
+template <class Put>
+__device__ __forceinline__ void merge_load(const TileArgs& a, int j, int d0, int q0, int q1, Put put) {
+  if (q0 >= q1) return;
+  const int U = a.totals[0].x;
+  const int np = a.tprior[j];
+  const int s0 = a.tstart[j];
+  const int nn = (j + 1 < U ? a.tstart[j + 1] : (int)a.n) - s0;
+  const uint32_t key = a.tkey[j];
+  const int live = a.tbuf[j] ^ 1;
+  const double* pm = a.s.slot_m + slot_base(a.s.K, live, key);
+  const double* pw = a.s.slot_w + slot_base(a.s.K, live, key);
+  const double pscale = a.tpscale[j];
+  const bool rescale = pscale != 1.0;
+  const double sf = a.tsf[j];
+  const uint64_t* nk = a.k64 + s0;
+  const double* wts = a.call->wts;
+  const uint32_t* sidx = a.sidx ? a.sidx + s0 : nullptr;
+  const int d = d0 + q0;
+  int lo = max(0, d - nn), hi = min(d, np);
+  while (lo < hi) {  // priors among the first d merged elements
+    const int mid = (lo + hi) >> 1;
+    if (kd_order_key(pm[mid]) <= nk[d - mid - 1]) lo = mid + 1;
+    else hi = mid;
+  }
+  int ia = lo, ib = d - lo;
+  for (int q = q0; q < q1; ++q) {
+    const bool take_prior = ia < np && (ib >= nn || kd_order_key(pm[ia]) <= nk[ib]);
+    if (take_prior) {
+      put(q, kd_from_order_key(kd_order_key(pm[ia])), rescale ? KD_MUL(pw[ia], pscale) : pw[ia]);
+      ++ia;
+    } else {
+      put(q, kd_from_order_key(nk[ib]), wts ? wts[sidx[ib]] : sf);
+      ++ib;
+    }
+  }
+}
 
 __device__ __forceinline__ bool tiles_fit(const TileArgs& a, int T) {
   const int I = *a.I;
@@ -1258,12 +1214,23 @@ __global__ void __launch_bounds__(32 * (CAP == KD_TILE ? 1 : 4)) k_tiles(TileArg
     const int E = tile_chunk(n), SE = E | 1;
     const unsigned inv = tile_inv(E);
     bool integral = true;
-    for (int p = lane; p < n; p += 32) {
-      const int slot = tile_slot(p, E, SE, inv);
-      const double wv = a.dw[src + p];
-      t.x[slot] = a.dx[src + p];
-      t.w[slot] = wv;
-      integral = integral && kd_is_small_int(wv);
+    if (a.level0) {
+      const int per = (n + 31) >> 5;
+      merge_load(a, j, lt * KD_TILE, min(n, lane * per), min(n, lane * per + per),
+                 [&](int q, double xv, double wv) {
+                   const int slot = tile_slot(q, E, SE, inv);
+                   t.x[slot] = xv;
+                   t.w[slot] = wv;
+                   integral = integral && kd_is_small_int(wv);
+                 });
+    } else {
+      for (int p = lane; p < n; p += 32) {
+        const int slot = tile_slot(p, E, SE, inv);
+        const double wv = a.dw[src + p];
+        t.x[slot] = a.dx[src + p];
+        t.w[slot] = wv;
+        integral = integral && kd_is_small_int(wv);
+      }
     }
     integral = __all_sync(0xffffffffu, integral);
     __syncwarp();
@@ -1299,12 +1266,23 @@ __global__ void __launch_bounds__(KD_TILE_WARPS * 32) k_tiles_blk(TileArgs a) {
     const int E = tile_chunk(n), SE = E | 1;
     const unsigned inv = tile_inv(E);
     bool integral = true;
-    for (int p = threadIdx.x; p < n; p += blockDim.x) {
-      const int slot = tile_slot(p, E, SE, inv);
-      const double wv = a.dw[src + p];
-      t.x[slot] = a.dx[src + p];
-      t.w[slot] = wv;
-      integral = integral && kd_is_small_int(wv);
+    if (a.level0) {
+      const int per = (n + blockDim.x - 1) / blockDim.x;
+      const int q0 = min(n, (int)threadIdx.x * per);
+      merge_load(a, j, lt * KD_TILE, q0, min(n, q0 + per), [&](int q, double xv, double wv) {
+        const int slot = tile_slot(q, E, SE, inv);
+        t.x[slot] = xv;
+        t.w[slot] = wv;
+        integral = integral && kd_is_small_int(wv);
+      });
+    } else {
+      for (int p = threadIdx.x; p < n; p += blockDim.x) {
+        const int slot = tile_slot(p, E, SE, inv);
+        const double wv = a.dw[src + p];
+        t.x[slot] = a.dx[src + p];
+        t.w[slot] = wv;
+        integral = integral && kd_is_small_int(wv);
+      }
     }
     integral = __syncthreads_and(integral);
     const TileOut o = tile_out(a, ai, lt, j, m);
@@ -1805,11 +1783,24 @@ static KdSortBufs sort_bufs(KdWorkspace& w) {
 }
 
 static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, const KdLevelDev& lv,
-                          const double* dx, const double* dw, int id_last, KdStepView& v) {
+                          const double* dx, const double* dw, int id_last, KdStepView& v,
+                          const TileArgs* level0 = nullptr) {
   cudaStream_t str = s->stream;
   TileArgs ta{sd, lv.Tl, lv.Ts, lv.I, lv, dx, dw, w.tkey, w.tbuf, w.st_count, w.scr_m,
               w.scr_w, w.tcount, w.cap_work, w.cap_inter, w.needs, s->force_exact, id_last,
               w.err};
+  if (level0) {  // merge inputs of level 0
+    ta.level0 = 1;
+    ta.k64 = level0->k64;
+    ta.sidx = level0->sidx;
+    ta.call = level0->call;
+    ta.tstart = level0->tstart;
+    ta.tprior = level0->tprior;
+    ta.tsf = level0->tsf;
+    ta.tpscale = level0->tpscale;
+    ta.totals = level0->totals;
+    ta.n = level0->n;
+  }
   k_tiles_blk<<<s->num_sms * s->large_bps, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
   k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * s->small_bps, 128, tile_smem_small(), str>>>(ta);
   v.launches += 2;
@@ -1918,17 +1909,19 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
     InterArgs ia{a1, l0, w.lv[1], l0.I, w.cap_inter, w.needs, w.err};
     k_inter0<<<1, 1024, 0, str>>>(ia);
   }
-  {
-    MergeArgs ma{sd, n, k64, skey, sidx, w.d_call, w.tkey, w.tmap, w.tstart, w.tprior, w.tbuf,
-                 w.tsf, w.tpscale, l0.base, w.totals, w.dx[0], w.dw[0], w.cap_merged, w.needs, w.err};
-    int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
-    k_merge_new<<<grid, 256, 0, str>>>(ma);
-    int pgrid = (int)std::min<long long>((keys_max * 32 + 255) / 256, (long long)s->num_sms * 16);
-    k_merge_prior<<<pgrid, 256, 0, str>>>(ma);
-  }
-  v.launches += 3 + 1 + 3 + 1 + 2;
+  v.launches += 3 + 1 + 3 + 1;
   stage_mark(s, 3);
-  enqueue_tiles(s, w, sd, l0, w.dx[0], w.dw[0], id_last, v);
+  TileArgs m0{};
+  m0.k64 = k64;
+  m0.sidx = sidx;
+  m0.call = w.d_call;
+  m0.tstart = w.tstart;
+  m0.tprior = w.tprior;
+  m0.tsf = w.tsf;
+  m0.tpscale = w.tpscale;
+  m0.totals = w.totals;
+  m0.n = n;
+  enqueue_tiles(s, w, sd, l0, nullptr, nullptr, id_last, v, &m0);
   stage_mark(s, 4);
   v.curA = a1;
   v.Iprev = l0.I;
