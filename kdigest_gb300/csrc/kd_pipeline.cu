@@ -86,6 +86,11 @@ static_assert(offsetof(WarpTile, ef) == offsetof(WarpTile, hf) + WarpTile::SLOTS
 static_assert(offsetof(WarpTileSmall, ef) == offsetof(WarpTileSmall, hf) + WarpTileSmall::SLOTS &&
                   2 * WarpTileSmall::SLOTS >= 2 * KD_SERIAL_TILE_MAX,
               "position list overlays hf/ef");
+// The small-tile loader stages up to KD_SERIAL_TILE_MAX order keys in L and
+// as many in the contiguous P .. endpos block.
+static_assert(sizeof(((WarpTileSmall*)0)->L) >= 8 * KD_SERIAL_TILE_MAX &&
+                  sizeof(WarpTileSmall) - offsetof(WarpTileSmall, P) >= 8 * KD_SERIAL_TILE_MAX,
+              "small-tile merge staging");
 static_assert(offsetof(WarpTile, endpos) == offsetof(WarpTile, headpos) + 2 * KD_TILE &&
                   offsetof(WarpTileSmall, endpos) ==
                       offsetof(WarpTileSmall, headpos) + 2 * KD_SERIAL_TILE_MAX,
@@ -1214,7 +1219,57 @@ __global__ void __launch_bounds__(32 * (CAP == KD_TILE ? 1 : 4)) k_tiles(TileArg
     const int E = tile_chunk(n), SE = E | 1;
     const unsigned inv = tile_inv(E);
     bool integral = true;
-    if (a.level0) {
+    if (a.level0 && CAP <= KD_SERIAL_TILE_MAX && m <= CAP) {
+      // The key's whole merged input is this tile: stage both sorted lists'
+      // order keys in shared memory (one round of loads each), then place
+      // every element by a shared-memory search (a new sample after the
+      // priors <= it, a prior after the new samples < it).
+      const int U = a.totals[0].x;
+      const int np = a.tprior[j];
+      const int s0 = a.tstart[j];
+      const int nn = (j + 1 < U ? a.tstart[j + 1] : (int)a.n) - s0;
+      const uint32_t key = a.tkey[j];
+      const int live = a.tbuf[j] ^ 1;
+      const double* pm = s.slot_m + slot_base(s.K, live, key);
+      const double* pw = s.slot_w + slot_base(s.K, live, key);
+      uint64_t* pk = reinterpret_cast<uint64_t*>(t.L);     // prior order keys
+      uint64_t* nk = reinterpret_cast<uint64_t*>(t.P);     // new order keys (P .. endpos)
+      for (int i = lane; i < np; i += 32) pk[i] = kd_order_key(pm[i]);
+      for (int i = lane; i < nn; i += 32) nk[i] = a.k64[s0 + i];
+      __syncwarp();
+      const double pscale = a.tpscale[j];
+      const double sf = a.tsf[j];
+      const double* wts = a.call->wts;
+      for (int i = lane; i < np; i += 32) {
+        const uint64_t v = pk[i];
+        int lo = 0, hi = nn;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (nk[mid] < v) lo = mid + 1;
+          else hi = mid;
+        }
+        const double wv = pscale != 1.0 ? KD_MUL(pw[i], pscale) : pw[i];
+        const int slot = tile_slot(i + lo, E, SE, inv);
+        t.x[slot] = kd_from_order_key(v);
+        t.w[slot] = wv;
+        integral = integral && kd_is_small_int(wv);
+      }
+      for (int i = lane; i < nn; i += 32) {
+        const uint64_t v = nk[i];
+        int lo = 0, hi = np;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (pk[mid] <= v) lo = mid + 1;
+          else hi = mid;
+        }
+        const double wv = wts ? wts[a.sidx[s0 + i]] : sf;
+        const int slot = tile_slot(i + lo, E, SE, inv);
+        t.x[slot] = kd_from_order_key(v);
+        t.w[slot] = wv;
+        integral = integral && kd_is_small_int(wv);
+      }
+      __syncwarp();
+    } else if (a.level0) {
       const int per = (n + 31) >> 5;
       merge_load(a, j, lt * KD_TILE, min(n, lane * per), min(n, lane * per + per),
                  [&](int q, double xv, double wv) {
