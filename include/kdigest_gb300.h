@@ -138,6 +138,21 @@ KD_API int kd_store_stats(kd_store* st, int64_t* num_keys, int64_t* total_centro
  * for all keys at once (grouped.mojo:182-185). */
 KD_API int kd_store_counts(kd_store* st, int32_t* out, int flags);
 
+/* to_bytes for many keys at once (tdigest.mojo:627-648 per record): the records
+ * of keys[0..nkeys) (keys NULL: keys 0..nkeys-1) concatenated in buf;
+ * offsets[i] (host, nkeys + 1 entries) is where record i starts and
+ * offsets[nkeys] the total.  buf NULL computes the offsets only.  The reference
+ * serialises one digest per call; batching the records is a checkpoint of a
+ * resident store. */
+KD_API int kd_store_export(kd_store* st, const uint32_t* keys, int64_t nkeys, uint8_t* buf,
+                           int64_t cap, int64_t* offsets, int flags);
+/* from_bytes for many keys (tdigest.mojo:650-698 per record): record i,
+ * buf[offsets[i] .. offsets[i+1]), is installed as key keys[i] (keys NULL: i).
+ * Every record is validated before any key changes (KD_EINVAL: version or key,
+ * KD_ERANGE: truncated).  The store keeps its own compression and decay rate. */
+KD_API int kd_store_import(kd_store* st, const uint32_t* keys, int64_t nkeys, const uint8_t* buf,
+                           const int64_t* offsets, int flags);
+
 /* Serving loop over a resident store (no counterpart in the reference, which
  * has none).  Client threads submit ingest and query requests with
  * non-decreasing timestamps; a worker thread serves them by continuous

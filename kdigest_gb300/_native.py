@@ -31,6 +31,7 @@ EXPORTED = (
     "kd_store_counts", "kd_compress_noalloc",
     "kd_server_create", "kd_server_submit", "kd_server_advance", "kd_server_wait",
     "kd_server_flush", "kd_server_stats", "kd_server_destroy",
+    "kd_store_export", "kd_store_import",
 )
 KD_REQ_INGEST, KD_REQ_QUANTILE, KD_REQ_CDF = 0, 1, 2
 
@@ -87,6 +88,8 @@ def load(path: str = LIB_PATH):
     L.kd_store_to_bytes.argtypes = [_P, ctypes.c_uint32, _P, _I64, ctypes.POINTER(_I64)]
     L.kd_store_from_bytes.argtypes = [_P, ctypes.c_uint32, _P, _I64]
     L.kd_store_counts.argtypes = [_P, _P, ctypes.c_int]
+    L.kd_store_export.argtypes = [_P, _P, _I64, _P, _I64, _P, ctypes.c_int]
+    L.kd_store_import.argtypes = [_P, _P, _I64, _P, _P, ctypes.c_int]
     L.kd_server_create.argtypes = [_P, _D, ctypes.c_size_t, ctypes.POINTER(_P)]
     L.kd_server_submit.argtypes = [_P, ctypes.c_int, _D, _P, _P, _I64, _P, ctypes.POINTER(_I64)]
     L.kd_server_advance.argtypes = [_P, _D]

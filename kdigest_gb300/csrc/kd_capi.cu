@@ -300,6 +300,10 @@ void kd_store_free(KdStore* st) {
                d.min_v, d.max_v, d.dfac};
   for (void* q : p)
     if (q) cudaFree(q);
+  d.slot_m = d.slot_w = d.prefix = nullptr;
+  d.cur = nullptr;
+  d.count = nullptr;
+  d.total = d.log_scale = d.clock = d.min_v = d.max_v = d.dfac = nullptr;
   if (st->sess) st->sess->mem_used -= std::min(st->sess->mem_used, st->bytes);
   st->bytes = 0;
 }
@@ -371,7 +375,17 @@ KD_API void kd_session_destroy(kd_session* h) {
   if (!h) return;
   KdSession* s = &h->s;
   cudaSetDevice(s->device);
+  // Servers and stores still alive lose their session: servers stop and drain,
+  // stores give back their device memory and become orphans (destroying them
+  // later only frees their host object).
+  for (kd_server* v : std::vector<kd_server*>(s->servers)) kd_server_orphan(v);
+  s->servers.clear();
   cudaStreamSynchronize(s->stream);
+  for (KdStore* st : s->stores) {
+    kd_store_free(st);
+    st->sess = nullptr;
+  }
+  s->stores.clear();
   if (s->scratch_store) {
     kd_store_free(s->scratch_store);
     delete s->scratch_store;
@@ -470,15 +484,19 @@ KD_API int kd_store_create(kd_session* h, int64_t num_keys, int scale, double co
     return rc;
   }
   *out = st;
+  s->stores.push_back(&st->st);
   return KD_OK;
 }
 
 KD_API void kd_store_destroy(kd_store* st) {
   if (!st) return;
   KdSession* s = st->st.sess;
-  cudaSetDevice(s->device);
-  cudaStreamSynchronize(s->stream);
-  kd_store_free(&st->st);
+  if (s) {  // an orphan (its session destroyed first) has no device memory left
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+    s->stores.erase(std::remove(s->stores.begin(), s->stores.end(), &st->st), s->stores.end());
+    kd_store_free(&st->st);
+  }
   delete st;
 }
 
@@ -501,6 +519,7 @@ KD_API int kd_store_ingest(kd_store* h, const uint32_t* keys, const double* valu
   if (!h) return KD_EINVAL;
   KdStore* st = &h->st;
   KdSession* s = st->sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
   if (n < 0 || (n > 0 && !values)) return fail(s, KD_EINVAL, "values must be non-null");
   if (clock_mode != KD_CLOCK_COUNT && clock_mode != KD_CLOCK_TIME) return fail(s, KD_EINVAL, "unknown clock mode");
   if (clock_mode == KD_CLOCK_TIME && !kd_isfinite(timestamp)) return fail(s, KD_EINVAL, "timestamp must be finite");
@@ -535,6 +554,7 @@ static int query_common(kd_store* h, const uint32_t* keys, const double* q, int6
   if (!h) return KD_EINVAL;
   KdStore* st = &h->st;
   KdSession* s = st->sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
   if (nq < 0 || (nq > 0 && (!q || !out))) return fail(s, KD_EINVAL, "null query arrays");
   if (nq == 0) return KD_OK;
   cudaSetDevice(s->device);
@@ -571,6 +591,7 @@ KD_API int kd_store_merge(kd_store* dst, kd_store* src, const int64_t* group_off
                           const uint32_t* parts, int64_t ngroups) {
   if (!dst || !src) return KD_EINVAL;
   KdSession* s = dst->st.sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
   if (src->st.sess != s) return fail(s, KD_EINVAL, "stores belong to different sessions");
   if (ngroups < 0 || (ngroups > 0 && (!group_offsets || !parts))) return fail(s, KD_EINVAL, "null group arrays");
   if (ngroups == 0) return KD_OK;
@@ -586,6 +607,7 @@ KD_API int kd_store_get_digest(kd_store* h, uint32_t key, double* header8, doubl
   if (!h) return KD_EINVAL;
   KdStore* st = &h->st;
   KdSession* s = st->sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
   const KdStoreDev& d = st->d;
   if ((long long)key >= d.K) return fail(s, KD_EINVAL, "key out of range [0, num_keys)");
   cudaSetDevice(s->device);
@@ -619,6 +641,7 @@ KD_API int kd_store_set_digest(kd_store* h, uint32_t key, const double* header8,
   if (!h || !header8) return KD_EINVAL;
   KdStore* st = &h->st;
   KdSession* s = st->sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
   KdStoreDev& d = st->d;
   if ((long long)key >= d.K) return fail(s, KD_EINVAL, "key out of range [0, num_keys)");
   if (count < 0 || count > KD_TILE) return fail(s, KD_ERANGE, "a digest holds at most 1024 centroids");
@@ -658,6 +681,7 @@ static double get_f64(const uint8_t* p) {
 KD_API int kd_store_to_bytes(kd_store* h, uint32_t key, uint8_t* buf, int64_t cap, int64_t* out_len) {
   if (!h) return KD_EINVAL;
   KdSession* s = h->st.sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
   double hdr[8];
   int64_t cnt = 0;
   int rc = kd_store_get_digest(h, key, hdr, nullptr, nullptr, 0, &cnt);
@@ -681,6 +705,7 @@ KD_API int kd_store_to_bytes(kd_store* h, uint32_t key, uint8_t* buf, int64_t ca
 KD_API int kd_store_from_bytes(kd_store* h, uint32_t key, const uint8_t* buf, int64_t len) {
   if (!h) return KD_EINVAL;
   KdSession* s = h->st.sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
   if (len <= 0 || !buf || buf[0] != 1) return fail(s, KD_EINVAL, "unrecognized digest serialization version");
   if (len < 65) return fail(s, KD_ERANGE, "truncated digest: not enough bytes for a Float64");
   double hdr[8];
@@ -700,6 +725,7 @@ KD_API int kd_store_stats(kd_store* h, int64_t* num_keys, int64_t* total_centroi
   if (!h) return KD_EINVAL;
   KdStore* st = &h->st;
   KdSession* s = st->sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
   cudaSetDevice(s->device);
   if (num_keys) *num_keys = st->d.K;
   if (device_bytes) *device_bytes = st->bytes;
@@ -718,6 +744,7 @@ KD_API int kd_store_counts(kd_store* h, int32_t* out, int flags) {
   if (!h || !out) return KD_EINVAL;
   KdStore* st = &h->st;
   KdSession* s = st->sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
   cudaSetDevice(s->device);
   KD_CK(cudaMemcpyAsync(out, st->d.count, (size_t)st->d.K * 4,
                         (flags & KD_PTR_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,

@@ -324,6 +324,7 @@ KD_API int kd_server_create(kd_store* store, double window_s, size_t budget_byte
     return rc;
   }
   v->worker = std::thread(worker_main, v);
+  s->servers.push_back(v);
   *out = v;
   return KD_OK;
 }
@@ -433,19 +434,38 @@ KD_API int kd_server_stats(kd_server* v, double* lat3, int64_t* completed, int64
   return KD_OK;
 }
 
-KD_API void kd_server_destroy(kd_server* v) {
-  if (!v) return;
+// Drains and stops the worker, then frees the device resources; the handle
+// stays valid for waits and stats.
+static void server_stop(kd_server* v) {
   {
     std::lock_guard<std::mutex> lk(v->mu);
     v->stop = true;  // remaining windows are processed before the worker exits
     v->cv.notify_all();
   }
   if (v->worker.joinable()) v->worker.join();
+  if (!v->s) return;
   cudaSetDevice(v->s->device);
   cudaStreamSynchronize(v->s->stream);
   for (Buf& b : v->buf) free_buf(b);
   if (v->copy_stream) cudaStreamDestroy(v->copy_stream);
+  v->copy_stream = nullptr;
+}
+
+KD_API void kd_server_destroy(kd_server* v) {
+  if (!v) return;
+  if (v->s) {  // an orphan was already stopped by its session's destruction
+    auto& list = v->s->servers;
+    list.erase(std::remove(list.begin(), list.end(), v), list.end());
+    server_stop(v);
+  }
   delete v;
 }
 
 }  // extern "C"
+
+void kd_server_orphan(kd_server* v) {
+  server_stop(v);
+  std::lock_guard<std::mutex> lk(v->mu);
+  v->s = nullptr;
+  v->st = nullptr;
+}

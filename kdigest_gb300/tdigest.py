@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import sys
 
 import numpy as np
 
@@ -117,7 +118,8 @@ class GpuSession:
 
     def __del__(self):
         try:
-            self.close()
+            if not sys.is_finalizing():  # process exit releases everything
+                self.close()
         except Exception:
             pass
 
@@ -170,7 +172,7 @@ class _Store:
 
     def __del__(self):
         try:
-            if getattr(self, "_h", None):
+            if getattr(self, "_h", None) and not sys.is_finalizing():
                 N.load().kd_store_destroy(self._h)
                 self._h = None
         except Exception:
@@ -469,6 +471,59 @@ class GroupedTDigest:
             return float(hdr[4] * math.exp(-hdr[2]))
         return float(hdr[4])
 
+    # -- checkpoint ------------------------------------------------------------
+    def export(self, keys=None):
+        """to_bytes of many keys at once: (records as one bytes buffer, int64
+        offsets with one entry more than keys)."""
+        k = None if keys is None else np.ascontiguousarray(keys, dtype=np.uint32)
+        nk = self.num_keys if k is None else len(k)
+        offs = np.zeros(nk + 1, dtype=np.int64)
+        L = N.load()
+        h = self._store._h
+        self._store._chk(L.kd_store_export(h, N.ptr(k), nk, None, 0, N.ptr(offs), 0))
+        buf = np.empty(int(offs[-1]), dtype=np.uint8)
+        self._store._chk(L.kd_store_export(h, N.ptr(k), nk, N.ptr(buf), len(buf), N.ptr(offs), 0))
+        return buf.tobytes(), offs
+
+    def import_records(self, data: bytes, offsets, keys=None):
+        """from_bytes of many keys; every record is validated before any key changes."""
+        buf = np.frombuffer(data, dtype=np.uint8)
+        offs = np.ascontiguousarray(offsets, dtype=np.int64)
+        k = None if keys is None else np.ascontiguousarray(keys, dtype=np.uint32)
+        nk = len(offs) - 1
+        self._store._chk(N.load().kd_store_import(self._store._h, N.ptr(k), nk, N.ptr(buf),
+                                                  N.ptr(offs), 0))
+
+    _SNAP_MAGIC = b"KDGB300S"
+
+    def snapshot(self, path: str):
+        """Write every key's record (the to_bytes wire format) with the store's
+        shape to a file."""
+        data, offs = self.export()
+        head = np.array([self.num_keys, self.scale], dtype=np.int64)
+        par = np.array([self.compression, self.decay.rate_lambda], dtype=np.float64)
+        with open(path, "wb") as f:
+            f.write(self._SNAP_MAGIC)
+            f.write(head.tobytes())
+            f.write(par.tobytes())
+            f.write(offs.tobytes())
+            f.write(data)
+
+    @classmethod
+    def restore(cls, path: str, session: GpuSession | None = None) -> "GroupedTDigest":
+        """A store rebuilt from a snapshot file."""
+        with open(path, "rb") as f:
+            if f.read(8) != cls._SNAP_MAGIC:
+                raise ValueError("not a grouped digest snapshot")
+            num_keys, scale = np.frombuffer(f.read(16), dtype=np.int64)
+            compression, lam = np.frombuffer(f.read(16), dtype=np.float64)
+            offs = np.frombuffer(f.read(8 * (int(num_keys) + 1)), dtype=np.int64)
+            data = f.read(int(offs[-1]))
+        g = cls(int(num_keys), float(compression), decay=Decay.rate(float(lam)), scale=int(scale),
+                session=session)
+        g.import_records(data, offs)
+        return g
+
     def merge_groups(self, src: "GroupedTDigest", group_offsets, parts):
         """Batched merge_into: key g of this store becomes the P-path merge of
         src keys parts[group_offsets[g]:group_offsets[g+1]] (in order)."""
@@ -550,6 +605,7 @@ class Server:
 
     def __del__(self):
         try:
-            self.close()
+            if not sys.is_finalizing():  # process exit releases everything
+                self.close()
         except Exception:
             pass
