@@ -189,6 +189,27 @@ KD_API int kd_server_stats(kd_server* srv, double* lat3, int64_t* completed, int
                            double* busy_s);
 KD_API void kd_server_destroy(kd_server* srv);
 
+/* Key dictionary.  No counterpart in the reference: GroupedTDigest.add_batch
+ * takes dense ids in [0, num_keys) (grouped.mojo:60-63) and leaves the mapping
+ * from application keys to them to the caller.  A kd_keymap maps arbitrary
+ * 64-bit keys to dense ids on the device, ready to pass to kd_store_ingest with
+ * KD_PTR_DEVICE.  Ids are handed out in first-seen order across calls; within
+ * one call, the order among keys new to the map is unspecified.  Once given, an
+ * id never changes.  The key value UINT64_MAX is reserved (KD_EINVAL).  A map of
+ * `capacity` ids holds 12 bytes per slot, with at least 2 * capacity slots.
+ * kd_keymap_map inserts unknown keys; past capacity it returns KD_ENOMEM, and
+ * the keys that did get ids keep them.  kd_keymap_lookup inserts nothing and
+ * writes UINT32_MAX for unknown keys.  keys and ids are device pointers with
+ * KD_PTR_DEVICE in flags, else host pointers. */
+typedef struct kd_keymap kd_keymap;
+KD_API int kd_keymap_create(kd_session* s, int64_t capacity, kd_keymap** out);
+KD_API int kd_keymap_map(kd_keymap* m, const uint64_t* keys, int64_t n, uint32_t* ids, int flags);
+KD_API int kd_keymap_lookup(kd_keymap* m, const uint64_t* keys, int64_t n, uint32_t* ids,
+                            int flags);
+/* Number of ids handed out; -1 for a map whose session is gone. */
+KD_API int64_t kd_keymap_size(kd_keymap* m);
+KD_API void kd_keymap_destroy(kd_keymap* m);
+
 /* No counterpart in the reference.  kd_compress for callers that cannot call
  * cudaMalloc: a host program whose own pool owns all device memory (memory taken
  * behind its back is unaccounted and may not exist), or a latency-critical loop

@@ -32,6 +32,7 @@ EXPORTED = (
     "kd_server_create", "kd_server_submit", "kd_server_advance", "kd_server_wait",
     "kd_server_flush", "kd_server_stats", "kd_server_destroy",
     "kd_store_export", "kd_store_import",
+    "kd_keymap_create", "kd_keymap_map", "kd_keymap_lookup", "kd_keymap_size", "kd_keymap_destroy",
 )
 KD_REQ_INGEST, KD_REQ_QUANTILE, KD_REQ_CDF = 0, 1, 2
 
@@ -102,6 +103,12 @@ def load(path: str = LIB_PATH):
                                       ctypes.POINTER(_I64), _P, ctypes.c_char_p, ctypes.c_int]
     L.kd_store_stats.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                  ctypes.POINTER(ctypes.c_size_t)]
+    L.kd_keymap_create.argtypes = [_P, _I64, ctypes.POINTER(_P)]
+    L.kd_keymap_map.argtypes = [_P, _P, _I64, _P, ctypes.c_int]
+    L.kd_keymap_lookup.argtypes = [_P, _P, _I64, _P, ctypes.c_int]
+    L.kd_keymap_size.restype = _I64
+    L.kd_keymap_size.argtypes = [_P]
+    L.kd_keymap_destroy.argtypes = [_P]
     _lib = L
     return L
 

@@ -381,6 +381,8 @@ KD_API void kd_session_destroy(kd_session* h) {
   for (kd_server* v : std::vector<kd_server*>(s->servers)) kd_server_orphan(v);
   s->servers.clear();
   cudaStreamSynchronize(s->stream);
+  for (kd_keymap* m : s->keymaps) kd_keymap_orphan(m);
+  s->keymaps.clear();
   for (KdStore* st : s->stores) {
     kd_store_free(st);
     st->sess = nullptr;

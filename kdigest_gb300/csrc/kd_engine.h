@@ -173,11 +173,16 @@ struct KdSession {
   struct KdStore* scratch_store = nullptr;  // 1-key store for stateless compress
   std::vector<struct KdStore*> stores;         // live stores of this session
   std::vector<struct kd_server*> servers;      // live serving loops over them
+  std::vector<struct kd_keymap*> keymaps;      // live key dictionaries
 };
 
 // Stops a server whose session is being destroyed (drains it, joins its
 // worker, frees its buffers); kd_server_destroy then only frees the handle.
 void kd_server_orphan(struct kd_server* v);
+
+// Frees the device tables of a key dictionary whose session is being
+// destroyed; kd_keymap_destroy then only frees the handle.
+void kd_keymap_orphan(struct kd_keymap* m);
 
 // What a captured ingest step depends on besides the per-call block: launch
 // shapes, kernel arguments that are baked in, and the buffers.

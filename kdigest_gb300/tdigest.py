@@ -530,6 +530,66 @@ class GroupedTDigest:
         self._store.merge_from(src._store, group_offsets, parts)
 
 
+class KeyDictionary:
+    """Device-resident map from arbitrary 64-bit keys to dense ids [0, capacity)
+    (no reference counterpart: GroupedTDigest.add_batch takes dense ids,
+    grouped.mojo:60-63).  Ids are stable once given; keys first seen in the
+    same call get theirs in an unspecified order.  2**64 - 1 is reserved.
+
+    ``map`` / ``lookup`` take a host array (returning a numpy uint32 array) or a
+    CUDA tensor with ``data_ptr()`` (returning a CUDA int32 tensor of the ids'
+    bit patterns, ready for a device-pointer ingest)."""
+
+    def __init__(self, capacity: int, session: GpuSession | None = None):
+        self.session = session or default_session()
+        self.capacity = int(capacity)
+        h = ctypes.c_void_p()
+        rc = N.load().kd_keymap_create(self.session.handle, self.capacity, ctypes.byref(h))
+        _check(self.session.handle, rc)
+        self._h = h.value
+
+    def _run(self, fn, keys):
+        if hasattr(keys, "data_ptr") and getattr(keys, "is_cuda", False):
+            import torch
+
+            k = keys.contiguous()
+            if k.element_size() != 8:
+                raise ValueError("device keys must be a 64-bit integer tensor")
+            out = torch.empty(k.numel(), dtype=torch.int32, device=k.device)
+            torch.cuda.current_stream(k.device).synchronize()
+            rc = fn(self._h, k.data_ptr(), k.numel(), out.data_ptr(), N.KD_PTR_DEVICE)
+            _check(self.session.handle, rc)
+            return out
+        k = np.ascontiguousarray(np.asarray(keys).astype(np.uint64, copy=False))
+        out = np.empty(len(k), np.uint32)
+        rc = fn(self._h, N.ptr(k), len(k), N.ptr(out), 0)
+        _check(self.session.handle, rc)
+        return out
+
+    def map(self, keys):
+        """Ids of keys, inserting unknown keys (KdError when the map is full)."""
+        return self._run(N.load().kd_keymap_map, keys)
+
+    def lookup(self, keys):
+        """Ids of keys; unknown keys give 2**32 - 1 (-1 in a device tensor)."""
+        return self._run(N.load().kd_keymap_lookup, keys)
+
+    def __len__(self) -> int:
+        return int(N.load().kd_keymap_size(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().kd_keymap_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            if not sys.is_finalizing():  # process exit releases everything
+                self.close()
+        except Exception:
+            pass
+
+
 class Server:
     """Serving loop over a resident digest store (no reference counterpart):
     requests with non-decreasing timestamps are batched per window of the
