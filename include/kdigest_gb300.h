@@ -106,6 +106,26 @@ KD_API void kd_store_destroy(kd_store* st);
 KD_API int kd_store_ingest(kd_store* st, const uint32_t* keys, const double* values, int64_t n,
                            int clock_mode, double timestamp, int flags);
 
+/* The single-sample path of a one-key store (TDigest.add / add_at,
+ * tdigest.mojo:153-175, 324-458): the reference's add loop over n samples in
+ * order, which is also what TDigest.add_batch runs below its GPU crossover
+ * (tdigest.mojo:177-221).  Each sample advances the clock by one (timestamps =
+ * NULL) or to its timestamp when later (add_at), is buffered with weight *
+ * e^{log_scale} (weights = NULL: 1.0), and a full buffer (5 * int(compression)
+ * samples) runs the sequential merge pass.  As in the loop, samples before the
+ * first invalid one (non-finite value, weight <= 0 or non-finite) stay applied
+ * and the call returns KD_EINVAL.  quantile, cdf, to_bytes and export merge the
+ * buffer first (tdigest.mojo:493, 542, 639); kd_store_ingest folds it into its
+ * batch (tdigest.mojo:262-268).  Pointers are host or device (flags). */
+KD_API int kd_store_add(kd_store* st, const double* values, const double* weights,
+                        const double* timestamps, int64_t n, int flags);
+/* TDigest.merge (tdigest.mojo:391-439): merges the buffered samples, if any. */
+KD_API int kd_store_flush(kd_store* st);
+/* TDigest.merge_into (tdigest.mojo:589-623) of two one-key stores: src is
+ * merged and (with decay) renormalised in place, then its centroids join dst's
+ * merge pass. */
+KD_API int kd_store_merge_into(kd_store* dst, kd_store* src);
+
 /* TDigest.quantile / cdf per (key, q|x) (tdigest.mojo:485-587); keys may be
  * NULL (all key 0).  Errors fill NaN and return the first failing status. */
 KD_API int kd_store_quantile(kd_store* st, const uint32_t* keys, const double* qs, int64_t nq,

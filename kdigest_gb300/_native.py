@@ -33,6 +33,7 @@ EXPORTED = (
     "kd_server_flush", "kd_server_stats", "kd_server_destroy",
     "kd_store_export", "kd_store_import",
     "kd_keymap_create", "kd_keymap_map", "kd_keymap_lookup", "kd_keymap_size", "kd_keymap_destroy",
+    "kd_store_add", "kd_store_flush", "kd_store_merge_into",
 )
 KD_REQ_INGEST, KD_REQ_QUANTILE, KD_REQ_CDF = 0, 1, 2
 
@@ -103,6 +104,9 @@ def load(path: str = LIB_PATH):
                                       ctypes.POINTER(_I64), _P, ctypes.c_char_p, ctypes.c_int]
     L.kd_store_stats.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                  ctypes.POINTER(ctypes.c_size_t)]
+    L.kd_store_add.argtypes = [_P, _P, _P, _P, _I64, ctypes.c_int]
+    L.kd_store_flush.argtypes = [_P]
+    L.kd_store_merge_into.argtypes = [_P, _P]
     L.kd_keymap_create.argtypes = [_P, _I64, ctypes.POINTER(_P)]
     L.kd_keymap_map.argtypes = [_P, _P, _I64, _P, ctypes.c_int]
     L.kd_keymap_lookup.argtypes = [_P, _P, _I64, _P, ctypes.c_int]

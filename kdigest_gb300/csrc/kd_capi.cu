@@ -295,6 +295,9 @@ void kd_store_drop_graphs(KdStore* st) {
 
 void kd_store_free(KdStore* st) {
   kd_store_drop_graphs(st);
+  kd_spath_free(st->sess, st);
+  st->pending = false;
+  st->carry = false;
   KdStoreDev& d = st->d;
   void* p[] = {d.slot_m, d.slot_w, d.prefix, d.cur, d.count, d.total, d.log_scale, d.clock,
                d.min_v, d.max_v, d.dfac};
@@ -546,9 +549,10 @@ KD_API int kd_store_ingest(kd_store* h, const uint32_t* keys, const double* valu
     KD_CK(cudaMemcpyAsync(base + kb, values, (size_t)n * 8, cudaMemcpyHostToDevice, s->stream));
     dv = (const double*)(base + kb);
   }
-  return kd_pipeline_ingest(s, st, dk, dv, nullptr, n,
-                            clock_mode == KD_CLOCK_TIME ? KD_MODE_TIME : KD_MODE_COUNT, timestamp,
-                            nullptr, nullptr, nullptr);
+  const int mode = clock_mode == KD_CLOCK_TIME ? KD_MODE_TIME : KD_MODE_COUNT;
+  if (st->carry && st->d.K == 1)  // the digest came from the single-sample path
+    return kd_spath_carry_ingest(s, st, dv, n, mode, timestamp);
+  return kd_pipeline_ingest(s, st, dk, dv, nullptr, n, mode, timestamp, nullptr, nullptr, nullptr);
 }
 
 static int query_common(kd_store* h, const uint32_t* keys, const double* q, int64_t nq,
@@ -560,6 +564,8 @@ static int query_common(kd_store* h, const uint32_t* keys, const double* q, int6
   if (nq < 0 || (nq > 0 && (!q || !out))) return fail(s, KD_EINVAL, "null query arrays");
   if (nq == 0) return KD_OK;
   cudaSetDevice(s->device);
+  int frc = kd_spath_flush(s, st);  // quantile / cdf run merge() first (tdigest.mojo:493,542)
+  if (frc) return frc;
   if (flags & KD_PTR_DEVICE) return kd_pipeline_quantile(s, st, keys, q, nq, out, is_cdf);
   size_t kb = keys ? ((size_t)nq * 4 + 15) / 16 * 16 : 0;
   int rc = stage_in(s, kb + (size_t)nq * 16);
@@ -601,7 +607,12 @@ KD_API int kd_store_merge(kd_store* dst, kd_store* src, const int64_t* group_off
   for (int64_t g = 0; g < ngroups; ++g)
     if (group_offsets[g + 1] < group_offsets[g]) return fail(s, KD_EINVAL, "group_offsets must be non-decreasing");
   cudaSetDevice(s->device);
-  return kd_pipeline_merge(s, &dst->st, &src->st, (const long long*)group_offsets, parts, ngroups);
+  int rc = kd_pipeline_merge(s, &dst->st, &src->st, (const long long*)group_offsets, parts, ngroups);
+  if (rc == KD_OK) {  // every destination digest was replaced (its buffer cleared)
+    dst->st.pending = false;
+    dst->st.carry = false;
+  }
+  return rc;
 }
 
 KD_API int kd_store_get_digest(kd_store* h, uint32_t key, double* header8, double* means,
@@ -666,7 +677,12 @@ KD_API int kd_store_set_digest(kd_store* h, uint32_t key, const double* header8,
   KD_CK(cudaMemcpy(d.max_v + key, &header8[6], 8, cudaMemcpyHostToDevice));
   k_fix_key<<<1, 1, 0, s->stream>>>(d, key);
   KD_CK(cudaGetLastError());
+  if (d.bcount) KD_CK(cudaMemsetAsync(d.bcount + key, 0, 4, s->stream));  // a new digest has no buffer
   KD_CK(cudaStreamSynchronize(s->stream));
+  if (d.K == 1) {  // centroids in any order: the next batch sorts them with its samples
+    st->pending = false;
+    st->carry = true;
+  }
   return KD_OK;
 }
 
@@ -684,9 +700,12 @@ KD_API int kd_store_to_bytes(kd_store* h, uint32_t key, uint8_t* buf, int64_t ca
   if (!h) return KD_EINVAL;
   KdSession* s = h->st.sess;
   if (!s) return KD_EINVAL;  // the store's session was destroyed
+  cudaSetDevice(s->device);
+  int rc = kd_spath_flush(s, &h->st);  // to_bytes runs merge() first (tdigest.mojo:639)
+  if (rc) return rc;
   double hdr[8];
   int64_t cnt = 0;
-  int rc = kd_store_get_digest(h, key, hdr, nullptr, nullptr, 0, &cnt);
+  rc = kd_store_get_digest(h, key, hdr, nullptr, nullptr, 0, &cnt);
   if (rc) return rc;
   const int64_t need = 1 + 8 * 8 + 16 * cnt;
   if (out_len) *out_len = need;

@@ -29,6 +29,13 @@ struct KdStoreDev {
   double* min_v;        // [K]
   double* max_v;        // [K]
   double* dfac;         // [K] e^{-log_scale} (singleton test of queries)
+  // Single-sample path (TDigest.add / add_at): samples wait in a per-key buffer
+  // of buf_cap entries until it fills and the sequential merge pass runs.
+  // Null until a store first takes that path.
+  int* bcount;          // [K] buffered samples
+  double* buf_m;        // [K][buf_cap] their values
+  double* buf_w;        // [K][buf_cap] their stored (decay-scaled) weights
+  int buf_cap;          // 5 * int(compression), at least 1
 };
 
 struct KdErrHost {
@@ -49,6 +56,11 @@ struct KdCallArgs {
   const double* merge_max;
   const double* merge_clock;
   double timestamp;
+  // A batch of a one-key store whose digest came from the single-sample path:
+  // the first `carry` inputs are its centroids and buffered samples (with their
+  // stored weights in wts), the rest are the batch's unit-weight samples.
+  long long carry;
+  const unsigned long long* carry_mm;  // order keys of the batch's min and max
   KdErrHost err;  // the step's status word (device copy: KdWorkspace::err)
 };
 
@@ -220,6 +232,13 @@ struct KdStore {
   KdGraphEntry graphs[KD_GRAPH_CACHE];
   int graph_next = 0;
   KdGraphKey last_eager;
+  // Single-sample path state (one-key stores).  `pending`: samples wait in the
+  // buffer.  `carry`: the next batch must carry the centroids and buffer in
+  // its input (their order is the sequential pass's, not the batch path's).
+  bool pending = false;
+  bool carry = false;
+  void* sp_scratch = nullptr;  // working memory of the pass when shared memory is too small
+  size_t sp_scratch_bytes = 0;
 };
 
 // The opaque handles of the C-ABI.
@@ -237,7 +256,16 @@ enum KdIngestMode { KD_MODE_COUNT = 0, KD_MODE_TIME = 1, KD_MODE_REPLACE = 2, KD
 int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const double* d_vals,
                        const double* d_wts, long long n, int mode, double timestamp,
                        const double* d_merge_min, const double* d_merge_max,
-                       const double* d_merge_clock);
+                       const double* d_merge_clock, long long carry = 0,
+                       const unsigned long long* d_carry_mm = nullptr);
+// Single-sample path (kd_spath.cu).  Merges the buffered samples of a one-key
+// store (TDigest.merge, tdigest.mojo:391-439) when any wait; a no-op otherwise.
+int kd_spath_flush(KdSession* s, KdStore* st);
+// A batch into a one-key store with `carry` set: the centroids and buffer go
+// into the batch's input ahead of its samples.
+int kd_spath_carry_ingest(KdSession* s, KdStore* st, const double* d_vals, long long n, int mode,
+                          double timestamp);
+void kd_spath_free(KdSession* s, KdStore* st);
 int kd_pipeline_quantile(KdSession* s, KdStore* st, const uint32_t* d_keys, const double* d_q,
                          long long nq, double* d_out, int is_cdf);
 int kd_pipeline_merge(KdSession* s, KdStore* dst, KdStore* src, const long long* h_group_off,
@@ -261,4 +289,5 @@ int kd_pipeline_prepare_device(KdSession* s);
 int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_t* d_keys,
                         const double* d_vals, const double* d_wts, long long n, int mode,
                         double timestamp, const double* d_merge_min, const double* d_merge_max,
-                        const double* d_merge_clock);
+                        const double* d_merge_clock, long long carry = 0,
+                        const unsigned long long* d_carry_mm = nullptr);

@@ -770,7 +770,7 @@ __global__ void k_prep(long long n, const KdCallArgs* __restrict__ call, long lo
     const uint32_t key = keys ? keys[i] : 0u;
     const double v = vals[i];
     bool bad = (long long)key >= K || !kd_isfinite(v);
-    if (wts) {
+    if (wts && call->carry == 0) {  // carried weights come from the store itself
       const double w = wts[i];
       bad = bad || !(w > 0.0) || !kd_isfinite(w);
     }
@@ -926,8 +926,13 @@ __global__ void k_prepare(PrepareArgs a) {
   double mn = s.min_v[key], mx = s.max_v[key];
   double pscale = 1.0;
   double sf = 1.0;
-  const double vmin = kd_from_order_key(a.k64[start]);
-  const double vmax = kd_from_order_key(a.k64[end - 1]);
+  const long long carry = a.call->carry;
+  // A carried batch (one-key store): its centroids and buffered samples lead
+  // the input; only the rest are the batch's samples.
+  const int nb = nn - (int)carry;
+  const double vmin = kd_from_order_key(carry ? a.call->carry_mm[0] : a.k64[start]);
+  const double vmax = kd_from_order_key(carry ? a.call->carry_mm[1] : a.k64[end - 1]);
+  if (carry) prior = 0;
   if (a.mode == KD_MODE_REPLACE || a.mode == KD_MODE_MERGE) {
     prior = 0;
     ls = 0.0;
@@ -945,7 +950,7 @@ __global__ void k_prepare(PrepareArgs a) {
     double new_clock = clock;
     bool advance = false;
     if (a.mode == KD_MODE_COUNT) {
-      new_clock = KD_ADD(clock, (double)nn);
+      new_clock = KD_ADD(clock, (double)nb);
       advance = true;
     } else if (a.call->timestamp > clock) {
       new_clock = a.call->timestamp;
@@ -963,7 +968,7 @@ __global__ void k_prepare(PrepareArgs a) {
       clock = new_clock;
     }
     sf = decay ? kd_exp(ls) : 1.0;
-    const double added = KD_MUL((double)nn, sf);
+    const double added = KD_MUL((double)nb, sf);
     total = KD_ADD(total, added);
     if (total == added && prior == 0) {
       mn = vmin;
@@ -1120,6 +1125,19 @@ struct TileArgs {
 // priors first on equal values (gpu/sort.mojo:38-41).  A merge-path binary
 // search finds where the range starts, then the range is merged in order;
 // put(q, value, weight) receives every element.
+// Weight of the sample at input position i: its own weight, or the key's decay
+// weight sf.  In a carried batch the leading `carry` inputs are the digest's
+// centroids and buffered samples, whose stored weights take the
+// renormalisation factor like any prior centroid (tdigest.mojo:359-371); the
+// batch's own samples take sf.
+__device__ __forceinline__ double sample_weight(const double* wts, uint32_t i, long long carry,
+                                                double sf, double pscale) {
+  if (!wts) return sf;
+  if (!carry) return wts[i];
+  if ((long long)i >= carry) return sf;
+  return pscale != 1.0 ? KD_MUL(wts[i], pscale) : wts[i];
+}
+
 template <class Put>
 __device__ __forceinline__ void merge_load(const TileArgs& a, int j, int d0, int q0, int q1, Put put) {
   if (q0 >= q1) return;
@@ -1151,7 +1169,7 @@ __device__ __forceinline__ void merge_load(const TileArgs& a, int j, int d0, int
       put(q, kd_from_order_key(kd_order_key(pm[ia])), rescale ? KD_MUL(pw[ia], pscale) : pw[ia]);
       ++ia;
     } else {
-      put(q, kd_from_order_key(nk[ib]), wts ? wts[sidx[ib]] : sf);
+      put(q, kd_from_order_key(nk[ib]), sample_weight(wts, sidx[ib], a.call->carry, sf, pscale));
       ++ib;
     }
   }
@@ -1262,7 +1280,7 @@ __global__ void __launch_bounds__(32 * (CAP == KD_TILE ? 1 : 4)) k_tiles(TileArg
           if (pk[mid] <= v) lo = mid + 1;
           else hi = mid;
         }
-        const double wv = wts ? wts[a.sidx[s0 + i]] : sf;
+        const double wv = sample_weight(wts, a.sidx ? a.sidx[s0 + i] : 0u, a.call->carry, sf, pscale);
         const int slot = tile_slot(i + lo, E, SE, inv);
         t.x[slot] = kd_from_order_key(v);
         t.w[slot] = wv;
@@ -1550,6 +1568,7 @@ __global__ void k_commit(CommitArgs a) {
   s.min_v[key] = a.st_min[j];
   s.max_v[key] = a.st_max[j];
   s.dfac[key] = s.lambda > 0.0 ? kd_exp(-ls) : 1.0;
+  if (s.bcount) s.bcount[key] = 0;  // a carried batch consumed the buffer
   s.cur[key] = (unsigned char)b;
 }
 
@@ -1988,7 +2007,8 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
 int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_t* d_keys,
                         const double* d_vals, const double* d_wts, long long n, int mode,
                         double timestamp, const double* d_merge_min, const double* d_merge_max,
-                        const double* d_merge_clock) {
+                        const double* d_merge_clock, long long carry,
+                        const unsigned long long* d_carry_mm) {
   cudaStream_t str = s->stream;
   const KdStoreDev sd = st->d;
   const long long keys_max = std::min<long long>(n, sd.K);
@@ -2008,6 +2028,8 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
   c.merge_max = d_merge_max;
   c.merge_clock = d_merge_clock;
   c.timestamp = timestamp;
+  c.carry = carry;
+  c.carry_mm = d_carry_mm;
   c.err = KdErrHost{0, 0, 0x7fffffffffffffffLL};
   KdSortBufs sb = sort_bufs(w);
   kd_rs_epoch_reserve(sb, str);
@@ -2119,7 +2141,8 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
 int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const double* d_vals,
                        const double* d_wts, long long n, int mode, double timestamp,
                        const double* d_merge_min, const double* d_merge_max,
-                       const double* d_merge_clock) {
+                       const double* d_merge_clock, long long carry,
+                       const unsigned long long* d_carry_mm) {
   if (n <= 0) return KD_OK;
   if (n > (1LL << 31) - 1) {
     kd_set_msg(s, "batch too large (limit 2^31 - 1 samples per call)");
@@ -2137,7 +2160,7 @@ int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const 
                        std::max(want_work, w0.cap_work), std::max(want_merged, w0.cap_merged), st->d.K);
     if (rc) return rc;
     rc = kd_pipeline_attempt(s, st, s->ws, d_keys, d_vals, d_wts, n, mode, timestamp, d_merge_min,
-                             d_merge_max, d_merge_clock);
+                             d_merge_max, d_merge_clock, carry, d_carry_mm);
     if (rc != KD_ERANGE_SCRATCH) return rc;
     const int* need = s->ws.h_scalars;
     want_work = std::max<long long>(want_work, (long long)need[0] + need[0] / 4 + 64);

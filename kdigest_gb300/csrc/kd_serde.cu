@@ -123,6 +123,7 @@ __global__ void k_import(KdStoreDev s, const uint32_t* keys, long long key0, lon
     __syncwarp();
     if (lane == 0) {
       s.count[key] = cnt;
+      if (s.bcount) s.bcount[key] = 0;  // an installed digest has no buffered samples
       s.log_scale[key] = get_f64_dev(rec + 17);
       s.clock[key] = get_f64_dev(rec + 25);
       s.total[key] = get_f64_dev(rec + 33);
@@ -173,6 +174,15 @@ long long chunk_end(const int64_t* off, long long i0, long long nkeys) {
     if (rc_) return rc_;                  \
   } while (0)
 
+// A one-key store whose digest was installed from records: the centroids may
+// come in any order, so the next batch sorts them together with its samples.
+static void imported(KdStore* st) {
+  if (st->d.K == 1) {
+    st->pending = false;
+    st->carry = true;
+  }
+}
+
 extern "C" {
 
 KD_API int kd_store_export(kd_store* h, const uint32_t* keys, int64_t nkeys, uint8_t* buf,
@@ -197,6 +207,10 @@ KD_API int kd_store_export(kd_store* h, const uint32_t* keys, int64_t nkeys, uin
   cudaStream_t str = s->stream;
   offsets[0] = 0;
   if (nkeys == 0) return KD_OK;
+  {
+    const int frc = kd_spath_flush(s, st);  // each record is to_bytes, which merges first
+    if (frc) return frc;
+  }
   DevBuf dkeys, dcnt, doff, dout;
   const uint32_t* kp = keys;
   if (keys && !dev) {
@@ -319,6 +333,7 @@ KD_API int kd_store_import(kd_store* h, const uint32_t* keys, int64_t nkeys, con
     k_import<<<g, 256, 0, str>>>(d, kp, 0, nkeys, buf, (const long long*)doff.p);
     KD_SCK(cudaGetLastError());
     KD_SCK(cudaStreamSynchronize(str));
+    imported(st);
     return KD_OK;
   }
   KD_SCK(cudaMalloc(&doff.p, (size_t)(nkeys + 1) * 8));
@@ -338,6 +353,7 @@ KD_API int kd_store_import(kd_store* h, const uint32_t* keys, int64_t nkeys, con
     KD_SCK(cudaStreamSynchronize(str));
     i0 = i1;
   }
+  imported(st);
   return KD_OK;
 }
 

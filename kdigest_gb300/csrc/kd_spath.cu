@@ -1,0 +1,1125 @@
+// kd_spath.cu — the single-sample path of a one-key store on the device:
+// TDigest.add / add_at and the sequential merge pass they trigger
+// (src/kdigest/tdigest.mojo:153-175, 324-458), merge() before reads, and the
+// sequential merge_into (:589-623).
+//
+// The reference runs batches below its GPU crossover through this path
+// (tdigest.mojo:177-221), so a one-key store reproduces it exactly: samples
+// wait in a buffer of 5 * int(compression) entries, and a full buffer runs the
+// merge pass — a stable sort of centroids ++ buffer by mean, then a greedy
+// left-to-right sweep that grows a cluster while k(q_right) - k(q_left) <= 1
+// or the candidate's mean equals the cluster's running mean.
+//
+// One CTA runs a whole call; its state lives in shared memory (or in a global
+// scratch block when the buffer is too large for it).  The sweep is sequential
+// in the reference, and parallel here without changing a bit:
+//   * with integral weights every q the sweep forms is an exact prefix sum over
+//     the stored total, so k is evaluated for every position in parallel;
+//   * one warp follows the chain of cluster starts, 32 candidates per step;
+//   * one thread per cluster replays its running mean and weight in order;
+//   * with non-integral weights (decay) the chain is first speculated from
+//     plain prefix sums, then every decision is re-checked with the exact sums
+//     of the chain; a mismatch (or a candidate whose coalescing rests on an
+//     exact mean tie) sends the pass to a one-thread replay of the reference
+//     loop.
+// Every FP64 operation is the reference's, in its order, through the
+// correctly rounded intrinsics of kd_math.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+
+#include "../../include/kdigest_gb300.h"
+#include "kd_engine.h"
+#include "kd_internal.cuh"
+#include "kd_math.h"
+
+namespace {
+
+constexpr int SP_T = 1024;  // threads of the one CTA
+constexpr double SP_RENORM = 400.0;    // tdigest.mojo:43
+constexpr double SP_PRUNE_EPS = 1e-6;  // tdigest.mojo:47
+constexpr double SP_EXACT = 9007199254740992.0;  // 2^53
+
+enum { SP_ADD = 0, SP_FLUSH = 1, SP_MERGE_INTO = 2 };
+
+struct SpStatus {
+  int code;
+  int noop;
+  long long index;  // first rejected sample (KD_EINVAL)
+  int count;
+  int bcount;
+};
+
+struct SpArgs {
+  KdStoreDev s;      // the digest (key 0)
+  KdStoreDev o;      // merge_into: the other digest (key 0), already flushed
+  const double* vals;
+  const double* wts;  // per-sample weights, or null (1.0)
+  const double* ts;   // per-sample timestamps (add_at), or null (add)
+  long long n;
+  int op;
+  int bmax;  // buffer capacity inside the call: max(buf_cap, KD_TILE)
+  int wpb;   // power of two >= bmax (width of the buffer sort)
+  unsigned char* scratch;  // global working memory, or null (dynamic shared memory)
+  SpStatus* out;
+};
+
+struct SpMem {
+  double *cm, *cw;  // centroids [KD_TILE]
+  double *bm, *bw;  // buffer [bmax]
+  unsigned long long* okey;  // buffer sort keys [wpb]
+  unsigned* sidx;            // buffer sort positions [wpb]
+  double *sm, *sw;  // merged work [KD_TILE + bmax]
+  double* kk;       // k at every prefix [KD_TILE + bmax + 1]
+  double* rw;       // running cluster weight before each element [KD_TILE + bmax + 1]
+  int* cst;         // cluster starts [KD_TILE + 1]
+  int* cid;         // cluster of each element [KD_TILE + bmax]
+  double* sls;      // log-scale of each sample of a segment [bmax]
+  double *wsf, *kl;  // weight before each cluster and its k [KD_TILE + 1]
+};
+
+__host__ __device__ inline size_t sp_align(size_t b) { return (b + 255) & ~(size_t)255; }
+
+__host__ __device__ inline size_t sp_layout(int bmax, int wpb, unsigned char* base, SpMem* m) {
+  const size_t W = (size_t)KD_TILE + bmax;
+  size_t off = 0;
+  auto take = [&](size_t bytes) -> unsigned char* {
+    unsigned char* p = base ? base + off : nullptr;
+    off += sp_align(bytes);
+    return p;
+  };
+  SpMem t;
+  t.cm = (double*)take(8 * KD_TILE);
+  t.cw = (double*)take(8 * KD_TILE);
+  t.bm = (double*)take(8 * (size_t)bmax);
+  t.bw = (double*)take(8 * (size_t)bmax);
+  t.okey = (unsigned long long*)take(8 * (size_t)wpb);
+  t.sidx = (unsigned*)take(4 * (size_t)wpb);
+  t.sm = (double*)take(8 * W);
+  t.sw = (double*)take(8 * W);
+  t.kk = (double*)take(8 * (W + 1));
+  t.rw = (double*)take(8 * (W + 1));
+  t.cst = (int*)take(4 * (KD_TILE + 1));
+  t.cid = (int*)take(4 * W);
+  t.sls = (double*)take(8 * (size_t)bmax);
+  t.wsf = (double*)take(8 * (KD_TILE + 1));
+  t.kl = (double*)take(8 * (KD_TILE + 1));
+  if (m) *m = t;
+  return off;
+}
+
+// Scalars of the call, shared by the CTA.
+struct SpSh {
+  double st, ls, clock, mn, mx;
+  double factor, nrm, renorm_clock;
+  long long first_bad;
+  int C, B, err, nc, mismatch, unsorted, exact, cut, renorm, pre_adv, integral;
+};
+
+__device__ __forceinline__ double sp_k(int scale, double q, double nrm) { return kd_k(scale, q, nrm); }
+
+// Block-wide exclusive prefix of v[0..n) into out[0..n] (out[n] = total), in
+// any association order: used only where the sums are exact (integers below
+// 2^53) or a speculation that is re-checked exactly.
+__device__ void sp_prefix(const double* v, double* out, int n, double* tmp_warp) {
+  // per-thread chunk sums, then a serial scan of the 1024 chunk sums by warp 0
+  const int per = (n + SP_T - 1) / SP_T;
+  const int b = threadIdx.x * per, e = min(n, b + per);
+  double sum = 0.0;
+  for (int i = b; i < e; ++i) sum = KD_ADD(sum, v[i]);
+  tmp_warp[threadIdx.x] = sum;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    // warp scan over 1024 values: each lane owns 32 consecutive chunks
+    double* mine = tmp_warp + threadIdx.x * 32;
+    double acc = 0.0;
+    for (int i = 0; i < 32; ++i) acc = KD_ADD(acc, mine[i]);
+    double incl = acc;
+    for (int o = 1; o < 32; o <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)threadIdx.x >= o) incl = KD_ADD(incl, y);
+    }
+    double run = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (threadIdx.x == 0) run = 0.0;
+    for (int i = 0; i < 32; ++i) {  // chunk sums -> exclusive chunk offsets, in place
+      const double v = mine[i];
+      mine[i] = run;
+      run = KD_ADD(run, v);
+    }
+  }
+  __syncthreads();
+  double run = tmp_warp[threadIdx.x];
+  for (int i = b; i < e; ++i) {
+    out[i] = run;
+    run = KD_ADD(run, v[i]);
+  }
+  if (e == n && b < e) out[n] = run;
+  if (n == 0 && threadIdx.x == 0) out[0] = 0.0;
+  __syncthreads();
+}
+
+// Stable ascending sort of the buffer (bm[0..B)) by value: bitonic over
+// (order key, position), so equal values (and -0.0 / +0.0) keep their order.
+__device__ void sp_sort_buffer(const SpMem& m, int B, int wpb) {
+  int P = 1;
+  while (P < B) P <<= 1;
+  for (int i = threadIdx.x; i < P; i += SP_T) {
+    if (i < B) {
+      m.okey[i] = kd_order_key(m.bm[i]);
+      m.sidx[i] = (unsigned)i;
+    } else {
+      m.okey[i] = ~0ull;
+      m.sidx[i] = 0xffffffffu;
+    }
+  }
+  __syncthreads();
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < P; i += SP_T) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const unsigned long long a = m.okey[i], b = m.okey[ixj];
+          const unsigned ia = m.sidx[i], ib = m.sidx[ixj];
+          const bool gt = a > b || (a == b && ia > ib);
+          if (gt == ((i & k) == 0)) {
+            m.okey[i] = b;
+            m.okey[ixj] = a;
+            m.sidx[i] = ib;
+            m.sidx[ixj] = ia;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// The merge pass (tdigest.mojo:391-439, _prune :441-458) over C centroids and
+// B buffered samples in shared state.  Leaves the new centroids in cm/cw.
+__device__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh) {
+  const int B = sh.B, C = sh.C;
+  if (B == 0) return;
+  const int scale = a.s.scale;
+  const bool decay = a.s.lambda > 0.0;
+  // 1. work = centroids ++ buffer, stably sorted by mean
+  sp_sort_buffer(m, B, a.wpb);
+  if (threadIdx.x == 0) sh.unsorted = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i + 1 < C; i += SP_T)
+    if (m.cm[i] > m.cm[i + 1]) sh.unsorted = 1;
+  __syncthreads();
+  if (sh.unsorted && threadIdx.x == 0) {  // stable insertion sort (tdigest.mojo:64-77)
+    for (int i = 1; i < C; ++i) {
+      const double km = m.cm[i], kw = m.cw[i];
+      int j = i - 1;
+      while (j >= 0 && m.cm[j] > km) {
+        m.cm[j + 1] = m.cm[j];
+        m.cw[j + 1] = m.cw[j];
+        --j;
+      }
+      m.cm[j + 1] = km;
+      m.cw[j + 1] = kw;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < C; i += SP_T) {  // centroids precede equal buffered values
+    const unsigned long long v = kd_order_key(m.cm[i]);
+    int lo = 0, hi = B;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (m.okey[mid] < v) lo = mid + 1;
+      else hi = mid;
+    }
+    m.sm[i + lo] = m.cm[i];
+    m.sw[i + lo] = m.cw[i];
+  }
+  for (int j = threadIdx.x; j < B; j += SP_T) {
+    const unsigned long long v = m.okey[j];
+    int lo = 0, hi = C;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (kd_order_key(m.cm[mid]) <= v) lo = mid + 1;
+      else hi = mid;
+    }
+    m.sm[j + lo] = m.bm[m.sidx[j]];
+    m.sw[j + lo] = m.bw[m.sidx[j]];
+  }
+  const int W = C + B;
+  // 2. totals: k limits use the effective total, q positions the stored one
+  if (threadIdx.x == 0) {
+    const double eff = decay ? KD_MUL(sh.st, kd_exp(-sh.ls)) : sh.st;
+    sh.nrm = kd_normalizer(scale, a.s.compression, eff);
+    sh.B = 0;
+    sh.exact = 1;
+    sh.mismatch = 0;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < W; i += SP_T) {
+    const double w = m.sw[i];
+    if (!(w == floor(w)) || w > SP_EXACT) sh.exact = 0;
+  }
+  __syncthreads();
+  const double st = sh.st, nrm = sh.nrm;
+  // 3. k at every prefix: exact q for integral weights, a speculation otherwise
+  sp_prefix(m.sw, m.rw, W, m.wsf);  // rw doubles as the prefix array here
+  if (threadIdx.x == 0 && sh.exact && !(m.rw[W] <= SP_EXACT)) sh.exact = 0;
+  for (int i = threadIdx.x; i <= W; i += SP_T) m.kk[i] = sp_k(scale, KD_DIV(m.rw[i], st), nrm);
+  __syncthreads();
+  // 4. the chain of cluster starts (warp 0)
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    int s = 0, nc = 0;
+    bool overflow = false;
+    while (s < W) {
+      if (nc >= KD_TILE) {
+        overflow = true;
+        break;
+      }
+      if (lane == 0) m.cst[nc] = s;
+      ++nc;
+      const double ks = m.kk[s], ms = m.sm[s];
+      int b = W;
+      for (int j0 = s + 1; j0 < W; j0 += 32) {
+        const int j = j0 + lane;
+        bool split = false;
+        if (j < W) split = !(KD_SUB(m.kk[j + 1], ks) <= 1.0 || m.sm[j] == ms);
+        const unsigned bal = __ballot_sync(0xffffffffu, split);
+        if (bal) {
+          b = j0 + __ffs(bal) - 1;
+          break;
+        }
+      }
+      s = b;
+    }
+    if (lane == 0) {
+      m.cst[overflow ? KD_TILE : nc] = W;
+      sh.nc = overflow ? -1 : nc;
+    }
+  }
+  __syncthreads();
+  int nc = sh.nc;
+  if (nc < 0) {
+    if (threadIdx.x == 0) sh.err = KD_ERANGE;
+    __syncthreads();
+    return;
+  }
+  // 5. one thread per cluster: the running mean and weight, in order
+  //    (Centroid.add_sample, centroid.mojo:25-36)
+  const double* sm = m.sm;
+  const double* sw = m.sw;
+  for (int t = threadIdx.x; t < nc; t += SP_T) {
+    const int s = m.cst[t], e = m.cst[t + 1];
+    double cur_m = sm[s], cur_w = sw[s];
+    m.cid[s] = t;
+    for (int j = s + 1; j < e; ++j) {
+      m.rw[j] = cur_w;
+      const double nw = KD_ADD(cur_w, sw[j]);
+      cur_m = KD_ADD(cur_m, KD_MUL(KD_SUB(sm[j], cur_m), KD_DIV(sw[j], nw)));
+      cur_w = nw;
+      m.cid[j] = t;
+    }
+    if (e < W) {
+      m.rw[e] = cur_w;
+      if (sm[e] == cur_m) sh.mismatch = 1;  // the reference coalesces an exact mean tie
+    }
+    m.cm[t] = cur_m;
+    m.cw[t] = cur_w;
+  }
+  __syncthreads();
+  // 6. non-integral weights: re-check every decision with the chain's exact sums
+  if (!sh.exact && !sh.mismatch) {
+    if (threadIdx.x == 0) {
+      double acc = 0.0;
+      for (int t = 0; t < nc; ++t) {
+        m.wsf[t] = acc;
+        acc = KD_ADD(acc, m.cw[t]);
+      }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc; t += SP_T) m.kl[t] = sp_k(scale, KD_DIV(m.wsf[t], st), nrm);
+    __syncthreads();
+    for (int j = 1 + threadIdx.x; j < W; j += SP_T) {
+      const int t = m.cid[j];
+      const bool start = m.cst[t] == j;
+      const int tt = start ? t - 1 : t;
+      const double qr = KD_DIV(KD_ADD(KD_ADD(m.wsf[tt], m.rw[j]), sw[j]), st);
+      const bool fits = KD_SUB(sp_k(scale, qr, nrm), m.kl[tt]) <= 1.0;
+      if (start) {
+        if (fits) sh.mismatch = 1;
+      } else if (!fits && !(sm[j] == sm[m.cst[tt]])) {
+        sh.mismatch = 1;
+      }
+    }
+    __syncthreads();
+  }
+  // 7. mismatch: the reference loop, one thread
+  if (sh.mismatch) {
+    if (threadIdx.x == 0) {
+      double wsf = 0.0, cur_m = sm[0], cur_w = sw[0];
+      double kq = sp_k(scale, KD_DIV(wsf, st), nrm);
+      int k = 0;
+      bool overflow = false;
+      for (int i = 1; i < W; ++i) {
+        const double qr = KD_DIV(KD_ADD(KD_ADD(wsf, cur_w), sw[i]), st);
+        const double span = KD_SUB(sp_k(scale, qr, nrm), kq);
+        if (sm[i] == cur_m || span <= 1.0) {
+          const double nw = KD_ADD(cur_w, sw[i]);
+          cur_m = KD_ADD(cur_m, KD_MUL(KD_SUB(sm[i], cur_m), KD_DIV(sw[i], nw)));
+          cur_w = nw;
+        } else {
+          if (k >= KD_TILE - 1) {
+            overflow = true;
+            break;
+          }
+          m.cm[k] = cur_m;
+          m.cw[k] = cur_w;
+          ++k;
+          wsf = KD_ADD(wsf, cur_w);
+          kq = sp_k(scale, KD_DIV(wsf, st), nrm);
+          cur_m = sm[i];
+          cur_w = sw[i];
+        }
+      }
+      m.cm[k] = cur_m;
+      m.cw[k] = cur_w;
+      sh.nc = k + 1;
+      if (overflow) sh.err = KD_ERANGE;
+    }
+    __syncthreads();
+    nc = sh.nc;
+  }
+  // 8. prune decayed mass (tdigest.mojo:441-458)
+  if (threadIdx.x == 0) {
+    int c = nc;
+    if (decay) {
+      const double floor_w = KD_MUL(SP_PRUNE_EPS, kd_exp(sh.ls));
+      int k = 0;
+      double removed = 0.0;
+      for (int i = 0; i < c; ++i) {
+        const double wi = m.cw[i];
+        if (wi >= floor_w) {
+          m.cm[k] = m.cm[i];
+          m.cw[k] = wi;
+          ++k;
+        } else {
+          removed = KD_ADD(removed, wi);
+        }
+      }
+      if (removed > 0.0) {
+        sh.st = KD_SUB(sh.st, removed);
+        c = k;
+      }
+    }
+    sh.C = c;
+  }
+  __syncthreads();
+}
+
+// Renormalise (tdigest.mojo:359-371): every stored weight and the total by
+// e^{-log_scale}; the exponent restarts at 0.
+__device__ void sp_renormalize(const SpMem& m, SpSh& sh) {
+  if (threadIdx.x == 0) sh.factor = kd_exp(-sh.ls);
+  __syncthreads();
+  const double f = sh.factor;
+  for (int i = threadIdx.x; i < sh.C; i += SP_T) m.cw[i] = KD_MUL(m.cw[i], f);
+  for (int i = threadIdx.x; i < sh.B; i += SP_T) m.bw[i] = KD_MUL(m.bw[i], f);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sh.st = KD_MUL(sh.st, f);
+    sh.ls = 0.0;
+  }
+  __syncthreads();
+}
+
+// Reduction that keeps the first occurrence among equal values (the reference
+// updates its running min / max only on a strict improvement).
+struct SpPick {
+  unsigned long long key;  // order key (equal values compare equal)
+  long long seq;
+  double v;
+};
+__device__ __forceinline__ SpPick sp_pick_min(SpPick a, SpPick b) {
+  if (b.key < a.key || (b.key == a.key && b.seq < a.seq)) return b;
+  return a;
+}
+__device__ __forceinline__ SpPick sp_pick_max(SpPick a, SpPick b) {
+  if (b.key > a.key || (b.key == a.key && b.seq < a.seq)) return b;
+  return a;
+}
+__device__ SpPick sp_shfl(SpPick p, int o) {
+  SpPick q;
+  q.key = __shfl_down_sync(0xffffffffu, p.key, o);
+  q.seq = __shfl_down_sync(0xffffffffu, p.seq, o);
+  q.v = __shfl_down_sync(0xffffffffu, p.v, o);
+  return q;
+}
+
+__device__ void sp_reduce_minmax(SpPick& mn, SpPick& mx, SpPick* red) {
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = sp_pick_min(mn, sp_shfl(mn, o));
+    mx = sp_pick_max(mx, sp_shfl(mx, o));
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    red[w] = mn;
+    red[32 + w] = mx;
+  }
+  __syncthreads();
+  if (w == 0) {
+    mn = red[lane];
+    mx = red[32 + lane];
+    for (int o = 16; o > 0; o >>= 1) {
+      mn = sp_pick_min(mn, sp_shfl(mn, o));
+      mx = sp_pick_max(mx, sp_shfl(mx, o));
+    }
+    if (lane == 0) {
+      red[0] = mn;
+      red[32] = mx;
+    }
+  }
+  __syncthreads();
+  mn = red[0];
+  mx = red[32];
+  __syncthreads();
+}
+
+// The add loop over samples [0, n_eff) (tdigest.mojo:153-175, 334-350): each
+// sample advances the clock, is buffered with its decay-scaled weight, and a
+// full buffer runs the merge pass.
+__device__ void sp_add(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_eff, SpPick* red,
+                       double* dred) {
+  const bool decay = a.s.lambda > 0.0;
+  const double lambda = a.s.lambda;
+  const int L = a.s.buf_cap;
+  long long i = 0;
+  while (i < n_eff && !sh.err) {
+    const long long room = (long long)(L - sh.B);
+    const int seg = (int)(n_eff - i < room ? n_eff - i : room);
+    const int B0 = sh.B;
+    // clock, decay exponent and renormalisation, in sample order
+    bool fast = false;
+    if (!decay) {
+      // Without decay the exponent never moves: the clock is the only chain.
+      // Count clock: integral clocks below 2^52 add exactly, so clock + seg is
+      // the sum of seg additions of 1.  Time clock: the latest timestamp wins,
+      // the earliest of equal ones (strict comparisons).
+      fast = a.ts != nullptr || (sh.clock == floor(sh.clock) && fabs(sh.clock) < 4.0e15);
+    }
+    __syncthreads();  // every thread has read the clock before it moves
+    if (fast) {
+      if (a.ts) {
+        SpPick mx{kd_order_key(sh.clock), -1, sh.clock}, dummy{0, 0, 0.0};
+        for (int k = threadIdx.x; k < seg; k += SP_T) {
+          const double t = a.ts[i + k];
+          if (t == t) mx = sp_pick_max(mx, SpPick{kd_order_key(t), (long long)k, t});
+        }
+        dummy = SpPick{~0ull, -1, 0.0};
+        sp_reduce_minmax(dummy, mx, red);
+        if (threadIdx.x == 0) {
+          // `timestamp > clock` advances; an equal later timestamp does not
+          if (mx.seq >= 0 && mx.v > sh.clock) sh.clock = mx.v;
+          sh.cut = seg;
+          sh.renorm = 0;
+        }
+      } else if (threadIdx.x == 0) {
+        sh.clock = KD_ADD(sh.clock, (double)seg);
+        sh.cut = seg;
+        sh.renorm = 0;
+      }
+      for (int k = threadIdx.x; k < seg; k += SP_T) m.sls[k] = sh.ls;
+    } else if (threadIdx.x == 0) {
+      int cut = 0;
+      sh.renorm = 0;
+      double clock = sh.clock, ls = sh.ls;
+      for (int k = 0; k < seg; ++k) {
+        const long long j = i + k;
+        bool adv;
+        double nc = clock;
+        if (sh.pre_adv && k == 0) {
+          adv = false;  // this sample's clock step ran before the renormalisation
+        } else if (a.ts) {
+          adv = a.ts[j] > clock;
+          nc = a.ts[j];
+        } else {
+          adv = true;
+          nc = KD_ADD(clock, 1.0);
+        }
+        if (adv) {
+          if (decay && nc > clock) {
+            ls = KD_ADD(ls, KD_MUL(lambda, KD_SUB(nc, clock)));
+            if (ls > SP_RENORM) {
+              sh.renorm = 1;
+              sh.renorm_clock = nc;
+              break;
+            }
+          }
+          clock = nc;
+        }
+        m.sls[k] = ls;
+        cut = k + 1;
+      }
+      sh.pre_adv = 0;
+      sh.clock = clock;
+      sh.ls = ls;
+      sh.cut = cut;
+    }
+    __syncthreads();
+    const int cut = sh.cut;
+    // buffer the samples with their scaled weights (weight * e^{log_scale})
+    for (int k = threadIdx.x; k < cut; k += SP_T) {
+      const double w = a.wts ? a.wts[i + k] : 1.0;
+      m.bm[B0 + k] = a.vals[i + k];
+      m.bw[B0 + k] = KD_MUL(w, decay ? kd_exp(m.sls[k]) : 1.0);
+    }
+    __syncthreads();
+    // running min / max (reset by the first sample of an empty digest) and the
+    // stored total, in sample order
+    if (cut > 0) {
+      const bool reset = sh.st == 0.0 && B0 == 0;
+      SpPick mn{~0ull, 0x7fffffffffffffffLL, 0.0}, mx{0ull, 0x7fffffffffffffffLL, 0.0};
+      if (!reset && threadIdx.x == 0) {
+        mn = SpPick{kd_order_key(sh.mn), -1, sh.mn};
+        mx = SpPick{kd_order_key(sh.mx), -1, sh.mx};
+      }
+      double part = 0.0;
+      for (int k = threadIdx.x; k < cut; k += SP_T) {
+        const double v = m.bm[B0 + k];
+        const SpPick p{kd_order_key(v), (long long)k, v};
+        mn = sp_pick_min(mn, p);
+        mx = sp_pick_max(mx, p);
+        part = KD_ADD(part, m.bw[B0 + k]);
+      }
+      sp_reduce_minmax(mn, mx, red);
+      // an exact total: integral weights and total below 2^53 sum in any order
+      bool exact = sh.st == floor(sh.st) && sh.integral && !decay;
+      for (int o = 16; o > 0; o >>= 1) part = KD_ADD(part, __shfl_down_sync(0xffffffffu, part, o));
+      if ((threadIdx.x & 31) == 0) dred[threadIdx.x >> 5] = part;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        sh.mn = mn.v;
+        sh.mx = mx.v;
+        double tot = sh.st;
+        if (exact) {
+          double sum = 0.0;
+          for (int t = 0; t < SP_T / 32; ++t) sum = KD_ADD(sum, dred[t]);
+          if (KD_ADD(tot, sum) <= SP_EXACT) tot = KD_ADD(tot, sum);
+          else exact = false;
+        }
+        if (!exact) {
+          tot = sh.st;
+          for (int k = 0; k < cut; ++k) tot = KD_ADD(tot, m.bw[B0 + k]);
+        }
+        sh.st = tot;
+        sh.B = B0 + cut;
+      }
+      __syncthreads();
+    }
+    i += cut;
+    if (sh.renorm) {
+      // The next sample's clock step took the exponent (now in sh.ls) past the
+      // threshold: renormalise, finish that step, then insert the sample.
+      sp_renormalize(m, sh);
+      if (threadIdx.x == 0) {
+        sh.clock = sh.renorm_clock;
+        sh.pre_adv = 1;
+        sh.renorm = 0;
+      }
+      __syncthreads();
+    }
+    if (sh.B >= L) sp_merge(a, m, sh);
+    __syncthreads();
+  }
+}
+
+// Writes the call's result to the store: new centroids into the back slot,
+// the quantile-walk prefix, the header and the buffer; then flips the slot.
+__device__ void sp_commit(const SpArgs& a, const SpMem& m, SpSh& sh) {
+  const KdStoreDev& s = a.s;
+  const int live = s.cur[0];
+  const int b = live ^ 1;
+  double* dm = s.slot_m + (size_t)b * (size_t)s.K * KD_TILE;
+  double* dw = s.slot_w + (size_t)b * (size_t)s.K * KD_TILE;
+  const int C = sh.C, B = sh.B;
+  for (int i = threadIdx.x; i < C; i += SP_T) {
+    dm[i] = m.cm[i];
+    dw[i] = m.cw[i];
+  }
+  for (int i = threadIdx.x; i < B; i += SP_T) {
+    s.buf_m[i] = m.bm[i];
+    s.buf_w[i] = m.bw[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double* P = s.prefix;  // the same walk prefix as the batch path's commit
+    if (C > 0) {
+      double run = KD_MUL(m.cw[0], 0.5);
+      P[0] = run;
+      for (int i = 0; i + 1 < C; ++i) {
+        run = KD_ADD(run, KD_MUL(KD_ADD(m.cw[i], m.cw[i + 1]), 0.5));
+        P[i + 1] = run;
+      }
+    }
+    s.count[0] = C;
+    s.total[0] = sh.st;
+    s.log_scale[0] = sh.ls;
+    s.clock[0] = sh.clock;
+    s.min_v[0] = sh.mn;
+    s.max_v[0] = sh.mx;
+    s.dfac[0] = s.lambda > 0.0 ? kd_exp(-sh.ls) : 1.0;
+    s.bcount[0] = B;
+    __threadfence();
+    s.cur[0] = (unsigned char)b;
+    a.out->count = C;
+    a.out->bcount = B;
+  }
+}
+
+// Renormalises the other digest of a merge_into in place (its weights, total
+// and exponent; the walk prefix follows the new weights).
+__device__ void sp_renorm_other(const SpArgs& a, SpSh& sh, double factor) {
+  const KdStoreDev& o = a.o;
+  const int live = o.cur[0];
+  double* ow = o.slot_w + (size_t)live * (size_t)o.K * KD_TILE;
+  const int C = o.count[0];
+  for (int i = threadIdx.x; i < C; i += SP_T) ow[i] = KD_MUL(ow[i], factor);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double* P = o.prefix;
+    if (C > 0) {
+      double run = KD_MUL(ow[0], 0.5);
+      P[0] = run;
+      for (int i = 0; i + 1 < C; ++i) {
+        run = KD_ADD(run, KD_MUL(KD_ADD(ow[i], ow[i + 1]), 0.5));
+        P[i + 1] = run;
+      }
+    }
+    o.total[0] = KD_MUL(o.total[0], factor);
+    o.log_scale[0] = 0.0;
+    o.dfac[0] = 1.0;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(SP_T) k_spath(SpArgs a) {
+  extern __shared__ __align__(256) unsigned char sp_smem[];
+  __shared__ SpSh sh;
+  __shared__ SpPick red[64];
+  __shared__ double dred[SP_T / 32];
+  SpMem m;
+  sp_layout(a.bmax, a.wpb, a.scratch ? a.scratch : sp_smem, &m);
+  const KdStoreDev& s = a.s;
+  const int live = s.cur[0];
+  if (threadIdx.x == 0) {
+    sh.C = s.count[0];
+    sh.B = s.bcount[0];
+    sh.st = s.total[0];
+    sh.ls = s.log_scale[0];
+    sh.clock = s.clock[0];
+    sh.mn = s.min_v[0];
+    sh.mx = s.max_v[0];
+    sh.err = 0;
+    sh.pre_adv = 0;
+    sh.renorm = 0;
+    sh.first_bad = a.n;
+    sh.integral = 1;
+    a.out->noop = 0;
+  }
+  __syncthreads();
+  {
+    const double* lm = s.slot_m + (size_t)live * (size_t)s.K * KD_TILE;
+    const double* lw = s.slot_w + (size_t)live * (size_t)s.K * KD_TILE;
+    for (int i = threadIdx.x; i < sh.C; i += SP_T) {
+      m.cm[i] = lm[i];
+      m.cw[i] = lw[i];
+    }
+    for (int i = threadIdx.x; i < sh.B; i += SP_T) {
+      m.bm[i] = s.buf_m[i];
+      m.bw[i] = s.buf_w[i];
+    }
+  }
+  __syncthreads();
+  if (a.op == SP_ADD) {
+    // the first invalid sample ends the loop there (the reference raises at it)
+    for (long long i = threadIdx.x; i < a.n; i += SP_T) {
+      const double v = a.vals[i];
+      const double w = a.wts ? a.wts[i] : 1.0;
+      const bool bad = !kd_isfinite(v) || !(w > 0.0) || !kd_isfinite(w);
+      if (bad) atomicMin((unsigned long long*)&sh.first_bad, (unsigned long long)i);
+      if (!(w == floor(w)) || w > SP_EXACT) sh.integral = 0;
+    }
+    __syncthreads();
+    sp_add(a, m, sh, sh.first_bad, red, dred);
+    if (threadIdx.x == 0 && !sh.err && sh.first_bad < a.n) {
+      a.out->code = KD_EINVAL;
+      a.out->index = sh.first_bad;
+    }
+  } else if (a.op == SP_FLUSH) {
+    sp_merge(a, m, sh);
+  } else {  // SP_MERGE_INTO (tdigest.mojo:589-623)
+    const KdStoreDev& o = a.o;
+    const double o_st = o.total[0], o_ls = o.log_scale[0];
+    const double o_eff = o.lambda > 0.0 ? KD_MUL(o_st, kd_exp(-o_ls)) : o_st;
+    if (o_eff == 0.0) {
+      if (threadIdx.x == 0) a.out->noop = 1;
+      return;
+    }
+    sp_merge(a, m, sh);
+    if (s.lambda > 0.0) sp_renormalize(m, sh);
+    double o_total = o_st;
+    if (o.lambda > 0.0) {
+      const double f = kd_exp(-o_ls);
+      sp_renorm_other(a, sh, f);
+      o_total = o.total[0];
+    }
+    const int oC = o.count[0];
+    const int olive = o.cur[0];
+    const double* om = o.slot_m + (size_t)olive * (size_t)o.K * KD_TILE;
+    const double* ow = o.slot_w + (size_t)olive * (size_t)o.K * KD_TILE;
+    for (int i = threadIdx.x; i < oC; i += SP_T) {
+      m.bm[i] = om[i];
+      m.bw[i] = ow[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const bool was_empty = sh.st == 0.0;
+      sh.B = oC;
+      sh.st = KD_ADD(sh.st, o_total);
+      const double omn = o.min_v[0], omx = o.max_v[0];
+      if (was_empty) {
+        sh.mn = omn;
+        sh.mx = omx;
+      } else {
+        sh.mn = sh.mn < omn ? sh.mn : omn;
+        sh.mx = sh.mx > omx ? sh.mx : omx;
+      }
+      sh.clock = sh.clock > o.clock[0] ? sh.clock : o.clock[0];
+    }
+    __syncthreads();
+    sp_merge(a, m, sh);
+  }
+  __syncthreads();
+  if (sh.err) {
+    if (threadIdx.x == 0) {
+      a.out->code = sh.err;
+      a.out->index = -1;
+    }
+    return;
+  }
+  sp_commit(a, m, sh);
+}
+
+int sp_fail(KdSession* s, int code, const char* msg) {
+  kd_set_msg(s, msg);
+  return code;
+}
+
+// Buffer storage of a one-key store, made on first use of the path.
+int sp_ensure(KdSession* s, KdStore* st) {
+  KdStoreDev& d = st->d;
+  if (d.K != 1) return sp_fail(s, KD_EINVAL, "the single-sample path serves one-digest stores");
+  if (d.bcount) return KD_OK;
+  long long L = (long long)d.compression * 5;  // Int(compression) * _BUFFER_FACTOR
+  if (L < 1) L = 1;
+  if (L > (1 << 20)) return sp_fail(s, KD_EINVAL, "compression too large for the single-sample path");
+  const size_t bytes = 64 + (size_t)L * 16;
+  if (s->mem_budget && s->mem_used + bytes > s->mem_budget)
+    return sp_fail(s, KD_ENOMEM, "device-memory budget exceeded by the sample buffer");
+  int* bc = nullptr;
+  double* bm = nullptr;
+  double* bw = nullptr;
+  if (cudaMalloc(&bc, 64) != cudaSuccess || cudaMalloc(&bm, (size_t)L * 8) != cudaSuccess ||
+      cudaMalloc(&bw, (size_t)L * 8) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(bc);
+    cudaFree(bm);
+    return sp_fail(s, KD_ENOMEM, "sample buffer allocation failed");
+  }
+  cudaMemsetAsync(bc, 0, 64, s->stream);
+  d.bcount = bc;
+  d.buf_m = bm;
+  d.buf_w = bw;
+  d.buf_cap = (int)L;
+  s->mem_used += bytes;
+  st->bytes += bytes;
+  kd_store_drop_graphs(st);  // captured steps hold the store view by value
+  return KD_OK;
+}
+
+struct SpShape {
+  int bmax, wpb;
+  size_t bytes;
+};
+SpShape sp_shape(const KdStoreDev& d) {
+  SpShape sh;
+  sh.bmax = std::max(d.buf_cap, KD_TILE);
+  sh.wpb = 1;
+  while (sh.wpb < sh.bmax) sh.wpb <<= 1;
+  sh.bytes = sp_layout(sh.bmax, sh.wpb, nullptr, nullptr);
+  return sh;
+}
+
+constexpr size_t SP_SMEM_MAX = 160 * 1024;  // beyond this the state lives in global scratch
+
+// The call's status block sits behind the buffer count in the same allocation.
+SpStatus* sp_status(KdStore* st) {
+  return reinterpret_cast<SpStatus*>(reinterpret_cast<char*>(st->d.bcount) + 16);
+}
+
+int sp_run(KdSession* s, KdStore* st, int op, const double* d_vals, const double* d_wts,
+           const double* d_ts, long long n, KdStore* other, SpStatus* result) {
+  KdStoreDev& d = st->d;
+  const SpShape shp = sp_shape(d);
+  unsigned char* scratch = nullptr;
+  size_t smem = shp.bytes;
+  if (shp.bytes > SP_SMEM_MAX) {
+    if (st->sp_scratch_bytes < shp.bytes) {
+      if (st->sp_scratch) cudaFree(st->sp_scratch);
+      st->sp_scratch = nullptr;
+      st->sp_scratch_bytes = 0;
+      if (cudaMalloc(&st->sp_scratch, shp.bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return sp_fail(s, KD_ENOMEM, "single-sample path scratch allocation failed");
+      }
+      st->sp_scratch_bytes = shp.bytes;
+    }
+    scratch = (unsigned char*)st->sp_scratch;
+    smem = 0;
+  }
+  static bool attr_done[64] = {};
+  const int dev = s->device;
+  if (smem && dev >= 0 && dev < 64 && !attr_done[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k_spath, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SP_SMEM_MAX);
+    if (e != cudaSuccess) return kd_cuda_fail(s, e, "single-sample path attributes");
+    attr_done[dev] = true;
+  }
+  SpStatus* dstat = sp_status(st);
+  SpArgs a;
+  a.s = d;
+  a.o = other ? other->d : d;
+  a.vals = d_vals;
+  a.wts = d_wts;
+  a.ts = d_ts;
+  a.n = n;
+  a.op = op;
+  a.bmax = shp.bmax;
+  a.wpb = shp.wpb;
+  a.scratch = scratch;
+  a.out = dstat;
+  cudaStream_t str = s->stream;
+  cudaError_t e = cudaMemsetAsync(dstat, 0, sizeof(SpStatus), str);
+  if (e != cudaSuccess) return kd_cuda_fail(s, e, "single-sample path");
+  k_spath<<<1, SP_T, smem, str>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return kd_cuda_fail(s, e, "single-sample path launch");
+  SpStatus h{};
+  e = cudaMemcpyAsync(&h, dstat, sizeof(SpStatus), cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+  if (e != cudaSuccess) return kd_cuda_fail(s, e, "single-sample path");
+  *result = h;
+  s->stats.launches += 1;
+  return KD_OK;
+}
+
+int sp_after(KdSession* s, KdStore* st, const SpStatus& r) {
+  if (r.code == KD_ERANGE) {
+    return sp_fail(s, KD_ERANGE, "a merge pass produced more than 1024 centroids");
+  }
+  if (!r.noop && r.code != KD_ERANGE) {
+    st->pending = r.bcount > 0;
+    st->carry = true;
+  }
+  if (r.code == KD_EINVAL) {
+    char msg[160];
+    snprintf(msg, sizeof msg,
+             "sample %lld: value must be finite (got NaN or inf) and weight positive and finite",
+             r.index);
+    kd_set_msg(s, msg);
+    return KD_EINVAL;
+  }
+  return r.code;
+}
+
+__global__ void k_carry_build(KdStoreDev s, const double* __restrict__ vals, long long n, int C,
+                              int B, double* __restrict__ ov, double* __restrict__ ow,
+                              unsigned long long* mm) {
+  const int live = s.cur[0];
+  const double* lm = s.slot_m + (size_t)live * (size_t)s.K * KD_TILE;
+  const double* lw = s.slot_w + (size_t)live * (size_t)s.K * KD_TILE;
+  const long long tot = (long long)C + B + n;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot;
+       i += (long long)gridDim.x * blockDim.x) {
+    double v, w;
+    if (i < C) {
+      v = lm[i];
+      w = lw[i];
+    } else if (i < C + B) {
+      v = s.buf_m[i - C];
+      w = s.buf_w[i - C];
+    } else {
+      v = vals[i - C - B];
+      w = 0.0;  // the batch's samples take the decay weight of the step
+      if (kd_isfinite(v)) {
+        const unsigned long long k = kd_order_key(v);
+        atomicMin(&mm[0], k);
+        atomicMax(&mm[1], k);
+      }
+    }
+    ov[i] = v;
+    ow[i] = w;
+  }
+}
+
+}  // namespace
+
+int kd_spath_flush(KdSession* s, KdStore* st) {
+  if (!st->pending) return KD_OK;
+  cudaSetDevice(s->device);
+  SpStatus r{};
+  int rc = sp_run(s, st, SP_FLUSH, nullptr, nullptr, nullptr, 0, nullptr, &r);
+  if (rc) return rc;
+  return sp_after(s, st, r);
+}
+
+int kd_spath_carry_ingest(KdSession* s, KdStore* st, const double* d_vals, long long n, int mode,
+                          double timestamp) {
+  cudaStream_t str = s->stream;
+  int hc[2] = {0, 0};
+  cudaError_t e = cudaMemcpyAsync(&hc[0], st->d.count, 4, cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess && st->d.bcount)
+    e = cudaMemcpyAsync(&hc[1], st->d.bcount, 4, cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+  if (e != cudaSuccess) return kd_cuda_fail(s, e, "carried batch");
+  const long long carry = (long long)hc[0] + hc[1];
+  if (carry == 0) {
+    st->carry = false;
+    st->pending = false;
+    return kd_pipeline_ingest(s, st, nullptr, d_vals, nullptr, n, mode, timestamp, nullptr,
+                              nullptr, nullptr);
+  }
+  const long long tot = carry + n;
+  void* buf = nullptr;
+  const size_t bytes = (size_t)tot * 16 + 64;
+  if (cudaMalloc(&buf, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return sp_fail(s, KD_ENOMEM, "carried batch staging allocation failed");
+  }
+  unsigned long long* mm = (unsigned long long*)buf;
+  double* ov = (double*)((char*)buf + 64);
+  double* ow = ov + tot;
+  const unsigned long long init[2] = {~0ull, 0ull};
+  e = cudaMemcpyAsync(mm, init, 16, cudaMemcpyHostToDevice, str);
+  if (e == cudaSuccess) {
+    const int grid = (int)std::min<long long>((tot + 255) / 256, (long long)s->num_sms * 8);
+    k_carry_build<<<grid, 256, 0, str>>>(st->d, d_vals, n, hc[0], hc[1], ov, ow, mm);
+    e = cudaGetLastError();
+  }
+  int rc = e == cudaSuccess ? KD_OK : kd_cuda_fail(s, e, "carried batch");
+  if (rc == KD_OK) {
+    rc = kd_pipeline_ingest(s, st, nullptr, ov, ow, tot, mode, timestamp, nullptr, nullptr,
+                            nullptr, carry, mm);
+    if (rc == KD_OK) {
+      st->carry = false;
+      st->pending = false;
+    }
+  }
+  cudaStreamSynchronize(str);
+  cudaFree(buf);
+  return rc;
+}
+
+// Frees the buffer and scratch of a store (their bytes are part of st->bytes,
+// which the caller gives back to the session).
+void kd_spath_free(KdSession*, KdStore* st) {
+  KdStoreDev& d = st->d;
+  if (d.bcount) {
+    cudaFree(d.bcount);
+    cudaFree(d.buf_m);
+    cudaFree(d.buf_w);
+  }
+  d.bcount = nullptr;
+  d.buf_m = nullptr;
+  d.buf_w = nullptr;
+  if (st->sp_scratch) cudaFree(st->sp_scratch);
+  st->sp_scratch = nullptr;
+  st->sp_scratch_bytes = 0;
+}
+
+extern "C" {
+
+KD_API int kd_store_add(kd_store* h, const double* values, const double* weights,
+                        const double* timestamps, int64_t n, int flags) {
+  if (!h) return KD_EINVAL;
+  KdStore* st = &h->st;
+  KdSession* s = st->sess;
+  if (!s) return KD_EINVAL;
+  if (n < 0 || (n > 0 && !values)) return sp_fail(s, KD_EINVAL, "values must be non-null");
+  if (n == 0) return KD_OK;
+  cudaSetDevice(s->device);
+  int rc = sp_ensure(s, st);
+  if (rc) return rc;
+  const double* dv = values;
+  const double* dw = weights;
+  const double* dt = timestamps;
+  void* tmp = nullptr;
+  cudaStream_t str = s->stream;
+  if (!(flags & KD_PTR_DEVICE)) {
+    const size_t per = 8 * (1 + (weights ? 1 : 0) + (timestamps ? 1 : 0));
+    if (cudaMalloc(&tmp, (size_t)n * per) != cudaSuccess) {
+      cudaGetLastError();
+      return sp_fail(s, KD_ENOMEM, "sample staging allocation failed");
+    }
+    double* p = (double*)tmp;
+    cudaMemcpyAsync(p, values, (size_t)n * 8, cudaMemcpyHostToDevice, str);
+    dv = p;
+    p += n;
+    if (weights) {
+      cudaMemcpyAsync(p, weights, (size_t)n * 8, cudaMemcpyHostToDevice, str);
+      dw = p;
+      p += n;
+    }
+    if (timestamps) {
+      cudaMemcpyAsync(p, timestamps, (size_t)n * 8, cudaMemcpyHostToDevice, str);
+      dt = p;
+    }
+  }
+  SpStatus r{};
+  rc = sp_run(s, st, SP_ADD, dv, dw, dt, n, nullptr, &r);
+  if (tmp) cudaFree(tmp);
+  if (rc) return rc;
+  return sp_after(s, st, r);
+}
+
+KD_API int kd_store_flush(kd_store* h) {
+  if (!h) return KD_EINVAL;
+  KdStore* st = &h->st;
+  KdSession* s = st->sess;
+  if (!s) return KD_EINVAL;
+  return kd_spath_flush(s, st);
+}
+
+KD_API int kd_store_merge_into(kd_store* dst, kd_store* src) {
+  if (!dst || !src || dst == src) return KD_EINVAL;
+  KdStore* st = &dst->st;
+  KdStore* so = &src->st;
+  KdSession* s = st->sess;
+  if (!s || !so->sess) return KD_EINVAL;
+  if (so->sess->device != s->device)
+    return sp_fail(s, KD_EINVAL, "merge_into needs both digests on one device");
+  if (st->d.K != 1 || so->d.K != 1)
+    return sp_fail(s, KD_EINVAL, "merge_into joins two one-digest stores");
+  cudaSetDevice(s->device);
+  int rc = sp_ensure(s, st);
+  if (rc) return rc;
+  if (so->sess != s) cudaStreamSynchronize(so->sess->stream);
+  rc = kd_spath_flush(so->sess, so);  // other.merge()
+  if (rc) return rc;
+  SpStatus r{};
+  rc = sp_run(s, st, SP_MERGE_INTO, nullptr, nullptr, nullptr, 0, so, &r);
+  if (rc) return rc;
+  if (!r.noop && so->d.lambda > 0.0) so->carry = true;
+  return sp_after(s, st, r);
+}
+
+}  // extern "C"

@@ -246,8 +246,22 @@ def _validate_values(values) -> np.ndarray:
     return v
 
 
+# add_batch takes the batch path from these sizes up, the single-sample loop
+# below them (tdigest.mojo:49-58, 199, 215).
+GPU_CROSSOVER = 60_000
+GPU_CROSSOVER_SESSION = 40_000
+_ADD_QUEUE = 4096  # single adds queued on the host before one device call
+
+
 class TDigest:
-    """One t-digest on the device (tdigest.mojo:97-726) — a one-key store."""
+    """One t-digest on the device (tdigest.mojo:97-726) — a one-key store.
+
+    ``add`` / ``add_at`` and ``add_batch`` below the crossover run the
+    reference's single-sample loop on the device (buffer, sequential merge
+    pass); ``add_batch`` from the crossover up runs the batch path with the
+    buffer folded in, as the reference does.  Single adds are validated at once
+    and queued on the host; every other call first sends the queue, in order,
+    so results are those of the reference's loop."""
 
     def __init__(self, compression: float = 100.0, scale: int = K1, decay: Decay | None = None,
                  session: GpuSession | None = None, _store: _Store | None = None):
@@ -255,66 +269,119 @@ class TDigest:
         self.scale = scale
         self._decay = decay if decay is not None else Decay.none()
         self._store = _store or _Store(1, compression, scale, self._decay, session)
+        self._qv: list[float] = []
+        self._qw: list[float] = []
+        self._qt: list[float] | None = None  # timestamps when the queue holds add_at
 
     @property
     def session(self) -> GpuSession:
         return self._store.session
 
     # -- ingest ---------------------------------------------------------------
+    def _add_many(self, values, weights=None, timestamps=None):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+        t = None if timestamps is None else np.ascontiguousarray(timestamps, dtype=np.float64)
+        rc = N.load().kd_store_add(self._store._h, N.ptr(v), N.ptr(w), N.ptr(t), len(v), 0)
+        self._store._chk(rc)
+
+    def _sync(self):
+        """Send the queued single adds (in order) to the device."""
+        if not self._qv:
+            return
+        v, w, t = self._qv, self._qw, self._qt
+        self._qv, self._qw, self._qt = [], [], None
+        weights = None if all(x == 1.0 for x in w) else w
+        self._add_many(v, weights, t)
+
+    def _queue(self, value, weight, timestamp):
+        timed = timestamp is not None
+        if self._qv and (self._qt is not None) != timed:
+            self._sync()
+        self._qv.append(float(value))
+        self._qw.append(float(weight))
+        if timed:
+            if self._qt is None:
+                self._qt = []
+            self._qt.append(float(timestamp))
+        if len(self._qv) >= _ADD_QUEUE:
+            self._sync()
+
+    def add(self, value: float, weight: float = 1.0):
+        """One sample, one clock tick (tdigest.mojo:153-161)."""
+        _validate_sample(value, weight)
+        self._queue(value, weight, None)
+
+    def add_at(self, value: float, timestamp: float, weight: float = 1.0):
+        """One sample at `timestamp` (tdigest.mojo:163-175)."""
+        _validate_sample(value, weight)
+        self._queue(value, weight, timestamp)
+
     def add_batch(self, values, session: GpuSession | None = None):
         """Fold a batch of unit-weight samples in (tdigest.mojo:177-234); the
-        clock advances by len(values) ticks."""
+        clock advances by len(values) ticks.  Below the crossover (60,000, or
+        40,000 with a session) this is the reference's add loop, which stops at
+        the first invalid value; from it up the batch path validates first."""
+        self._sync()
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        if v.size == 0:
+            return
+        crossover = GPU_CROSSOVER if session is None else GPU_CROSSOVER_SESSION
+        if v.size < crossover:
+            self._add_many(v)
+            return
+        v = _validate_values(v)
+        self._store.ingest(None, v, N.KD_CLOCK_COUNT, 0.0)
+
+    def add_batch_p(self, values):
+        """The batch path at any size (the reference's _add_batch_gpu,
+        tdigest.mojo:223-234)."""
+        self._sync()
         v = _validate_values(values)
         if v.size == 0:
             return
         self._store.ingest(None, v, N.KD_CLOCK_COUNT, 0.0)
 
     def add_batch_at(self, values, timestamp: float):
-        """Batch form of add_at (tdigest.mojo:163-175): the clock moves to
+        """Batch form of add_at on the batch path: the clock moves to
         `timestamp` once when later, then every sample is inserted."""
+        self._sync()
         v = _validate_values(values)
         if v.size == 0:
             return
         self._store.ingest(None, v, N.KD_CLOCK_TIME, float(timestamp))
 
-    def add(self, value: float, weight: float = 1.0):
-        """One unit-weight sample as a batch of one (P-path)."""
-        if weight != 1.0:
-            if not (weight > 0.0) or not math.isfinite(weight):
-                raise ValueError("weight must be positive and finite")
-            raise ValueError("weighted samples are not part of the GPU batch path")
-        self.add_batch([value])
-
-    def add_at(self, value: float, timestamp: float, weight: float = 1.0):
-        if weight != 1.0:
-            if not (weight > 0.0) or not math.isfinite(weight):
-                raise ValueError("weight must be positive and finite")
-            raise ValueError("weighted samples are not part of the GPU batch path")
-        self.add_batch_at([value], timestamp)
-
     def merge(self):
-        """Every batch is already compressed; nothing is buffered."""
+        """Merge the buffered samples (tdigest.mojo:391-439)."""
+        self._sync()
+        self._store._chk(N.load().kd_store_flush(self._store._h))
 
     # -- queries --------------------------------------------------------------
     def quantile(self, q: float) -> float:
         if not (0.0 <= q <= 1.0):
             raise ValueError("quantile q must be in [0, 1]")
+        self._sync()
         return float(self._store.query(None, [q], False)[0])
 
     def cdf(self, x: float) -> float:
+        self._sync()
         return float(self._store.query(None, [x], True)[0])
 
     def quantiles(self, qs) -> np.ndarray:
+        self._sync()
         return self._store.query(None, qs, False)
 
     def cdfs(self, xs) -> np.ndarray:
+        self._sync()
         return self._store.query(None, xs, True)
 
     # -- state ----------------------------------------------------------------
     def _state(self):
+        self._sync()
         return self._store.digest(0)
 
     def centroids(self):
+        """The merged centroids (buffered samples not included, as len())."""
         _, m, w = self._state()
         return m, w
 
@@ -340,12 +407,18 @@ class TDigest:
 
     # -- merge / serde --------------------------------------------------------
     def merge_into(self, other: "TDigest"):
-        """Fold `other` into this digest: both rebased to effective weights,
-        centroids concatenated (self first) and compressed once with the
-        P-path (gpu/query.mojo:348-369, tdigest.mojo:589-623)."""
-        merge_digests(self, [self, other])
+        """Fold `other` into this digest (tdigest.mojo:589-623): both merged,
+        both rebased to effective weights when decaying, other's centroids
+        through this digest's merge pass."""
+        if other is self:
+            raise ValueError("cannot merge a digest into itself")
+        self._sync()
+        other._sync()
+        rc = N.load().kd_store_merge_into(self._store._h, other._store._h)
+        self._store._chk(rc)
 
     def to_bytes(self) -> bytes:
+        self._sync()
         return self._store.to_bytes(0)
 
     @staticmethod
@@ -366,11 +439,22 @@ class TDigest:
         return d
 
 
+def _validate_sample(value: float, weight: float):
+    """TDigest._validate (tdigest.mojo:317-322)."""
+    if not math.isfinite(value):
+        raise ValueError("value must be finite (got NaN or inf)")
+    if not (weight > 0.0) or not math.isfinite(weight):
+        raise ValueError("weight must be positive and finite")
+
+
 def merge_digests(dst: TDigest, parts) -> None:
-    """Replace `dst` by the P-path merge of `parts` (gpu_merge_digests)."""
+    """Replace `dst` by the P-path merge of `parts` (gpu_merge_digests); each
+    part is merged first, as reading its centroids requires."""
     sess = dst.session
+    dst._sync()
     tmp = _Store(len(parts), parts[0].compression, parts[0].scale, parts[0]._decay, sess)
     for i, p in enumerate(parts):
+        p.merge()
         hdr, m, w = p._state()
         tmp.set_digest(i, hdr, m, w)
     dst._store.merge_from(tmp, [0, len(parts)], np.arange(len(parts), dtype=np.uint32))

@@ -77,7 +77,7 @@ def test_single_digest_and_compress_replays(kd, oracle):
     rng = np.random.default_rng(4)
     for step in range(8):
         v = rng.standard_normal(4096)
-        d.add_batch(v)
+        d.add_batch_p(v)
         ref.add_batch_p(v)
     m, w = d.centroids()
     om, ow = ref.centroids()
