@@ -282,32 +282,48 @@ def run_config1(args) -> int:
     ext = torch.cuda.ExternalStream(sess.stream, device=dev)
     L = N.load()
     nb = (C1_TOTAL + C1_BATCH - 1) // C1_BATCH
-    reps = []
-    for rep in range(args.warmup + 3):  # whole-stream passes; the first ones warm up
-        d = kd.TDigest(100.0, kd.K1, session=sess)
-        h = d._store._h
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(ext)
-        for b in range(nb):
-            n = min(C1_BATCH, C1_TOTAL - b * C1_BATCH)
-            rc = L.kd_store_ingest(h, None, vals.data_ptr() + b * C1_BATCH * 8, n, N.KD_CLOCK_COUNT,
-                                   0.0, N.KD_PTR_DEVICE)
-            if rc:
-                raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
-        e1.record(ext)
-        e1.synchronize()
-        if rep >= args.warmup:
-            reps.append(e0.elapsed_time(e1))
-    ms = statistics.median(reps)
+
+    def stream(single: bool):
+        """The whole stream in batches of 4096: the reference's path for this
+        size (the add loop on the device) or the batch path."""
+        reps = []
+        d = None
+        for rep in range(args.warmup + 3):  # whole-stream passes; the first ones warm up
+            d = kd.TDigest(100.0, kd.K1, session=sess)
+            h = d._store._h
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            for b in range(nb):
+                n = min(C1_BATCH, C1_TOTAL - b * C1_BATCH)
+                p = vals.data_ptr() + b * C1_BATCH * 8
+                if single:
+                    rc = L.kd_store_add(h, p, None, None, n, N.KD_PTR_DEVICE)
+                else:
+                    rc = L.kd_store_ingest(h, None, p, n, N.KD_CLOCK_COUNT, 0.0, N.KD_PTR_DEVICE)
+                if rc:
+                    raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+            e1.record(ext)
+            e1.synchronize()
+            if rep >= args.warmup:
+                reps.append(e0.elapsed_time(e1))
+        return statistics.median(reps), d
+
+    ms, d = stream(True)
+    ms_p, dp = stream(False)
     q7 = np.array(QUANTILES)
     sv = np.sort(vals_h)
     gq = d.quantiles(q7)
     gc = d.cdfs(np.array(C1_X))
-    out = {"gpu_p_path": {"rank_error_ppm": [round(x, 1) for x in rank_error_ppm(sv, gq, q7)],
-                          "centroids": len(d), "quantiles": gq.tolist(), "cdf": gc.tolist()}}
+    pq = dp.quantiles(q7)
+    out = {"gpu_s_path": {"rank_error_ppm": [round(x, 1) for x in rank_error_ppm(sv, gq, q7)],
+                          "centroids": len(d), "quantiles": gq.tolist(), "cdf": gc.tolist()},
+           "gpu_p_path": {"rank_error_ppm": [round(x, 1) for x in rank_error_ppm(sv, pq, q7)],
+                          "centroids": len(dp), "ms_per_stream": ms_p,
+                          "samples_per_s": C1_TOTAL / (ms_p / 1e3)}}
     cpu = None
+    parity = None
     if not args.no_cpu:
         from oracle import pyoracle as po
 
@@ -320,6 +336,10 @@ def run_config1(args) -> int:
         oq = np.array([od.quantile(q) for q in q7])
         out["cpu_s_path"] = {"rank_error_ppm": [round(x, 1) for x in rank_error_ppm(sv, oq, q7)],
                              "centroids": len(od.centroids()[0]), "quantiles": oq.tolist()}
+        om, ow = od.centroids()
+        gm, gw = d.centroids()
+        parity = bool(np.array_equal(om, gm) and np.array_equal(ow, gw) and
+                      np.array_equal(oq, gq) and d.to_bytes() == od.to_bytes())
         cpu = {"value": C1_TOTAL / dt, "unit": "samples/s", "cores": 1, "kind": "port",
                "sample": f"the whole stream through the oracle's sequential add loop in C "
                          f"({dt:.2f} s)"}
@@ -329,7 +349,10 @@ def run_config1(args) -> int:
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic N(0,1), seed 0, resident in HBM",
         "config": {"workload": "config 1: 1e6 N(0,1) samples into one TDigest[K1] d100 in "
-                               "batches of 4096 (a step is the whole stream)", "batch": C1_BATCH},
+                               "batches of 4096 (a step is the whole stream) through the "
+                               "reference's path for this batch size, the add loop",
+                   "batch": C1_BATCH},
+        "bit_exact_vs_reference_loop": parity,
         "accuracy": out, "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

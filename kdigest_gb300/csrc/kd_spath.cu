@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 
 #include "../../include/kdigest_gb300.h"
@@ -38,8 +39,8 @@ namespace {
 
 constexpr int SP_T = 1024;  // threads of the one CTA
 constexpr double SP_RENORM = 400.0;    // tdigest.mojo:43
+constexpr int SP_RCP_N = 1 << 16;      // reciprocal table entries
 constexpr double SP_PRUNE_EPS = 1e-6;  // tdigest.mojo:47
-constexpr double SP_EXACT = 9007199254740992.0;  // 2^53
 
 enum { SP_ADD = 0, SP_FLUSH = 1, SP_MERGE_INTO = 2 };
 
@@ -62,6 +63,7 @@ struct SpArgs {
   int bmax;  // buffer capacity inside the call: max(buf_cap, KD_TILE)
   int wpb;   // power of two >= bmax (width of the buffer sort)
   unsigned char* scratch;  // global working memory, or null (dynamic shared memory)
+  const double* rcp;       // 1 / d for d < SP_RCP_N (d = 0 unused)
   SpStatus* out;
 };
 
@@ -72,9 +74,11 @@ struct SpMem {
   unsigned* sidx;            // buffer sort positions [wpb]
   double *sm, *sw;  // merged work [KD_TILE + bmax]
   double* kk;       // k at every prefix [KD_TILE + bmax + 1]
-  double* rw;       // running cluster weight before each element [KD_TILE + bmax + 1]
+  double* rw;       // running cluster weight before each element, or its weight ratio [W + 1]
+  long long* pi;    // exact integer prefix of the work weights [W + 1]
   int* cst;         // cluster starts [KD_TILE + 1]
-  int* cid;         // cluster of each element [KD_TILE + bmax]
+  int* cid;         // cluster (or cluster start) of each element [KD_TILE + bmax]
+  int* nb;          // next cluster start after each possible start [KD_TILE + bmax]
   double* sls;      // log-scale of each sample of a segment [bmax]
   double *wsf, *kl;  // weight before each cluster and its k [KD_TILE + 1]
 };
@@ -100,8 +104,10 @@ __host__ __device__ inline size_t sp_layout(int bmax, int wpb, unsigned char* ba
   t.sw = (double*)take(8 * W);
   t.kk = (double*)take(8 * (W + 1));
   t.rw = (double*)take(8 * (W + 1));
+  t.pi = (long long*)take(8 * (W + 1));
   t.cst = (int*)take(4 * (KD_TILE + 1));
   t.cid = (int*)take(4 * W);
+  t.nb = (int*)take(4 * W);
   t.sls = (double*)take(8 * (size_t)bmax);
   t.wsf = (double*)take(8 * (KD_TILE + 1));
   t.kl = (double*)take(8 * (KD_TILE + 1));
@@ -114,10 +120,67 @@ struct SpSh {
   double st, ls, clock, mn, mx;
   double factor, nrm, renorm_clock;
   long long first_bad;
-  int C, B, err, nc, mismatch, unsorted, exact, cut, renorm, pre_adv, integral;
+  double k0, k1;  // FP64 k at q = 0 and q = 1 (filtered sweeps)
+  double f0, f1;  // the same with normaliser 1: k(q, nrm) = nrm * k(q, 1) at these q
+  double nrm01;   // the K0 / K1 normaliser (it does not depend on the total)
+  int C, B, err, nc, mismatch, unsorted, exact, cut, renorm, pre_adv, integral, fast, filt;
+  long long wsum[32];  // per-warp partial sums of block scans and reductions
 };
 
 __device__ __forceinline__ double sp_k(int scale, double q, double nrm) { return kd_k(scale, q, nrm); }
+
+// k at q = p / st in FP32 (integral p, st <= 1e14, 0 <= p <= st), in forms
+// without cancellation: q and 1 - q both come from exact integers, asin near
+// +-1 goes through asin(1 - 2s) = pi/2 - 2 asin(sqrt(s)).  Against the FP64
+// k of the same q the error is below 2e-5 * nrm for every scale (FP32
+// rounding of p, st and 1 - q, and the documented few-ulp accuracy of asinf,
+// logf and sqrtf); the sweep treats differences within nrm * 2^-12 of the
+// limit as undecided and settles them in FP64.
+__device__ __forceinline__ float sp_k32(int scale, long long p, double st, float nrmf, float k0f,
+                                        float k1f) {
+  if (p == 0) return k0f;
+  const double rest = st - (double)p;  // exact: integers below 2^47
+  if (rest == 0.0) return k1f;
+  const float a = (float)p, c = (float)rest, b = (float)st;
+  switch (scale) {
+    case KD_SCALE_K0:
+      return nrmf * (a / b);
+    case KD_SCALE_K1: {
+      const bool lo = a <= c;
+      const float t = 1.57079637f - 2.0f * asinf(sqrtf((lo ? a : c) / b));
+      return nrmf * (lo ? -t : t);
+    }
+    case KD_SCALE_K2:
+      return nrmf * logf(a / c);
+    default:
+      return a <= c ? nrmf * logf(2.0f * a / b) : -nrmf * logf(2.0f * c / b);
+  }
+}
+
+// The k-size test of the merge pass for candidate j of the cluster that starts
+// at s0: k(q(j + 1)) - k(q(s0)) <= 1 with FP64 k at exact prefix positions.
+// Filtered: the FP32 difference decides unless it is within tau of 1; then (and
+// only then) the FP64 values are evaluated.  ks64 caches the start's FP64 k.
+struct SpFit {
+  int scale;
+  bool filt;
+  float tau;
+  double st, nrm;
+  const float* k32;
+  const double* kk;
+  const long long* pi;
+  __device__ double k64(int i) const {
+    return filt ? sp_k(scale, KD_DIV((double)pi[i], st), nrm) : kk[i];
+  }
+  __device__ bool fits(int s0, int j, double& ks64) const {
+    if (!filt) return KD_SUB(kk[j + 1], kk[s0]) <= 1.0;
+    const float d = k32[j + 1] - k32[s0];
+    if (d <= 1.0f - tau) return true;
+    if (d > 1.0f + tau) return false;
+    if (ks64 != ks64) ks64 = k64(s0);
+    return KD_SUB(k64(j + 1), ks64) <= 1.0;
+  }
+};
 
 // Block-wide exclusive prefix of v[0..n) into out[0..n] (out[n] = total), in
 // any association order: used only where the sums are exact (integers below
@@ -159,51 +222,179 @@ __device__ void sp_prefix(const double* v, double* out, int n, double* tmp_warp)
   __syncthreads();
 }
 
-// Stable ascending sort of the buffer (bm[0..B)) by value: bitonic over
-// (order key, position), so equal values (and -0.0 / +0.0) keep their order.
-__device__ void sp_sort_buffer(const SpMem& m, int B, int wpb) {
-  int P = 1;
-  while (P < B) P <<= 1;
-  for (int i = threadIdx.x; i < P; i += SP_T) {
-    if (i < B) {
-      m.okey[i] = kd_order_key(m.bm[i]);
-      m.sidx[i] = (unsigned)i;
-    } else {
-      m.okey[i] = ~0ull;
-      m.sidx[i] = 0xffffffffu;
+// w as an integer when it is one in [1, 2^53] (integer ops only).
+__device__ __forceinline__ bool sp_int53(double w, long long* out) {
+  const unsigned long long b = kd_bits(w);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  if ((b >> 63) || e < 0 || e > 52) return false;
+  const unsigned long long mant = (b & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+  const int sh = 52 - e;
+  if (sh > 0 && (mant & ((1ull << sh) - 1ull))) return false;
+  *out = (long long)(mant >> sh);
+  return true;
+}
+
+// Block-wide sum of one int64 per thread (every thread gets the total).
+__device__ long long sp_isum(long long v, SpSh& sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh.wsum[threadIdx.x >> 5] = v;
+  __syncthreads();
+  long long t = 0;
+  for (int w = 0; w < SP_T / 32; ++w) t += sh.wsum[w];
+  __syncthreads();
+  return t;
+}
+
+// Block-wide exclusive scan of one int64 per thread; *total gets the sum.
+__device__ long long sp_iscan(long long v, SpSh& sh, long long* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  long long x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh.wsum[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    long long t = sh.wsum[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
     }
+    sh.wsum[lane] = t;
   }
   __syncthreads();
-  for (int k = 2; k <= P; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = threadIdx.x; i < P; i += SP_T) {
-        const int ixj = i ^ j;
-        if (ixj > i) {
-          const unsigned long long a = m.okey[i], b = m.okey[ixj];
-          const unsigned ia = m.sidx[i], ib = m.sidx[ixj];
-          const bool gt = a > b || (a == b && ia > ib);
-          if (gt == ((i & k) == 0)) {
-            m.okey[i] = b;
-            m.okey[ixj] = a;
-            m.sidx[i] = ib;
-            m.sidx[ixj] = ia;
+  const long long excl = x - v + (w > 0 ? sh.wsum[w - 1] : 0);
+  *total = sh.wsum[SP_T / 32 - 1];
+  __syncthreads();
+  return excl;
+}
+
+// Integer exclusive prefix out[0..n] of integral weights v[0..n) (exact).
+__device__ void sp_iprefix(const double* v, long long* out, int n, SpSh& sh) {
+  const int per = (n + SP_T - 1) / SP_T;
+  const int b = threadIdx.x * per, e = min(n, b + per);
+  long long sum = 0;
+  for (int i = b; i < e; ++i) {
+    long long x = 0;
+    sp_int53(v[i], &x);
+    sum += x;
+  }
+  long long total;
+  long long run = sp_iscan(sum, sh, &total);
+  for (int i = b; i < e; ++i) {
+    out[i] = run;
+    long long x = 0;
+    sp_int53(v[i], &x);
+    run += x;
+  }
+  if (threadIdx.x == 0) out[n] = total;
+  __syncthreads();
+}
+
+// Stable ascending sort of the buffer (bm[0..B)) by value: bitonic over
+// (order key, position), so equal values (and -0.0 / +0.0) keep their order.
+// Up to one element per thread the keys stay in registers: strides below 32
+// exchange through warp shuffles, larger ones through shared memory.
+__device__ __forceinline__ void sp_sort_buffer(const SpMem& m, int B) {
+  int P = 1;
+  while (P < B) P <<= 1;
+  if (P > SP_T) {
+    for (int i = threadIdx.x; i < P; i += SP_T) {
+      m.okey[i] = i < B ? kd_order_key(m.bm[i]) : ~0ull;
+      m.sidx[i] = i < B ? (unsigned)i : 0xffffffffu;
+    }
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int i = threadIdx.x; i < P; i += SP_T) {
+          const int ixj = i ^ j;
+          if (ixj > i) {
+            const unsigned long long a = m.okey[i], b = m.okey[ixj];
+            const unsigned ia = m.sidx[i], ib = m.sidx[ixj];
+            const bool gt = a > b || (a == b && ia > ib);
+            if (gt == ((i & k) == 0)) {
+              m.okey[i] = b;
+              m.okey[ixj] = a;
+              m.sidx[i] = ib;
+              m.sidx[ixj] = ia;
+            }
           }
         }
+        __syncthreads();
       }
-      __syncthreads();
     }
+    return;
+  }
+  // One element per thread: 32-element runs sorted in registers (bitonic over
+  // warp shuffles), then runs merged pairwise.  Keys are distinct (value key,
+  // then position; the padding has positions of its own), so an element's place
+  // in a merged run is its place in its own run plus the number of partner-run
+  // elements before it.
+  const int i = threadIdx.x;
+  const int R = P < 32 ? P : 32;
+  const bool warp_on = (i & ~31) < P;
+  unsigned long long key = ~0ull;
+  unsigned idx = 0x80000000u | (unsigned)i;
+  if (i < B) {
+    key = kd_order_key(m.bm[i]);
+    idx = (unsigned)i;
+  }
+  if (warp_on) {
+    const int lane = i & 31;  // every run of 32 ends ascending
+    for (int k = 2; k <= R; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, j);
+        const unsigned oi = __shfl_xor_sync(0xffffffffu, idx, j);
+        const bool up = (lane & k) == 0;
+        const bool lower = (lane & j) == 0;
+        const bool other_less = ok < key || (ok == key && oi < idx);
+        if ((lower == up) == other_less) {
+          key = ok;
+          idx = oi;
+        }
+      }
+    }
+  }
+  if (i < P) {
+    m.okey[i] = key;
+    m.sidx[i] = idx;
+  }
+  __syncthreads();
+  int at = i;  // where this thread's element sits
+  for (int run = 32; run < P; run <<= 1) {
+    int pos = 0;
+    if (i < P) {
+      const int base = (at / run) * run;
+      const int other = base ^ run;
+      int lo = 0, hi = run;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const unsigned long long ok = m.okey[other + mid];
+        if (ok < key || (ok == key && m.sidx[other + mid] < idx)) lo = mid + 1;
+        else hi = mid;
+      }
+      pos = (base < other ? base : other) + (at - base) + lo;
+    }
+    __syncthreads();
+    if (i < P) {
+      m.okey[pos] = key;
+      m.sidx[pos] = idx;
+      at = pos;
+    }
+    __syncthreads();
   }
 }
 
 // The merge pass (tdigest.mojo:391-439, _prune :441-458) over C centroids and
 // B buffered samples in shared state.  Leaves the new centroids in cm/cw.
-__device__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh) {
+__device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh) {
   const int B = sh.B, C = sh.C;
   if (B == 0) return;
   const int scale = a.s.scale;
   const bool decay = a.s.lambda > 0.0;
   // 1. work = centroids ++ buffer, stably sorted by mean
-  sp_sort_buffer(m, B, a.wpb);
+  sp_sort_buffer(m, B);
   if (threadIdx.x == 0) sh.unsorted = 0;
   __syncthreads();
   for (int i = threadIdx.x; i + 1 < C; i += SP_T)
@@ -242,55 +433,163 @@ __device__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh) {
       if (kd_order_key(m.cm[mid]) <= v) lo = mid + 1;
       else hi = mid;
     }
-    m.sm[j + lo] = m.bm[m.sidx[j]];
-    m.sw[j + lo] = m.bw[m.sidx[j]];
+    const unsigned si = m.sidx[j];
+    if (si >= (unsigned)B) {  // a sort that lost an element: fail, never read past the buffer
+      sh.err = KD_ECUDA;
+      continue;
+    }
+    m.sm[j + lo] = m.bm[si];
+    m.sw[j + lo] = m.bw[si];
   }
+  __syncthreads();
+  if (sh.err) return;
   const int W = C + B;
   // 2. totals: k limits use the effective total, q positions the stored one
   if (threadIdx.x == 0) {
-    const double eff = decay ? KD_MUL(sh.st, kd_exp(-sh.ls)) : sh.st;
-    sh.nrm = kd_normalizer(scale, a.s.compression, eff);
+    if (scale <= KD_SCALE_K1) {
+      sh.nrm = sh.nrm01;
+    } else {
+      const double eff = decay ? KD_MUL(sh.st, kd_exp(-sh.ls)) : sh.st;
+      sh.nrm = kd_normalizer(scale, a.s.compression, eff);
+    }
     sh.B = 0;
     sh.exact = 1;
     sh.mismatch = 0;
   }
   __syncthreads();
   for (int i = threadIdx.x; i < W; i += SP_T) {
-    const double w = m.sw[i];
-    if (!(w == floor(w)) || w > SP_EXACT) sh.exact = 0;
+    long long x;
+    if (!sp_int53(m.sw[i], &x)) sh.exact = 0;
   }
   __syncthreads();
   const double st = sh.st, nrm = sh.nrm;
-  // 3. k at every prefix: exact q for integral weights, a speculation otherwise
-  sp_prefix(m.sw, m.rw, W, m.wsf);  // rw doubles as the prefix array here
-  if (threadIdx.x == 0 && sh.exact && !(m.rw[W] <= SP_EXACT)) sh.exact = 0;
-  for (int i = threadIdx.x; i <= W; i += SP_T) m.kk[i] = sp_k(scale, KD_DIV(m.rw[i], st), nrm);
+  // 3. k at every prefix.  Integral weights: the prefix is exact in integers,
+  //    so every q the sweep forms is known up front.  Otherwise a speculation.
+  const bool exact_w = sh.exact != 0;
+  if (exact_w) {
+    sp_iprefix(m.sw, m.pi, W, sh);
+    if (threadIdx.x == 0 && m.pi[W] > (1LL << 53)) sh.exact = 0;
+    __syncthreads();
+  }
+  const bool exact = sh.exact != 0;
+  if (threadIdx.x == 0) {
+    sh.filt = exact && (double)m.pi[W] <= st && st >= 1.0 && st <= 1e14;
+    if (sh.filt) {  // nrm * k(q, 1) rounds exactly as k(q, nrm) at q = 0 and 1
+      sh.k0 = KD_MUL(nrm, sh.f0);
+      sh.k1 = KD_MUL(nrm, sh.f1);
+    }
+  }
   __syncthreads();
-  // 4. the chain of cluster starts (warp 0)
+  SpFit fit;
+  fit.scale = scale;
+  fit.filt = sh.filt != 0;
+  // FP32 error bound: 3.3e-6 * nrm (K0, K1) and 1.8e-5 * nrm (K2, K3) on a
+  // difference; the undecided band is several times wider
+  fit.tau = (float)KD_MUL(nrm, scale <= KD_SCALE_K1 ? 0x1p-15 : 0x1p-13);
+  fit.st = st;
+  fit.nrm = nrm;
+  fit.k32 = reinterpret_cast<const float*>(m.kk);
+  fit.kk = m.kk;
+  fit.pi = m.pi;
+  if (fit.filt) {
+    float* k32 = reinterpret_cast<float*>(m.kk);
+    const float nrmf = (float)nrm, k0f = (float)sh.k0, k1f = (float)sh.k1;
+    for (int i = threadIdx.x; i <= W; i += SP_T) k32[i] = sp_k32(scale, m.pi[i], st, nrmf, k0f, k1f);
+  } else if (exact) {
+    for (int i = threadIdx.x; i <= W; i += SP_T)
+      m.kk[i] = sp_k(scale, KD_DIV((double)m.pi[i], st), nrm);
+  } else {
+    sp_prefix(m.sw, m.rw, W, m.wsf);
+    for (int i = threadIdx.x; i <= W; i += SP_T) m.kk[i] = sp_k(scale, KD_DIV(m.rw[i], st), nrm);
+  }
+  __syncthreads();
+  // 4. for every element as a cluster start, where that cluster would end:
+  //    candidates coalesce while the k span fits or their mean equals the start's
+  //    (then all between are equal, and so is the running mean)
+  const double* sm = m.sm;
+  const double* sw = m.sw;
+  // With FP32 k non-decreasing along the prefix (checked), the sure fits of a
+  // start form a prefix of its candidates, found by binary search; the
+  // candidates after it are tested one by one (exactly where undecided).
+  if (threadIdx.x == 0) sh.unsorted = 0;  // here: FP32 k not monotone
+  __syncthreads();
+  if (fit.filt)
+    for (int i = threadIdx.x; i < W; i += SP_T)
+      if (fit.k32[i + 1] < fit.k32[i]) sh.unsorted = 1;
+  __syncthreads();
+  const bool mono = fit.filt && !sh.unsorted;
+  const float sure = 1.0f - fit.tau;
+  for (int s0 = threadIdx.x; s0 < W; s0 += SP_T) {
+    double ks64 = __longlong_as_double(0x7ff8000000000000LL);  // not yet evaluated
+    const unsigned long long ms = kd_order_key(sm[s0]);
+    int j = s0 + 1, steps = 0;
+    while (j < W && steps < 64 && kd_order_key(sm[j]) == ms) {  // equal means coalesce
+      ++j;
+      ++steps;
+    }
+    if (steps < 64 && mono) {
+      const float k0 = fit.k32[s0];
+      int lo = j, hi = W;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (fit.k32[mid + 1] - k0 <= sure) lo = mid + 1;
+        else hi = mid;
+      }
+      j = lo;
+      steps = 0;
+    }
+    while (j < W && steps < 64) {
+      if (!(kd_order_key(sm[j]) == ms || fit.fits(s0, j, ks64))) break;
+      ++j;
+      ++steps;
+    }
+    m.nb[s0] = (j < W && steps >= 64) ? -1 : j;
+  }
+  __syncthreads();
+  // 5. the chain of cluster starts from element 0 (warp 0); a cluster longer
+  //    than the precomputed reach is scanned 32 candidates at a time
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
-    int s = 0, nc = 0;
+    const int* const nbp = m.nb;
+    int* const cstp = m.cst;
+    int s0 = 0, nc = 0;
     bool overflow = false;
-    while (s < W) {
+    while (s0 < W) {
+      // the common case: hop along precomputed reaches (one lane is enough)
+      if (lane == 0) {
+        while (s0 < W && nc < KD_TILE) {
+          const int b = nbp[s0];
+          if (b < 0) break;
+          cstp[nc++] = s0;
+          s0 = b;
+        }
+      }
+      s0 = __shfl_sync(0xffffffffu, s0, 0);
+      nc = __shfl_sync(0xffffffffu, nc, 0);
+      if (s0 >= W) break;
       if (nc >= KD_TILE) {
         overflow = true;
         break;
       }
-      if (lane == 0) m.cst[nc] = s;
+      if (lane == 0) cstp[nc] = s0;
       ++nc;
-      const double ks = m.kk[s], ms = m.sm[s];
-      int b = W;
-      for (int j0 = s + 1; j0 < W; j0 += 32) {
-        const int j = j0 + lane;
-        bool split = false;
-        if (j < W) split = !(KD_SUB(m.kk[j + 1], ks) <= 1.0 || m.sm[j] == ms);
-        const unsigned bal = __ballot_sync(0xffffffffu, split);
-        if (bal) {
-          b = j0 + __ffs(bal) - 1;
-          break;
+      int b = nbp[s0];
+      if (b < 0) {
+        double ks64 = __longlong_as_double(0x7ff8000000000000LL);
+        const unsigned long long ms = kd_order_key(sm[s0]);
+        b = W;
+        for (int j0 = s0 + 65; j0 < W; j0 += 32) {
+          const int j = j0 + lane;
+          bool split = false;
+          if (j < W) split = !(kd_order_key(sm[j]) == ms || fit.fits(s0, j, ks64));
+          const unsigned bal = __ballot_sync(0xffffffffu, split);
+          if (bal) {
+            b = j0 + __ffs(bal) - 1;
+            break;
+          }
         }
       }
-      s = b;
+      s0 = b;
     }
     if (lane == 0) {
       m.cst[overflow ? KD_TILE : nc] = W;
@@ -304,31 +603,56 @@ __device__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh) {
     __syncthreads();
     return;
   }
-  // 5. one thread per cluster: the running mean and weight, in order
-  //    (Centroid.add_sample, centroid.mojo:25-36)
-  const double* sm = m.sm;
-  const double* sw = m.sw;
-  for (int t = threadIdx.x; t < nc; t += SP_T) {
-    const int s = m.cst[t], e = m.cst[t + 1];
-    double cur_m = sm[s], cur_w = sw[s];
-    m.cid[s] = t;
-    for (int j = s + 1; j < e; ++j) {
-      m.rw[j] = cur_w;
-      const double nw = KD_ADD(cur_w, sw[j]);
-      cur_m = KD_ADD(cur_m, KD_MUL(KD_SUB(sm[j], cur_m), KD_DIV(sw[j], nw)));
-      cur_w = nw;
-      m.cid[j] = t;
+  // 6. each cluster's running mean and weight, in order (Centroid.add_sample,
+  //    centroid.mojo:25-36)
+  if (exact) {
+    // the running weight before element j is pi[j] - pi[start]: every ratio
+    // w / (cur_w + w) is known up front; only the mean stays a chain
+    for (int t = threadIdx.x; t < nc; t += SP_T)
+      for (int j = m.cst[t]; j < m.cst[t + 1]; ++j) m.cid[j] = m.cst[t];
+    __syncthreads();
+    for (int j = threadIdx.x; j < W; j += SP_T) {
+      const int s0 = m.cid[j];
+      if (j > s0) {
+        const long long d = m.pi[j + 1] - m.pi[s0];
+        m.rw[j] = (kd_bits(sw[j]) == 0x3ff0000000000000ULL && d < SP_RCP_N)
+                      ? a.rcp[d]  // 1 / d, computed once by the same division
+                      : KD_DIV(sw[j], (double)d);
+      }
     }
-    if (e < W) {
-      m.rw[e] = cur_w;
-      if (sm[e] == cur_m) sh.mismatch = 1;  // the reference coalesces an exact mean tie
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc; t += SP_T) {
+      const int s0 = m.cst[t], e = m.cst[t + 1];
+      double cur_m = sm[s0];
+      for (int j = s0 + 1; j < e; ++j) cur_m = KD_ADD(cur_m, KD_MUL(KD_SUB(sm[j], cur_m), m.rw[j]));
+      if (e < W && sm[e] == cur_m) sh.mismatch = 1;  // the reference coalesces an exact mean tie
+      m.cm[t] = cur_m;
+      m.cw[t] = (double)(m.pi[e] - m.pi[s0]);
     }
-    m.cm[t] = cur_m;
-    m.cw[t] = cur_w;
+    __syncthreads();
+  } else {
+    for (int t = threadIdx.x; t < nc; t += SP_T) {
+      const int s0 = m.cst[t], e = m.cst[t + 1];
+      double cur_m = sm[s0], cur_w = sw[s0];
+      m.cid[s0] = t;
+      for (int j = s0 + 1; j < e; ++j) {
+        m.rw[j] = cur_w;
+        const double nw = KD_ADD(cur_w, sw[j]);
+        cur_m = KD_ADD(cur_m, KD_MUL(KD_SUB(sm[j], cur_m), KD_DIV(sw[j], nw)));
+        cur_w = nw;
+        m.cid[j] = t;
+      }
+      if (e < W) {
+        m.rw[e] = cur_w;
+        if (sm[e] == cur_m) sh.mismatch = 1;
+      }
+      m.cm[t] = cur_m;
+      m.cw[t] = cur_w;
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  // 6. non-integral weights: re-check every decision with the chain's exact sums
-  if (!sh.exact && !sh.mismatch) {
+  // 7. non-integral weights: re-check every decision with the chain's exact sums
+  if (!exact && !sh.mismatch) {
     if (threadIdx.x == 0) {
       double acc = 0.0;
       for (int t = 0; t < nc; ++t) {
@@ -353,7 +677,7 @@ __device__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh) {
     }
     __syncthreads();
   }
-  // 7. mismatch: the reference loop, one thread
+  // 8. mismatch: the reference loop, one thread
   if (sh.mismatch) {
     if (threadIdx.x == 0) {
       double wsf = 0.0, cur_m = sm[0], cur_w = sw[0];
@@ -389,7 +713,7 @@ __device__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh) {
     __syncthreads();
     nc = sh.nc;
   }
-  // 8. prune decayed mass (tdigest.mojo:441-458)
+  // 9. prune decayed mass (tdigest.mojo:441-458)
   if (threadIdx.x == 0) {
     int c = nc;
     if (decay) {
@@ -487,8 +811,8 @@ __device__ void sp_reduce_minmax(SpPick& mn, SpPick& mx, SpPick* red) {
 // The add loop over samples [0, n_eff) (tdigest.mojo:153-175, 334-350): each
 // sample advances the clock, is buffered with its decay-scaled weight, and a
 // full buffer runs the merge pass.
-__device__ void sp_add(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_eff, SpPick* red,
-                       double* dred) {
+__device__ __noinline__ void sp_add_decay(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_eff,
+                             SpPick* red) {
   const bool decay = a.s.lambda > 0.0;
   const double lambda = a.s.lambda;
   const int L = a.s.buf_cap;
@@ -498,16 +822,16 @@ __device__ void sp_add(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_ef
     const int seg = (int)(n_eff - i < room ? n_eff - i : room);
     const int B0 = sh.B;
     // clock, decay exponent and renormalisation, in sample order
-    bool fast = false;
-    if (!decay) {
+    if (threadIdx.x == 0) {
       // Without decay the exponent never moves: the clock is the only chain.
       // Count clock: integral clocks below 2^52 add exactly, so clock + seg is
       // the sum of seg additions of 1.  Time clock: the latest timestamp wins,
       // the earliest of equal ones (strict comparisons).
-      fast = a.ts != nullptr || (sh.clock == floor(sh.clock) && fabs(sh.clock) < 4.0e15);
+      sh.fast = !decay && (a.ts != nullptr || (sh.clock == floor(sh.clock) &&
+                                               fabs(sh.clock) < 4.0e15));
     }
-    __syncthreads();  // every thread has read the clock before it moves
-    if (fast) {
+    __syncthreads();
+    if (sh.fast) {
       if (a.ts) {
         SpPick mx{kd_order_key(sh.clock), -1, sh.clock}, dummy{0, 0, 0.0};
         for (int k = threadIdx.x; k < seg; k += SP_T) {
@@ -570,7 +894,7 @@ __device__ void sp_add(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_ef
     for (int k = threadIdx.x; k < cut; k += SP_T) {
       const double w = a.wts ? a.wts[i + k] : 1.0;
       m.bm[B0 + k] = a.vals[i + k];
-      m.bw[B0 + k] = KD_MUL(w, decay ? kd_exp(m.sls[k]) : 1.0);
+      m.bw[B0 + k] = decay ? KD_MUL(w, kd_exp(m.sls[k])) : w;  // w * 1.0 == w
     }
     __syncthreads();
     // running min / max (reset by the first sample of an empty digest) and the
@@ -582,30 +906,27 @@ __device__ void sp_add(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_ef
         mn = SpPick{kd_order_key(sh.mn), -1, sh.mn};
         mx = SpPick{kd_order_key(sh.mx), -1, sh.mx};
       }
-      double part = 0.0;
+      long long part = 0;  // integral weights sum exactly in integers
       for (int k = threadIdx.x; k < cut; k += SP_T) {
         const double v = m.bm[B0 + k];
         const SpPick p{kd_order_key(v), (long long)k, v};
         mn = sp_pick_min(mn, p);
         mx = sp_pick_max(mx, p);
-        part = KD_ADD(part, m.bw[B0 + k]);
+        long long x = 0;
+        sp_int53(m.bw[B0 + k], &x);
+        part += x;
       }
       sp_reduce_minmax(mn, mx, red);
-      // an exact total: integral weights and total below 2^53 sum in any order
-      bool exact = sh.st == floor(sh.st) && sh.integral && !decay;
-      for (int o = 16; o > 0; o >>= 1) part = KD_ADD(part, __shfl_down_sync(0xffffffffu, part, o));
-      if ((threadIdx.x & 31) == 0) dred[threadIdx.x >> 5] = part;
-      __syncthreads();
+      const bool int_w = sh.integral && !decay;
+      const long long sum = int_w ? sp_isum(part, sh) : 0;
       if (threadIdx.x == 0) {
         sh.mn = mn.v;
         sh.mx = mx.v;
         double tot = sh.st;
-        if (exact) {
-          double sum = 0.0;
-          for (int t = 0; t < SP_T / 32; ++t) sum = KD_ADD(sum, dred[t]);
-          if (KD_ADD(tot, sum) <= SP_EXACT) tot = KD_ADD(tot, sum);
-          else exact = false;
-        }
+        // an exact total: integral weights and a total below 2^53 sum in any order
+        bool exact = int_w && tot == floor(tot) && tot >= 0.0 && tot <= 4503599627370496.0 &&
+                     sum <= (1LL << 52);
+        if (exact) tot = KD_ADD(tot, (double)sum);
         if (!exact) {
           tot = sh.st;
           for (int k = 0; k < cut; ++k) tot = KD_ADD(tot, m.bw[B0 + k]);
@@ -632,6 +953,95 @@ __device__ void sp_add(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_ef
   }
 }
 
+// Without decay the exponent never moves and nothing is pruned, so the clock
+// and the running min / max have no effect on any merge: they are settled once
+// for the whole call (count clock: integral clocks below 2^52 add exactly, so
+// clock + n is the sum of n additions of 1; time clock: the latest timestamp,
+// the earliest of equal ones; min / max: the first occurrence of the extreme,
+// reset by the first sample of an empty digest).  Per buffer fill only the
+// samples, the stored total and the merge remain.
+__device__ __noinline__ void sp_add_plain(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_eff,
+                             SpPick* red) {
+  const int L = a.s.buf_cap;
+  if (n_eff == 0) return;
+  {
+    const bool reset = sh.st == 0.0 && sh.B == 0;
+    SpPick mn{~0ull, 0x7fffffffffffffffLL, 0.0}, mx{0ull, 0x7fffffffffffffffLL, 0.0};
+    if (!reset && threadIdx.x == 0) {
+      mn = SpPick{kd_order_key(sh.mn), -1, sh.mn};
+      mx = SpPick{kd_order_key(sh.mx), -1, sh.mx};
+    }
+    for (long long k = threadIdx.x; k < n_eff; k += SP_T) {
+      const double v = a.vals[k];
+      const SpPick p{kd_order_key(v), k, v};
+      mn = sp_pick_min(mn, p);
+      mx = sp_pick_max(mx, p);
+    }
+    sp_reduce_minmax(mn, mx, red);
+    if (threadIdx.x == 0) {
+      sh.mn = mn.v;
+      sh.mx = mx.v;
+    }
+    if (a.ts) {
+      SpPick tm{kd_order_key(sh.clock), -1, sh.clock}, dummy{~0ull, -1, 0.0};
+      for (long long k = threadIdx.x; k < n_eff; k += SP_T) {
+        const double t = a.ts[k];
+        if (t == t) tm = sp_pick_max(tm, SpPick{kd_order_key(t), k, t});
+      }
+      sp_reduce_minmax(dummy, tm, red);
+      if (threadIdx.x == 0 && tm.seq >= 0 && tm.v > sh.clock) sh.clock = tm.v;
+    } else if (threadIdx.x == 0) {
+      if (sh.clock == floor(sh.clock) && fabs(sh.clock) < 4.0e15 && n_eff < (1LL << 40)) {
+        sh.clock = KD_ADD(sh.clock, (double)n_eff);
+      } else {
+        double c = sh.clock;
+        for (long long k = 0; k < n_eff; ++k) c = KD_ADD(c, 1.0);
+        sh.clock = c;
+      }
+    }
+    __syncthreads();
+  }
+  long long i = 0;
+  while (i < n_eff && !sh.err) {
+    const int B0 = sh.B;
+    const long long room = (long long)(L - B0);
+    const int cut = (int)(n_eff - i < room ? n_eff - i : room);
+    long long part = 0;
+    for (int k = threadIdx.x; k < cut; k += SP_T) {
+      const double w = a.wts ? a.wts[i + k] : 1.0;  // w * e^0 == w
+      m.bm[B0 + k] = a.vals[i + k];
+      m.bw[B0 + k] = w;
+      long long x = 0;
+      sp_int53(w, &x);
+      part += x;
+    }
+    const long long sum = sh.integral ? sp_isum(part, sh) : 0;  // synchronises
+    if (!sh.integral) __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = sh.st;
+      // integral weights and a total below 2^53 sum exactly in any order
+      const bool exact = sh.integral && tot == floor(tot) && tot >= 0.0 &&
+                         tot <= 4503599627370496.0 && sum <= (1LL << 52);
+      if (exact) {
+        tot = KD_ADD(tot, (double)sum);
+      } else {
+        for (int k = 0; k < cut; ++k) tot = KD_ADD(tot, m.bw[B0 + k]);
+      }
+      sh.st = tot;
+      sh.B = B0 + cut;
+    }
+    __syncthreads();
+    i += cut;
+    if (sh.B >= L) sp_merge(a, m, sh);
+    __syncthreads();
+  }
+}
+
+__device__ void sp_add(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_eff, SpPick* red) {
+  if (a.s.lambda > 0.0) sp_add_decay(a, m, sh, n_eff, red);
+  else sp_add_plain(a, m, sh, n_eff, red);
+}
+
 // Writes the call's result to the store: new centroids into the back slot,
 // the quantile-walk prefix, the header and the buffer; then flips the slot.
 __device__ void sp_commit(const SpArgs& a, const SpMem& m, SpSh& sh) {
@@ -649,10 +1059,26 @@ __device__ void sp_commit(const SpArgs& a, const SpMem& m, SpSh& sh) {
     s.buf_m[i] = m.bm[i];
     s.buf_w[i] = m.bw[i];
   }
+  // The quantile-walk prefix, the same arithmetic as the batch path's commit:
+  // P[0] = w0/2, P[i+1] = P[i] + (w_i + w_{i+1})/2.  With integral weights
+  // below 2^52 every step is exact, so P[i] = (w_0 + ... + w_{i-1}) + w_i/2.
+  if (threadIdx.x == 0) sh.exact = 1;
   __syncthreads();
+  long long wi = 0;
+  if (threadIdx.x < C && !sp_int53(m.cw[threadIdx.x], &wi)) sh.exact = 0;
+  __syncthreads();
+  const bool int_p = sh.exact && C <= SP_T;
+  if (int_p) {
+    long long total;
+    const long long excl = sp_iscan(wi, sh, &total);
+    if (total <= (1LL << 52) && threadIdx.x < C)
+      s.prefix[threadIdx.x] = KD_ADD((double)excl, KD_MUL(m.cw[threadIdx.x], 0.5));
+    if (threadIdx.x == 0 && total > (1LL << 52)) sh.exact = 0;
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
-    double* P = s.prefix;  // the same walk prefix as the batch path's commit
-    if (C > 0) {
+    double* P = s.prefix;
+    if (C > 0 && !(int_p && sh.exact)) {
       double run = KD_MUL(m.cw[0], 0.5);
       P[0] = run;
       for (int i = 0; i + 1 < C; ++i) {
@@ -705,7 +1131,6 @@ __global__ void __launch_bounds__(SP_T) k_spath(SpArgs a) {
   extern __shared__ __align__(256) unsigned char sp_smem[];
   __shared__ SpSh sh;
   __shared__ SpPick red[64];
-  __shared__ double dred[SP_T / 32];
   SpMem m;
   sp_layout(a.bmax, a.wpb, a.scratch ? a.scratch : sp_smem, &m);
   const KdStoreDev& s = a.s;
@@ -724,6 +1149,11 @@ __global__ void __launch_bounds__(SP_T) k_spath(SpArgs a) {
     sh.first_bad = a.n;
     sh.integral = 1;
     a.out->noop = 0;
+    sh.f0 = sp_k(s.scale, 0.0, 1.0);
+  } else if (threadIdx.x == 32) {
+    sh.f1 = sp_k(s.scale, 1.0, 1.0);
+  } else if (threadIdx.x == 64) {
+    sh.nrm01 = s.scale <= KD_SCALE_K1 ? kd_normalizer(s.scale, s.compression, 1.0) : 0.0;
   }
   __syncthreads();
   {
@@ -746,10 +1176,11 @@ __global__ void __launch_bounds__(SP_T) k_spath(SpArgs a) {
       const double w = a.wts ? a.wts[i] : 1.0;
       const bool bad = !kd_isfinite(v) || !(w > 0.0) || !kd_isfinite(w);
       if (bad) atomicMin((unsigned long long*)&sh.first_bad, (unsigned long long)i);
-      if (!(w == floor(w)) || w > SP_EXACT) sh.integral = 0;
+      long long x;
+      if (!sp_int53(w, &x)) sh.integral = 0;
     }
     __syncthreads();
-    sp_add(a, m, sh, sh.first_bad, red, dred);
+    sp_add(a, m, sh, sh.first_bad, red);
     if (threadIdx.x == 0 && !sh.err && sh.first_bad < a.n) {
       a.out->code = KD_EINVAL;
       a.out->index = sh.first_bad;
@@ -807,6 +1238,15 @@ __global__ void __launch_bounds__(SP_T) k_spath(SpArgs a) {
     return;
   }
   sp_commit(a, m, sh);
+}
+
+// 1 / d for the unit-weight ratios of the merge pass, made once per device by
+// the same correctly rounded division the pass would run.
+__device__ double sp_rcp_table[SP_RCP_N];
+
+__global__ void k_rcp_init() {
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < SP_RCP_N; d += gridDim.x * blockDim.x)
+    sp_rcp_table[d] = d == 0 ? 0.0 : KD_DIV(1.0, (double)d);
 }
 
 int sp_fail(KdSession* s, int code, const char* msg) {
@@ -894,6 +1334,19 @@ int sp_run(KdSession* s, KdStore* st, int op, const double* d_vals, const double
     if (e != cudaSuccess) return kd_cuda_fail(s, e, "single-sample path attributes");
     attr_done[dev] = true;
   }
+  static std::atomic<bool> rcp_done[64];
+  static const double* rcp_ptr[64];
+  if (dev < 0 || dev >= 64) return sp_fail(s, KD_EINVAL, "device ordinal out of range");
+  if (!rcp_done[dev].load()) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, sp_rcp_table);
+    if (e != cudaSuccess) return kd_cuda_fail(s, e, "reciprocal table");
+    k_rcp_init<<<64, 256, 0, s->stream>>>();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return kd_cuda_fail(s, e, "reciprocal table");
+    rcp_ptr[dev] = (const double*)p;
+    rcp_done[dev].store(true);
+  }
   SpStatus* dstat = sp_status(st);
   SpArgs a;
   a.s = d;
@@ -906,6 +1359,7 @@ int sp_run(KdSession* s, KdStore* st, int op, const double* d_vals, const double
   a.bmax = shp.bmax;
   a.wpb = shp.wpb;
   a.scratch = scratch;
+  a.rcp = rcp_ptr[dev];
   a.out = dstat;
   cudaStream_t str = s->stream;
   cudaError_t e = cudaMemsetAsync(dstat, 0, sizeof(SpStatus), str);
@@ -926,6 +1380,8 @@ int sp_after(KdSession* s, KdStore* st, const SpStatus& r) {
   if (r.code == KD_ERANGE) {
     return sp_fail(s, KD_ERANGE, "a merge pass produced more than 1024 centroids");
   }
+  if (r.code != KD_OK && r.code != KD_EINVAL)
+    return sp_fail(s, r.code, "single-sample path: internal consistency check failed");
   if (!r.noop && r.code != KD_ERANGE) {
     st->pending = r.bcount > 0;
     st->carry = true;
