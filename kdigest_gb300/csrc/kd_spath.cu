@@ -1299,7 +1299,7 @@ SpShape sp_shape(const KdStoreDev& d) {
   return sh;
 }
 
-constexpr size_t SP_SMEM_MAX = 160 * 1024;  // beyond this the state lives in global scratch
+constexpr size_t SP_SMEM_MAX = 220 * 1024;  // beyond this the state lives in global scratch
 
 // The call's status block sits behind the buffer count in the same allocation.
 SpStatus* sp_status(KdStore* st) {

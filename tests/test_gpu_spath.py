@@ -229,3 +229,29 @@ def test_pending_buffer_reads(kd, oracle):
     r.add_batch(big)
     orr.add_batch_p(big)
     _same(r, orr)
+
+
+@pytest.mark.parametrize("scale", [2, 3])
+def test_long_streams_k2_k3(kd, oracle, scale):
+    """Normalisers that grow with the total (K2, K3) over 600,000 samples."""
+    d = kd.TDigest(150.0, scale)
+    od = oracle.Digest(scale, 150.0, 0.0)
+    rng = np.random.default_rng(20 + scale)
+    v = rng.lognormal(0, 2.0, 600_000)
+    for b in range(0, len(v), 5000):
+        d.add_batch(v[b:b + 5000])
+        od.add_many(v[b:b + 5000])
+    _same(d, od)
+    _same_queries(d, od, xs=(0.01, 0.5, 1.0, 4.0, 100.0))
+
+
+def test_tiny_compression_merges_every_sample(kd, oracle):
+    """int(compression) * 5 below 1: the buffer limit is one sample."""
+    d = kd.TDigest(0.15, kd.K1)
+    od = oracle.Digest(oracle.K1, 0.15, 0.0)
+    rng = np.random.default_rng(30)
+    v = rng.standard_normal(300)
+    d.add_batch(v)
+    od.add_many(v)
+    _same(d, od)
+    _same_queries(d, od)
