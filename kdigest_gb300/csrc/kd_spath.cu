@@ -81,6 +81,8 @@ struct SpMem {
   int* nb;          // next cluster start after each possible start [KD_TILE + bmax]
   double* sls;      // log-scale of each sample of a segment [bmax]
   double *wsf, *kl;  // weight before each cluster and its k [KD_TILE + 1]
+  unsigned long long* pk;  // buffers sorted ahead of their merge [SP_T]
+  unsigned* px;
 };
 
 __host__ __device__ inline size_t sp_align(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -111,6 +113,8 @@ __host__ __device__ inline size_t sp_layout(int bmax, int wpb, unsigned char* ba
   t.sls = (double*)take(8 * (size_t)bmax);
   t.wsf = (double*)take(8 * (KD_TILE + 1));
   t.kl = (double*)take(8 * (KD_TILE + 1));
+  t.pk = (unsigned long long*)take(8 * 1024);
+  t.px = (unsigned*)take(4 * 1024);
   if (m) *m = t;
   return off;
 }
@@ -296,6 +300,64 @@ __device__ void sp_iprefix(const double* v, long long* out, int n, SpSh& sh) {
 // (order key, position), so equal values (and -0.0 / +0.0) keep their order.
 // Up to one element per thread the keys stay in registers: strides below 32
 // exchange through warp shuffles, larger ones through shared memory.
+// Sorts blocks of P consecutive threads' (key, idx) pairs, each block on its
+// own (P a power of two, threads [0, nthr) hold elements, nthr a multiple of P
+// or P itself): 32-element runs in registers (bitonic over warp shuffles), then
+// runs merged pairwise.  Keys are distinct (value key, then position; the
+// padding has positions of its own), so an element's place in a merged run is
+// its place in its own run plus the number of partner-run elements before it.
+// The sorted blocks land in okey / sidx [0, nthr).
+__device__ __forceinline__ void sp_sort_regs(unsigned long long key, unsigned idx, int P, int nthr,
+                                             unsigned long long* okey, unsigned* sidx) {
+  const int i = threadIdx.x;
+  const int R = P < 32 ? P : 32;
+  const bool warp_on = (i & ~31) < nthr;
+  if (warp_on) {
+    const int lane = i & 31;  // every run ends ascending
+    for (int k = 2; k <= R; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, j);
+        const unsigned oi = __shfl_xor_sync(0xffffffffu, idx, j);
+        const bool up = (lane & k) == 0;
+        const bool lower = (lane & j) == 0;
+        const bool other_less = ok < key || (ok == key && oi < idx);
+        if ((lower == up) == other_less) {
+          key = ok;
+          idx = oi;
+        }
+      }
+    }
+  }
+  if (i < nthr) {
+    okey[i] = key;
+    sidx[i] = idx;
+  }
+  __syncthreads();
+  int at = i;  // where this thread's element sits
+  for (int run = 32; run < P; run <<= 1) {
+    int pos = 0;
+    if (i < nthr) {
+      const int base = (at / run) * run;
+      const int other = base ^ run;
+      int lo = 0, hi = run;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const unsigned long long ok = okey[other + mid];
+        if (ok < key || (ok == key && sidx[other + mid] < idx)) lo = mid + 1;
+        else hi = mid;
+      }
+      pos = (base < other ? base : other) + (at - base) + lo;
+    }
+    __syncthreads();
+    if (i < nthr) {
+      okey[pos] = key;
+      sidx[pos] = idx;
+      at = pos;
+    }
+    __syncthreads();
+  }
+}
+
 __device__ __forceinline__ void sp_sort_buffer(const SpMem& m, int B) {
   int P = 1;
   while (P < B) P <<= 1;
@@ -326,75 +388,31 @@ __device__ __forceinline__ void sp_sort_buffer(const SpMem& m, int B) {
     }
     return;
   }
-  // One element per thread: 32-element runs sorted in registers (bitonic over
-  // warp shuffles), then runs merged pairwise.  Keys are distinct (value key,
-  // then position; the padding has positions of its own), so an element's place
-  // in a merged run is its place in its own run plus the number of partner-run
-  // elements before it.
   const int i = threadIdx.x;
-  const int R = P < 32 ? P : 32;
-  const bool warp_on = (i & ~31) < P;
   unsigned long long key = ~0ull;
   unsigned idx = 0x80000000u | (unsigned)i;
   if (i < B) {
     key = kd_order_key(m.bm[i]);
     idx = (unsigned)i;
   }
-  if (warp_on) {
-    const int lane = i & 31;  // every run of 32 ends ascending
-    for (int k = 2; k <= R; k <<= 1) {
-      for (int j = k >> 1; j > 0; j >>= 1) {
-        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, j);
-        const unsigned oi = __shfl_xor_sync(0xffffffffu, idx, j);
-        const bool up = (lane & k) == 0;
-        const bool lower = (lane & j) == 0;
-        const bool other_less = ok < key || (ok == key && oi < idx);
-        if ((lower == up) == other_less) {
-          key = ok;
-          idx = oi;
-        }
-      }
-    }
-  }
-  if (i < P) {
-    m.okey[i] = key;
-    m.sidx[i] = idx;
-  }
-  __syncthreads();
-  int at = i;  // where this thread's element sits
-  for (int run = 32; run < P; run <<= 1) {
-    int pos = 0;
-    if (i < P) {
-      const int base = (at / run) * run;
-      const int other = base ^ run;
-      int lo = 0, hi = run;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        const unsigned long long ok = m.okey[other + mid];
-        if (ok < key || (ok == key && m.sidx[other + mid] < idx)) lo = mid + 1;
-        else hi = mid;
-      }
-      pos = (base < other ? base : other) + (at - base) + lo;
-    }
-    __syncthreads();
-    if (i < P) {
-      m.okey[pos] = key;
-      m.sidx[pos] = idx;
-      at = pos;
-    }
-    __syncthreads();
-  }
+  sp_sort_regs(key, idx, P, P < 32 ? 32 : P, m.okey, m.sidx);
 }
 
 // The merge pass (tdigest.mojo:391-439, _prune :441-458) over C centroids and
 // B buffered samples in shared state.  Leaves the new centroids in cm/cw.
-__device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh) {
+// pk / px: the buffer's sorted order when it was sorted ahead (else null).
+__device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
+                                      const unsigned long long* pk, const unsigned* px) {
   const int B = sh.B, C = sh.C;
   if (B == 0) return;
   const int scale = a.s.scale;
   const bool decay = a.s.lambda > 0.0;
   // 1. work = centroids ++ buffer, stably sorted by mean
-  sp_sort_buffer(m, B);
+  if (!pk) {
+    sp_sort_buffer(m, B);
+    pk = m.okey;
+    px = m.sidx;
+  }
   if (threadIdx.x == 0) sh.unsorted = 0;
   __syncthreads();
   for (int i = threadIdx.x; i + 1 < C; i += SP_T)
@@ -419,21 +437,21 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh)
     int lo = 0, hi = B;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
-      if (m.okey[mid] < v) lo = mid + 1;
+      if (pk[mid] < v) lo = mid + 1;
       else hi = mid;
     }
     m.sm[i + lo] = m.cm[i];
     m.sw[i + lo] = m.cw[i];
   }
   for (int j = threadIdx.x; j < B; j += SP_T) {
-    const unsigned long long v = m.okey[j];
+    const unsigned long long v = pk[j];
     int lo = 0, hi = C;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
       if (kd_order_key(m.cm[mid]) <= v) lo = mid + 1;
       else hi = mid;
     }
-    const unsigned si = m.sidx[j];
+    const unsigned si = px[j];
     if (si >= (unsigned)B) {  // a sort that lost an element: fail, never read past the buffer
       sh.err = KD_ECUDA;
       continue;
@@ -948,9 +966,40 @@ __device__ __noinline__ void sp_add_decay(const SpArgs& a, const SpMem& m, SpSh&
       }
       __syncthreads();
     }
-    if (sh.B >= L) sp_merge(a, m, sh);
+    if (sh.B >= L) sp_merge(a, m, sh, nullptr, nullptr);
     __syncthreads();
   }
+}
+
+// Buffers samples [i, i + cut) of the call (weights w * e^0 == w) and adds them
+// to the stored total: exactly in integers when every weight is one and the
+// total stays below 2^53, else in sample order.
+__device__ void sp_append(const SpArgs& a, const SpMem& m, SpSh& sh, long long i, int cut) {
+  const int B0 = sh.B;
+  long long part = 0;
+  for (int k = threadIdx.x; k < cut; k += SP_T) {
+    const double w = a.wts ? a.wts[i + k] : 1.0;
+    m.bm[B0 + k] = a.vals[i + k];
+    m.bw[B0 + k] = w;
+    long long x = 0;
+    sp_int53(w, &x);
+    part += x;
+  }
+  const long long sum = sh.integral ? sp_isum(part, sh) : 0;  // synchronises
+  if (!sh.integral) __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = sh.st;
+    const bool exact = sh.integral && tot == floor(tot) && tot >= 0.0 &&
+                       tot <= 4503599627370496.0 && sum <= (1LL << 52);
+    if (exact) {
+      tot = KD_ADD(tot, (double)sum);
+    } else {
+      for (int k = 0; k < cut; ++k) tot = KD_ADD(tot, m.bw[B0 + k]);
+    }
+    sh.st = tot;
+    sh.B = B0 + cut;
+  }
+  __syncthreads();
 }
 
 // Without decay the exponent never moves and nothing is pruned, so the clock
@@ -1001,38 +1050,42 @@ __device__ __noinline__ void sp_add_plain(const SpArgs& a, const SpMem& m, SpSh&
     }
     __syncthreads();
   }
+  // Two full buffers at a time are sorted ahead, each by half the block, when
+  // a buffer fits 512 entries: a sort is latency-bound, so two run for one.
+  int Lp = 1;
+  while (Lp < L) Lp <<= 1;
+  const bool pairs = 2 * Lp <= SP_T;
   long long i = 0;
   while (i < n_eff && !sh.err) {
     const int B0 = sh.B;
     const long long room = (long long)(L - B0);
-    const int cut = (int)(n_eff - i < room ? n_eff - i : room);
-    long long part = 0;
-    for (int k = threadIdx.x; k < cut; k += SP_T) {
-      const double w = a.wts ? a.wts[i + k] : 1.0;  // w * e^0 == w
-      m.bm[B0 + k] = a.vals[i + k];
-      m.bw[B0 + k] = w;
-      long long x = 0;
-      sp_int53(w, &x);
-      part += x;
-    }
-    const long long sum = sh.integral ? sp_isum(part, sh) : 0;  // synchronises
-    if (!sh.integral) __syncthreads();
-    if (threadIdx.x == 0) {
-      double tot = sh.st;
-      // integral weights and a total below 2^53 sum exactly in any order
-      const bool exact = sh.integral && tot == floor(tot) && tot >= 0.0 &&
-                         tot <= 4503599627370496.0 && sum <= (1LL << 52);
-      if (exact) {
-        tot = KD_ADD(tot, (double)sum);
-      } else {
-        for (int k = 0; k < cut; ++k) tot = KD_ADD(tot, m.bw[B0 + k]);
+    if (pairs && n_eff - i >= room + L) {
+      const int t = threadIdx.x, blk = t / Lp, loc = t - blk * Lp;
+      unsigned long long key = ~0ull;
+      unsigned idx = 0x80000000u | (unsigned)t;
+      if (blk < 2 && loc < L) {
+        // buffer A: the waiting samples, then the next `room` ones; buffer B:
+        // the L samples after those (each in insertion order)
+        const double v = blk == 0 ? (loc < B0 ? m.bm[loc] : a.vals[i + loc - B0])
+                                  : a.vals[i + room + loc];
+        key = kd_order_key(v);
+        idx = (unsigned)loc;
       }
-      sh.st = tot;
-      sh.B = B0 + cut;
+      sp_sort_regs(key, idx, Lp, 2 * Lp, m.pk, m.px);
+      sp_append(a, m, sh, i, (int)room);
+      sp_merge(a, m, sh, m.pk, m.px);
+      __syncthreads();
+      if (sh.err) break;
+      sp_append(a, m, sh, i + room, L);
+      sp_merge(a, m, sh, m.pk + Lp, m.px + Lp);
+      __syncthreads();
+      i += room + L;
+      continue;
     }
-    __syncthreads();
+    const int cut = (int)(n_eff - i < room ? n_eff - i : room);
+    sp_append(a, m, sh, i, cut);
     i += cut;
-    if (sh.B >= L) sp_merge(a, m, sh);
+    if (sh.B >= L) sp_merge(a, m, sh, nullptr, nullptr);
     __syncthreads();
   }
 }
@@ -1186,7 +1239,7 @@ __global__ void __launch_bounds__(SP_T) k_spath(SpArgs a) {
       a.out->index = sh.first_bad;
     }
   } else if (a.op == SP_FLUSH) {
-    sp_merge(a, m, sh);
+    sp_merge(a, m, sh, nullptr, nullptr);
   } else {  // SP_MERGE_INTO (tdigest.mojo:589-623)
     const KdStoreDev& o = a.o;
     const double o_st = o.total[0], o_ls = o.log_scale[0];
@@ -1195,7 +1248,7 @@ __global__ void __launch_bounds__(SP_T) k_spath(SpArgs a) {
       if (threadIdx.x == 0) a.out->noop = 1;
       return;
     }
-    sp_merge(a, m, sh);
+    sp_merge(a, m, sh, nullptr, nullptr);
     if (s.lambda > 0.0) sp_renormalize(m, sh);
     double o_total = o_st;
     if (o.lambda > 0.0) {
@@ -1227,7 +1280,7 @@ __global__ void __launch_bounds__(SP_T) k_spath(SpArgs a) {
       sh.clock = sh.clock > o.clock[0] ? sh.clock : o.clock[0];
     }
     __syncthreads();
-    sp_merge(a, m, sh);
+    sp_merge(a, m, sh, nullptr, nullptr);
   }
   __syncthreads();
   if (sh.err) {
