@@ -360,6 +360,74 @@ def run_config1(args) -> int:
 
 
 # ----------------------------------------------------------------------------
+# Key dictionary (no reference counterpart; the reference takes dense ids):
+# 2^25 64-bit keys drawn Zipf(1.1) from 65,536 distinct random keys, mapped to
+# dense ids on the device, then the same keys ingested through their ids.
+# ----------------------------------------------------------------------------
+KM_KEYS = 1 << 25
+
+
+def run_keymap(args) -> int:
+    import torch
+
+    import kdigest_gb300 as kd
+    from kdigest_gb300 import _native as N
+
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(SEED + 9)
+    pool = np.unique(rng.integers(0, 2**64 - 1, NUM_KEYS + 64, dtype=np.uint64))[:NUM_KEYS]
+    rank = (rng.zipf(1.1, KM_KEYS) - 1) % NUM_KEYS
+    keys = torch.from_numpy(pool[rank].view(np.int64)).to(dev)
+    sess = kd.GpuSession()
+    ext = torch.cuda.ExternalStream(sess.stream, device=dev)
+    L = N.load()
+    m = kd.KeyDictionary(2 * NUM_KEYS, session=sess)
+    ids = torch.empty(KM_KEYS, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):  # the first call inserts every key
+        rc = L.kd_keymap_map(m._h, keys.data_ptr(), KM_KEYS, ids.data_ptr(), N.KD_PTR_DEVICE)
+        if rc:
+            raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+    steps = max(3, min(args.steps, 10))
+    times = []
+    for _ in range(steps):  # inputs (384 MB per call) exceed L2
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        rc = L.kd_keymap_map(m._h, keys.data_ptr(), KM_KEYS, ids.data_ptr(), N.KD_PTR_DEVICE)
+        e1.record(ext)
+        e1.synchronize()
+        if rc:
+            raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    # ids are a bijection onto [0, len) and agree with a host dictionary's classes
+    h_ids = ids.cpu().numpy().view(np.uint32)
+    first = {}
+    ok = len(m) == len(np.unique(rank))
+    for k, i in zip(rank[:200000].tolist(), h_ids[:200000].tolist()):
+        ok = ok and first.setdefault(k, i) == i
+    peaks = measured_peaks()
+    achieved = 12.0 * KM_KEYS / (ms / 1e3) / 1e9
+    line = {
+        "metric": "key-dictionary map keys/s (64-bit keys to dense ids, all present)",
+        "value": KM_KEYS / (ms / 1e3), "unit": "keys/s", "n_gpus": 1, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded numpy, Zipf(1.1) over "
+        "65,536 random 64-bit keys), resident in HBM",
+        "config": {"workload": "kd_keymap_map of 2^25 keys, 65,536 distinct", "keys": KM_KEYS,
+                   "distinct": int(len(m)), "l2": "inputs and outputs (384 MB) exceed L2"},
+        "consistent_ids": bool(ok),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "peak_source": peaks["source"],
+                     "algorithmic_bytes_per_key": 12},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
 # Config 2: one K2 digest (compression 200), Decay.half_life(1e6 samples),
 # 2^26 lognormal(mu_t, 1.5) samples with mu_t drifting 0 -> 2, batches of 2^20,
 # then 4096 quantiles (2048 uniform, 1024 log-uniform in [1e-6, 1e-2] and their
@@ -1018,6 +1086,8 @@ def main():
     ap.add_argument("--serve-window", type=float, default=1e-3)
     ap.add_argument("--serve-rate", type=float, default=SERVE_RATE)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--keymap", action="store_true",
+                    help="run only the key-dictionary benchmark and print its line")
     ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4],
                     help="1: single digest, small batches; 2: single decayed digest; "
                          "3: grouped ingest (the headline); 4: batched merge and query")
@@ -1030,6 +1100,8 @@ def main():
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.keymap:
+        return run_keymap(args)
     if args.config == 1:
         return run_config1(args)
     if args.config == 2:

@@ -55,7 +55,10 @@ __device__ unsigned probe(unsigned long long* __restrict__ tk, unsigned* __restr
                           unsigned long long k, bool insert, KdErrHost* err, long long i) {
   unsigned long long h = mix64(k) & (unsigned long long)(size - 1);
   for (long long step = 0; step < size; ++step, h = (h + 1) & (unsigned long long)(size - 1)) {
-    unsigned long long cur = *(volatile unsigned long long*)&tk[h];
+    // A plain (L1-cached) read: a stale "empty" only sends the thread to the
+    // compare-and-swap, which reads the slot's real value; a slot never
+    // changes once it holds a key.  Hot keys then stay in every SM's L1.
+    unsigned long long cur = tk[h];
     if (cur == KD_KEYMAP_EMPTY) {
       if (!insert) return KD_KEYMAP_NOID;
       cur = atomicCAS(&tk[h], KD_KEYMAP_EMPTY, k);
@@ -72,6 +75,12 @@ __device__ unsigned probe(unsigned long long* __restrict__ tk, unsigned* __restr
       }
     }
     if (cur == k) {  // present: wait (bounded) until its id is published
+      const unsigned id0 = ti[h];  // a published id never changes
+      if (id0 == KD_KEYMAP_NOID - 1) {
+        if (insert && atomicCAS(&err->code, 0, KD_ENOMEM) == 0) err->index = i;
+        return KD_KEYMAP_NOID;
+      }
+      if (id0 != KD_KEYMAP_NOID) return id0;
       for (int spin = 0; spin < KD_KEYMAP_SPIN_LIMIT; ++spin) {
         const unsigned id = *(volatile unsigned*)&ti[h];
         if (id == KD_KEYMAP_NOID - 1) {  // stored when the map was already full
