@@ -128,6 +128,7 @@ struct SpSh {
   double f0, f1;  // the same with normaliser 1: k(q, nrm) = nrm * k(q, 1) at these q
   double nrm01;   // the K0 / K1 normaliser (it does not depend on the total)
   int C, B, err, nc, mismatch, unsorted, exact, cut, renorm, pre_adv, integral, fast, filt;
+  int longreach;  // a cluster start whose reach passed 64 candidates
   long long wsum[32];  // per-warp partial sums of block scans and reductions
 };
 
@@ -473,6 +474,7 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
     sh.B = 0;
     sh.exact = 1;
     sh.mismatch = 0;
+    sh.longreach = 0;
   }
   __syncthreads();
   for (int i = threadIdx.x; i < W; i += SP_T) {
@@ -562,11 +564,60 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
       ++steps;
     }
     m.nb[s0] = (j < W && steps >= 64) ? -1 : j;
+    if (j < W && steps >= 64) sh.longreach = 1;
   }
   __syncthreads();
-  // 5. the chain of cluster starts from element 0 (warp 0); a cluster longer
-  //    than the precomputed reach is scanned 32 candidates at a time
-  if (threadIdx.x < 32) {
+  // 5. the chain of cluster starts from element 0.  With every reach known, the
+  //    chain comes from jump tables J_k(s) = next^(2^k)(s): each lane of warp 0
+  //    takes one of 32 consecutive hops at once.  J_0 is the reach array, J_1 to
+  //    J_4 (16-bit) live in the k array, which the chain no longer needs.
+  const bool jumps = !sh.longreach && W + 1 <= 65535;
+  if (jumps) {
+    unsigned short* J = reinterpret_cast<unsigned short*>(m.kk);
+    const int stride = W + 1;
+    for (int k = 1; k <= 4; ++k) {
+      for (int x = threadIdx.x; x <= W; x += SP_T) {
+        int y;
+        if (k == 1) {
+          const int a1 = x < W ? m.nb[x] : W;
+          y = a1 < W ? m.nb[a1] : W;
+        } else {
+          const unsigned short* P = J + (size_t)(k - 2) * stride;
+          y = P[P[x]];
+        }
+        J[(size_t)(k - 1) * stride + x] = (unsigned short)y;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x < 32) {
+      const int lane = threadIdx.x;
+      int base = 0, nc = 0;
+      bool overflow = false;
+      while (base < W) {
+        int x = base;  // next^lane(base)
+        if (lane & 1) x = x < W ? m.nb[x] : W;
+        for (int k = 1; k <= 4; ++k)
+          if ((lane >> k) & 1) x = J[(size_t)(k - 1) * stride + x];
+        const unsigned valid = __ballot_sync(0xffffffffu, x < W);
+        const int cnt = __popc(valid);  // the chain increases, so the valid lanes lead
+        if (nc + cnt > KD_TILE) {
+          overflow = true;
+          break;
+        }
+        if (x < W) m.cst[nc + lane] = x;
+        nc += cnt;
+        const int last = __shfl_sync(0xffffffffu, x, 31);
+        base = last < W ? m.nb[last] : W;
+      }
+      if (lane == 0) {
+        m.cst[overflow ? KD_TILE : nc] = W;
+        sh.nc = overflow ? -1 : nc;
+      }
+    }
+  }
+  // otherwise one lane hops along the reaches; a cluster longer than the
+  // precomputed reach is scanned 32 candidates at a time
+  if (!jumps && threadIdx.x < 32) {
     const int lane = threadIdx.x;
     const int* const nbp = m.nb;
     int* const cstp = m.cst;
