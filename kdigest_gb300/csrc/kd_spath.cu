@@ -129,6 +129,7 @@ struct SpSh {
   double nrm01;   // the K0 / K1 normaliser (it does not depend on the total)
   int C, B, err, nc, mismatch, unsorted, exact, cut, renorm, pre_adv, integral, fast, filt;
   int longreach;  // a cluster start whose reach passed 64 candidates
+  int bfail;      // a bucket of the buffer merge was too large
   long long wsum[32];  // per-warp partial sums of block scans and reductions
 };
 
@@ -401,6 +402,74 @@ __device__ __forceinline__ void sp_sort_buffer(const SpMem& m, int B) {
 
 // The merge pass (tdigest.mojo:391-439, _prune :441-458) over C centroids and
 // B buffered samples in shared state.  Leaves the new centroids in cm/cw.
+// Places centroids ++ buffer in their stable sorted order without sorting the
+// buffer: a buffered value's bucket is the number of centroids at or below it
+// (centroids sort first on equal values), its place is its bucket plus the
+// number of buffered values before it, and those are the values of earlier
+// buckets plus its rank inside its own bucket, counted directly.  Needs sorted
+// centroids; returns false (and places nothing) when a bucket holds more than
+// 64 values, where counting would cost more than sorting.
+__device__ bool sp_bucket_merge(const SpMem& m, SpSh& sh, int C, int B) {
+  int* off = m.nb;     // [C + 1]: bucket sizes, then their offsets (free until the reach)
+  int* fill = m.cid;   // [C + 1]
+  int* bk = reinterpret_cast<int*>(m.kk);  // bucket of each buffered value (free until k)
+  unsigned long long* tk = m.okey;         // buffered keys grouped by bucket
+  unsigned* ti = m.sidx;
+  for (int k = threadIdx.x; k <= C; k += SP_T) {
+    off[k] = 0;
+    fill[k] = 0;
+  }
+  if (threadIdx.x == 0) sh.bfail = 0;
+  __syncthreads();
+  for (int b = threadIdx.x; b < B; b += SP_T) {
+    const unsigned long long key = kd_order_key(m.bm[b]);
+    int lo = 0, hi = C;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (kd_order_key(m.cm[mid]) <= key) lo = mid + 1;
+      else hi = mid;
+    }
+    bk[b] = lo;
+    atomicAdd(&off[lo], 1);
+  }
+  __syncthreads();
+  const int c = threadIdx.x < C ? off[threadIdx.x] : 0;  // C <= 1024 = SP_T
+  if (c > 64 || (threadIdx.x == 0 && off[C] > 64)) sh.bfail = 1;  // off[C]: the last bucket
+  long long total;
+  const long long excl = sp_iscan(c, sh, &total);  // synchronises
+  if (threadIdx.x < C) off[threadIdx.x] = (int)excl;
+  if (threadIdx.x == 0) off[C] = (int)total;
+  __syncthreads();
+  if (sh.bfail) return false;
+  for (int b = threadIdx.x; b < B; b += SP_T) {
+    const int k = bk[b];
+    const int slot = off[k] + atomicAdd(&fill[k], 1);
+    tk[slot] = kd_order_key(m.bm[b]);
+    ti[slot] = (unsigned)b;
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < B; b += SP_T) {
+    const int k = bk[b];
+    const unsigned long long key = kd_order_key(m.bm[b]);
+    const int lo = off[k], hi = k < C ? off[k + 1] : B;
+    int within = 0;
+    for (int t = lo; t < hi; ++t) {
+      const unsigned long long ok = tk[t];
+      within += (ok < key || (ok == key && ti[t] < (unsigned)b)) ? 1 : 0;
+    }
+    const int pos = k + lo + within;
+    m.sm[pos] = m.bm[b];
+    m.sw[pos] = m.bw[b];
+  }
+  for (int i = threadIdx.x; i < C; i += SP_T) {
+    const int pos = i + off[i + 1];
+    m.sm[pos] = m.cm[i];
+    m.sw[pos] = m.cw[i];
+  }
+  __syncthreads();
+  return true;
+}
+
 // pk / px: the buffer's sorted order when it was sorted ahead (else null).
 __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
                                       const unsigned long long* pk, const unsigned* px) {
@@ -409,11 +478,6 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
   const int scale = a.s.scale;
   const bool decay = a.s.lambda > 0.0;
   // 1. work = centroids ++ buffer, stably sorted by mean
-  if (!pk) {
-    sp_sort_buffer(m, B);
-    pk = m.okey;
-    px = m.sidx;
-  }
   if (threadIdx.x == 0) sh.unsorted = 0;
   __syncthreads();
   for (int i = threadIdx.x; i + 1 < C; i += SP_T)
@@ -433,7 +497,13 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < C; i += SP_T) {  // centroids precede equal buffered values
+  const bool placed = !pk && C > 0 && C <= SP_T && sp_bucket_merge(m, sh, C, B);
+  if (!placed && !pk) {
+    sp_sort_buffer(m, B);
+    pk = m.okey;
+    px = m.sidx;
+  }
+  for (int i = threadIdx.x; !placed && i < C; i += SP_T) {  // centroids precede equal values
     const unsigned long long v = kd_order_key(m.cm[i]);
     int lo = 0, hi = B;
     while (lo < hi) {
@@ -444,7 +514,7 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
     m.sm[i + lo] = m.cm[i];
     m.sw[i + lo] = m.cw[i];
   }
-  for (int j = threadIdx.x; j < B; j += SP_T) {
+  for (int j = threadIdx.x; !placed && j < B; j += SP_T) {
     const unsigned long long v = pk[j];
     int lo = 0, hi = C;
     while (lo < hi) {
@@ -677,11 +747,14 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
   if (exact) {
     // the running weight before element j is pi[j] - pi[start]: every ratio
     // w / (cur_w + w) is known up front; only the mean stays a chain
-    for (int t = threadIdx.x; t < nc; t += SP_T)
-      for (int j = m.cst[t]; j < m.cst[t + 1]; ++j) m.cid[j] = m.cst[t];
-    __syncthreads();
     for (int j = threadIdx.x; j < W; j += SP_T) {
-      const int s0 = m.cid[j];
+      int lo = 0, hi = nc;  // the last cluster start <= j
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (m.cst[mid] <= j) lo = mid;
+        else hi = mid;
+      }
+      const int s0 = m.cst[lo];
       if (j > s0) {
         const long long d = m.pi[j + 1] - m.pi[s0];
         m.rw[j] = (kd_bits(sw[j]) == 0x3ff0000000000000ULL && d < SP_RCP_N)
@@ -693,6 +766,7 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
     for (int t = threadIdx.x; t < nc; t += SP_T) {
       const int s0 = m.cst[t], e = m.cst[t + 1];
       double cur_m = sm[s0];
+#pragma unroll 4
       for (int j = s0 + 1; j < e; ++j) cur_m = KD_ADD(cur_m, KD_MUL(KD_SUB(sm[j], cur_m), m.rw[j]));
       if (e < W && sm[e] == cur_m) sh.mismatch = 1;  // the reference coalesces an exact mean tie
       m.cm[t] = cur_m;
@@ -1101,38 +1175,10 @@ __device__ __noinline__ void sp_add_plain(const SpArgs& a, const SpMem& m, SpSh&
     }
     __syncthreads();
   }
-  // Two full buffers at a time are sorted ahead, each by half the block, when
-  // a buffer fits 512 entries: a sort is latency-bound, so two run for one.
-  int Lp = 1;
-  while (Lp < L) Lp <<= 1;
-  const bool pairs = 2 * Lp <= SP_T;
   long long i = 0;
   while (i < n_eff && !sh.err) {
     const int B0 = sh.B;
     const long long room = (long long)(L - B0);
-    if (pairs && n_eff - i >= room + L) {
-      const int t = threadIdx.x, blk = t / Lp, loc = t - blk * Lp;
-      unsigned long long key = ~0ull;
-      unsigned idx = 0x80000000u | (unsigned)t;
-      if (blk < 2 && loc < L) {
-        // buffer A: the waiting samples, then the next `room` ones; buffer B:
-        // the L samples after those (each in insertion order)
-        const double v = blk == 0 ? (loc < B0 ? m.bm[loc] : a.vals[i + loc - B0])
-                                  : a.vals[i + room + loc];
-        key = kd_order_key(v);
-        idx = (unsigned)loc;
-      }
-      sp_sort_regs(key, idx, Lp, 2 * Lp, m.pk, m.px);
-      sp_append(a, m, sh, i, (int)room);
-      sp_merge(a, m, sh, m.pk, m.px);
-      __syncthreads();
-      if (sh.err) break;
-      sp_append(a, m, sh, i + room, L);
-      sp_merge(a, m, sh, m.pk + Lp, m.px + Lp);
-      __syncthreads();
-      i += room + L;
-      continue;
-    }
     const int cut = (int)(n_eff - i < room ? n_eff - i : room);
     sp_append(a, m, sh, i, cut);
     i += cut;
