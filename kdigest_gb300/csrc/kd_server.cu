@@ -309,6 +309,7 @@ KD_API int kd_server_create(kd_store* store, double window_s, size_t budget_byte
   if (!store || !out) return KD_EINVAL;
   *out = nullptr;
   KdSession* s = store->st.sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
   if (!(window_s > 0.0) || !kd_isfinite(window_s)) return srv_fail(s->last_error, "window must be positive", KD_EINVAL);
   kd_server* v = new (std::nothrow) kd_server();
   if (!v) return KD_ENOMEM;
@@ -318,6 +319,10 @@ KD_API int kd_server_create(kd_store* store, double window_s, size_t budget_byte
   v->budget = budget_bytes ? budget_bytes : ((size_t)1 << 40);
   cudaSetDevice(s->device);
   int rc = kd_pipeline_prepare_device(s);
+  // Samples a one-key store buffered on the single-sample path are merged
+  // first (as any read does); the server's batches then go through the batch
+  // path with the centroids as their priors.
+  if (rc == KD_OK) rc = kd_spath_flush(s, &store->st);
   if (rc == KD_OK && cudaStreamCreateWithFlags(&v->copy_stream, cudaStreamNonBlocking) != cudaSuccess) rc = KD_ECUDA;
   if (rc) {
     delete v;

@@ -1476,13 +1476,13 @@ int sp_run(KdSession* s, KdStore* st, int op, const double* d_vals, const double
     scratch = (unsigned char*)st->sp_scratch;
     smem = 0;
   }
-  static bool attr_done[64] = {};
+  static std::atomic<bool> attr_done[64];
   const int dev = s->device;
-  if (smem && dev >= 0 && dev < 64 && !attr_done[dev]) {
+  if (smem && dev >= 0 && dev < 64 && !attr_done[dev].load()) {
     cudaError_t e = cudaFuncSetAttribute(k_spath, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)SP_SMEM_MAX);
     if (e != cudaSuccess) return kd_cuda_fail(s, e, "single-sample path attributes");
-    attr_done[dev] = true;
+    attr_done[dev].store(true);
   }
   static std::atomic<bool> rcp_done[64];
   static const double* rcp_ptr[64];

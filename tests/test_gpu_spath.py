@@ -255,3 +255,16 @@ def test_tiny_compression_merges_every_sample(kd, oracle):
     od.add_many(v)
     _same(d, od)
     _same_queries(d, od)
+
+
+def test_server_over_single_digest_merges_the_buffer(kd, oracle):
+    """A serving loop takes the store over: buffered samples are merged first."""
+    d = kd.TDigest(100.0, kd.K2)
+    od = oracle.Digest(oracle.K2, 100.0, 0.0)
+    v = np.random.default_rng(31).standard_normal(777)
+    d.add_batch(v)
+    od.add_many(v)
+    srv = kd.Server(d, window=1e-3)
+    srv.close()
+    od.merge()
+    _same(d, od)
