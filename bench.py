@@ -283,13 +283,13 @@ def run_config1(args) -> int:
     L = N.load()
     nb = (C1_TOTAL + C1_BATCH - 1) // C1_BATCH
 
-    def stream(single: bool):
+    def stream(single: bool, decay=None, passes: int = 3):
         """The whole stream in batches of 4096: the reference's path for this
         size (the add loop on the device) or the batch path."""
         reps = []
         d = None
-        for rep in range(args.warmup + 3):  # whole-stream passes; the first ones warm up
-            d = kd.TDigest(100.0, kd.K1, session=sess)
+        for rep in range(args.warmup + passes):  # whole-stream passes; the first ones warm up
+            d = kd.TDigest(100.0, kd.K1, decay=decay, session=sess)
             h = d._store._h
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
@@ -312,6 +312,10 @@ def run_config1(args) -> int:
 
     ms, d = stream(True)
     ms_p, dp = stream(False)
+    # the same stream with count decay (half-life 10^5 samples): non-integral
+    # weights take the speculate-and-verify sweep and the per-sample clock chain
+    dec = kd.Decay.half_life(1e5)
+    ms_d, dd = stream(True, dec, passes=1)
     q7 = np.array(QUANTILES)
     sv = np.sort(vals_h)
     gq = d.quantiles(q7)
@@ -322,12 +326,20 @@ def run_config1(args) -> int:
            "gpu_p_path": {"rank_error_ppm": [round(x, 1) for x in rank_error_ppm(sv, pq, q7)],
                           "centroids": len(dp), "ms_per_stream": ms_p,
                           "samples_per_s": C1_TOTAL / (ms_p / 1e3)}}
+    out["gpu_s_path_decayed"] = {"samples_per_s": C1_TOTAL / (ms_d / 1e3), "ms_per_stream": ms_d,
+                                 "half_life_samples": 1e5, "centroids": len(dd)}
     cpu = None
     parity = None
     if not args.no_cpu:
         from oracle import pyoracle as po
 
         po.build()
+        odd = po.Digest(po.K1, 100.0, dec.rate_lambda)
+        t0 = time.perf_counter()
+        odd.add_many(vals_h)
+        out["gpu_s_path_decayed"]["cpu_samples_per_s"] = C1_TOTAL / (time.perf_counter() - t0)
+        out["gpu_s_path_decayed"]["bit_exact"] = bool(
+            np.array_equal(odd.centroids()[0], dd.centroids()[0]) and dd.to_bytes() == odd.to_bytes())
         od = po.Digest(po.K1, 100.0, 0.0)
         t0 = time.perf_counter()
         od.add_many(vals_h)

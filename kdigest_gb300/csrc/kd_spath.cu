@@ -40,6 +40,7 @@ namespace {
 constexpr int SP_T = 1024;  // threads of the one CTA
 constexpr double SP_RENORM = 400.0;    // tdigest.mojo:43
 constexpr int SP_RCP_N = 1 << 16;      // reciprocal table entries
+constexpr int SP_RUNS = 64;            // exponent runs per buffer fill
 constexpr double SP_PRUNE_EPS = 1e-6;  // tdigest.mojo:47
 
 enum { SP_ADD = 0, SP_FLUSH = 1, SP_MERGE_INTO = 2 };
@@ -83,6 +84,8 @@ struct SpMem {
   double *wsf, *kl;  // weight before each cluster and its k [KD_TILE + 1]
   unsigned long long* pk;  // buffers sorted ahead of their merge [SP_T]
   unsigned* px;
+  int *rk, *rn;      // runs of the exponent: first sample, length [SP_RUNS]
+  double *rx, *rr;   // value before the run, step
 };
 
 __host__ __device__ inline size_t sp_align(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -115,6 +118,10 @@ __host__ __device__ inline size_t sp_layout(int bmax, int wpb, unsigned char* ba
   t.kl = (double*)take(8 * (KD_TILE + 1));
   t.pk = (unsigned long long*)take(8 * 1024);
   t.px = (unsigned*)take(4 * 1024);
+  t.rk = (int*)take(4 * SP_RUNS);
+  t.rn = (int*)take(4 * SP_RUNS);
+  t.rx = (double*)take(8 * SP_RUNS);
+  t.rr = (double*)take(8 * SP_RUNS);
   if (m) *m = t;
   return off;
 }
@@ -127,9 +134,11 @@ struct SpSh {
   double k0, k1;  // FP64 k at q = 0 and q = 1 (filtered sweeps)
   double f0, f1;  // the same with normaliser 1: k(q, nrm) = nrm * k(q, 1) at these q
   double nrm01;   // the K0 / K1 normaliser (it does not depend on the total)
+  double inv_st;  // 1 / stored total, for approximate q (filters and speculation only)
   int C, B, err, nc, mismatch, unsorted, exact, cut, renorm, pre_adv, integral, fast, filt;
   int longreach;  // a cluster start whose reach passed 64 candidates
   int bfail;      // a bucket of the buffer merge was too large
+  int nruns;      // runs of the exponent in the current buffer fill
   long long wsum[32];  // per-warp partial sums of block scans and reductions
 };
 
@@ -163,6 +172,29 @@ __device__ __forceinline__ float sp_k32(int scale, long long p, double st, float
   }
 }
 
+// k at an FP64 q in FP32, with q and 1 - q each rounded once (1 - q is exact
+// in FP64 for q >= 1/2).  The same error bound as sp_k32 holds.  Near 0 and 1,
+// where the FP64 k clamps, it returns NaN unless `clamp` asks for the end values.
+__device__ __forceinline__ float sp_k32q(int scale, double q, float nrmf, float k0f, float k1f,
+                                         bool clamp) {
+  if (!(q > 1e-14)) return clamp ? k0f : __int_as_float(0x7fc00000);
+  if (!(q < 1.0 - 1e-14)) return clamp ? k1f : __int_as_float(0x7fc00000);
+  const float a = (float)q, c = (float)(1.0 - q);
+  switch (scale) {
+    case KD_SCALE_K0:
+      return nrmf * a;
+    case KD_SCALE_K1: {
+      const bool lo = a <= c;
+      const float t = 1.57079637f - 2.0f * asinf(sqrtf(lo ? a : c));
+      return nrmf * (lo ? -t : t);
+    }
+    case KD_SCALE_K2:
+      return nrmf * logf(a / c);
+    default:
+      return a <= c ? nrmf * logf(2.0f * a) : -nrmf * logf(2.0f * c);
+  }
+}
+
 // The k-size test of the merge pass for candidate j of the cluster that starts
 // at s0: k(q(j + 1)) - k(q(s0)) <= 1 with FP64 k at exact prefix positions.
 // Filtered: the FP32 difference decides unless it is within tau of 1; then (and
@@ -170,6 +202,7 @@ __device__ __forceinline__ float sp_k32(int scale, long long p, double st, float
 struct SpFit {
   int scale;
   bool filt;
+  bool spec;  // non-integral weights: FP32 k of approximate sums, a speculation only
   float tau;
   double st, nrm;
   const float* k32;
@@ -179,6 +212,7 @@ struct SpFit {
     return filt ? sp_k(scale, KD_DIV((double)pi[i], st), nrm) : kk[i];
   }
   __device__ bool fits(int s0, int j, double& ks64) const {
+    if (spec) return k32[j + 1] - k32[s0] <= 1.0f;
     if (!filt) return KD_SUB(kk[j + 1], kk[s0]) <= 1.0;
     const float d = k32[j + 1] - k32[s0];
     if (d <= 1.0f - tau) return true;
@@ -564,15 +598,16 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
   const bool exact = sh.exact != 0;
   if (threadIdx.x == 0) {
     sh.filt = exact && (double)m.pi[W] <= st && st >= 1.0 && st <= 1e14;
-    if (sh.filt) {  // nrm * k(q, 1) rounds exactly as k(q, nrm) at q = 0 and 1
-      sh.k0 = KD_MUL(nrm, sh.f0);
-      sh.k1 = KD_MUL(nrm, sh.f1);
-    }
+    // nrm * k(q, 1) rounds exactly as k(q, nrm) at q = 0 and 1
+    sh.k0 = KD_MUL(nrm, sh.f0);
+    sh.k1 = KD_MUL(nrm, sh.f1);
+    sh.inv_st = KD_DIV(1.0, st);
   }
   __syncthreads();
   SpFit fit;
   fit.scale = scale;
   fit.filt = sh.filt != 0;
+  fit.spec = !exact;
   // FP32 error bound: 3.3e-6 * nrm (K0, K1) and 1.8e-5 * nrm (K2, K3) on a
   // difference; the undecided band is several times wider
   fit.tau = (float)KD_MUL(nrm, scale <= KD_SCALE_K1 ? 0x1p-15 : 0x1p-13);
@@ -590,7 +625,11 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
       m.kk[i] = sp_k(scale, KD_DIV((double)m.pi[i], st), nrm);
   } else {
     sp_prefix(m.sw, m.rw, W, m.wsf);
-    for (int i = threadIdx.x; i <= W; i += SP_T) m.kk[i] = sp_k(scale, KD_DIV(m.rw[i], st), nrm);
+    float* k32 = reinterpret_cast<float*>(m.kk);
+    const float nrmf = (float)nrm, k0f = (float)sh.k0, k1f = (float)sh.k1;
+    const double inv_st = sh.inv_st;
+    for (int i = threadIdx.x; i <= W; i += SP_T)
+      k32[i] = sp_k32q(scale, KD_MUL(m.rw[i], inv_st), nrmf, k0f, k1f, true);
   }
   __syncthreads();
   // 4. for every element as a cluster start, where that cluster would end:
@@ -603,12 +642,12 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
   // candidates after it are tested one by one (exactly where undecided).
   if (threadIdx.x == 0) sh.unsorted = 0;  // here: FP32 k not monotone
   __syncthreads();
-  if (fit.filt)
+  if (fit.filt || fit.spec)
     for (int i = threadIdx.x; i < W; i += SP_T)
       if (fit.k32[i + 1] < fit.k32[i]) sh.unsorted = 1;
   __syncthreads();
-  const bool mono = fit.filt && !sh.unsorted;
-  const float sure = 1.0f - fit.tau;
+  const bool mono = (fit.filt || fit.spec) && !sh.unsorted;
+  const float sure = fit.spec ? 1.0f : 1.0f - fit.tau;
   for (int s0 = threadIdx.x; s0 < W; s0 += SP_T) {
     double ks64 = __longlong_as_double(0x7ff8000000000000LL);  // not yet evaluated
     const unsigned long long ms = kd_order_key(sm[s0]);
@@ -774,23 +813,32 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
     }
     __syncthreads();
   } else {
+    // running weights first (a serial chain of additions per cluster), then
+    // every ratio w / (cur_w + w) in parallel, then the mean chains
     for (int t = threadIdx.x; t < nc; t += SP_T) {
       const int s0 = m.cst[t], e = m.cst[t + 1];
-      double cur_m = sm[s0], cur_w = sw[s0];
+      double cur_w = sw[s0];
       m.cid[s0] = t;
       for (int j = s0 + 1; j < e; ++j) {
         m.rw[j] = cur_w;
-        const double nw = KD_ADD(cur_w, sw[j]);
-        cur_m = KD_ADD(cur_m, KD_MUL(KD_SUB(sm[j], cur_m), KD_DIV(sw[j], nw)));
-        cur_w = nw;
+        cur_w = KD_ADD(cur_w, sw[j]);
         m.cid[j] = t;
       }
-      if (e < W) {
-        m.rw[e] = cur_w;
-        if (sm[e] == cur_m) sh.mismatch = 1;
-      }
-      m.cm[t] = cur_m;
+      if (e < W) m.rw[e] = cur_w;
       m.cw[t] = cur_w;
+    }
+    __syncthreads();
+    double* ratio = m.kk;  // the k array is free once the chain is known
+    for (int j = threadIdx.x; j < W; j += SP_T)
+      if (m.cst[m.cid[j]] != j) ratio[j] = KD_DIV(sw[j], KD_ADD(m.rw[j], sw[j]));
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc; t += SP_T) {
+      const int s0 = m.cst[t], e = m.cst[t + 1];
+      double cur_m = sm[s0];
+#pragma unroll 4
+      for (int j = s0 + 1; j < e; ++j) cur_m = KD_ADD(cur_m, KD_MUL(KD_SUB(sm[j], cur_m), ratio[j]));
+      if (e < W && sm[e] == cur_m) sh.mismatch = 1;  // the reference coalesces an exact mean tie
+      m.cm[t] = cur_m;
     }
     __syncthreads();
   }
@@ -804,14 +852,31 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
       }
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < nc; t += SP_T) m.kl[t] = sp_k(scale, KD_DIV(m.wsf[t], st), nrm);
+    // the exact test k(q_right) - k(q_left) <= 1 through the FP32 filter; the
+    // FP64 k only where the FP32 difference cannot decide
+    // (the filter's q may be off by an ulp or two of FP64: far inside its band,
+    // so it multiplies by 1/st; the undecided cases divide exactly)
+    const float nrmf = (float)nrm, k0f = (float)sh.k0, k1f = (float)sh.k1;
+    const double inv_st = sh.inv_st;
+    float* kl32 = reinterpret_cast<float*>(m.kl);
+    for (int t = threadIdx.x; t < nc; t += SP_T)
+      kl32[t] = sp_k32q(scale, KD_MUL(m.wsf[t], inv_st), nrmf, k0f, k1f, false);
     __syncthreads();
     for (int j = 1 + threadIdx.x; j < W; j += SP_T) {
       const int t = m.cid[j];
       const bool start = m.cst[t] == j;
       const int tt = start ? t - 1 : t;
-      const double qr = KD_DIV(KD_ADD(KD_ADD(m.wsf[tt], m.rw[j]), sw[j]), st);
-      const bool fits = KD_SUB(sp_k(scale, qr, nrm), m.kl[tt]) <= 1.0;
+      const double num = KD_ADD(KD_ADD(m.wsf[tt], m.rw[j]), sw[j]);
+      const float d = sp_k32q(scale, KD_MUL(num, inv_st), nrmf, k0f, k1f, false) - kl32[tt];
+      bool fits;
+      if (d <= 1.0f - fit.tau) {
+        fits = true;
+      } else if (d > 1.0f + fit.tau) {
+        fits = false;
+      } else {  // undecided (or an end of the scale): FP64
+        fits = KD_SUB(sp_k(scale, KD_DIV(num, st), nrm), sp_k(scale, KD_DIV(m.wsf[tt], st), nrm)) <=
+               1.0;
+      }
       if (start) {
         if (fits) sh.mismatch = 1;
       } else if (!fits && !(sm[j] == sm[m.cst[tt]])) {
@@ -956,7 +1021,7 @@ __device__ void sp_reduce_minmax(SpPick& mn, SpPick& mx, SpPick* red) {
 // full buffer runs the merge pass.
 __device__ __noinline__ void sp_add_decay(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_eff,
                              SpPick* red) {
-  const bool decay = a.s.lambda > 0.0;
+  const bool decay = true;
   const double lambda = a.s.lambda;
   const int L = a.s.buf_cap;
   long long i = 0;
@@ -964,72 +1029,122 @@ __device__ __noinline__ void sp_add_decay(const SpArgs& a, const SpMem& m, SpSh&
     const long long room = (long long)(L - sh.B);
     const int seg = (int)(n_eff - i < room ? n_eff - i : room);
     const int B0 = sh.B;
-    // clock, decay exponent and renormalisation, in sample order
+    // clock, decay exponent and renormalisation, in sample order (one thread)
     if (threadIdx.x == 0) {
-      // Without decay the exponent never moves: the clock is the only chain.
-      // Count clock: integral clocks below 2^52 add exactly, so clock + seg is
-      // the sum of seg additions of 1.  Time clock: the latest timestamp wins,
-      // the earliest of equal ones (strict comparisons).
-      sh.fast = !decay && (a.ts != nullptr || (sh.clock == floor(sh.clock) &&
-                                               fabs(sh.clock) < 4.0e15));
-    }
-    __syncthreads();
-    if (sh.fast) {
-      if (a.ts) {
-        SpPick mx{kd_order_key(sh.clock), -1, sh.clock}, dummy{0, 0, 0.0};
-        for (int k = threadIdx.x; k < seg; k += SP_T) {
-          const double t = a.ts[i + k];
-          if (t == t) mx = sp_pick_max(mx, SpPick{kd_order_key(t), (long long)k, t});
-        }
-        dummy = SpPick{~0ull, -1, 0.0};
-        sp_reduce_minmax(dummy, mx, red);
-        if (threadIdx.x == 0) {
-          // `timestamp > clock` advances; an equal later timestamp does not
-          if (mx.seq >= 0 && mx.v > sh.clock) sh.clock = mx.v;
-          sh.cut = seg;
-          sh.renorm = 0;
-        }
-      } else if (threadIdx.x == 0) {
-        sh.clock = KD_ADD(sh.clock, (double)seg);
-        sh.cut = seg;
-        sh.renorm = 0;
-      }
-      for (int k = threadIdx.x; k < seg; k += SP_T) m.sls[k] = sh.ls;
-    } else if (threadIdx.x == 0) {
       int cut = 0;
       sh.renorm = 0;
+      sh.nruns = 0;
       double clock = sh.clock, ls = sh.ls;
-      for (int k = 0; k < seg; ++k) {
-        const long long j = i + k;
-        bool adv;
-        double nc = clock;
-        if (sh.pre_adv && k == 0) {
-          adv = false;  // this sample's clock step ran before the renormalisation
-        } else if (a.ts) {
-          adv = a.ts[j] > clock;
-          nc = a.ts[j];
-        } else {
-          adv = true;
-          nc = KD_ADD(clock, 1.0);
+      if (!a.ts && clock == floor(clock) && fabs(clock) < 4.0e15) {
+        // Count clock: every step is exactly clock + 1, so the exponent step
+        // lambda * (new - old) is exactly lambda.  Only the exponent's own
+        // chain of additions stays serial.
+        // The threshold test compares bit patterns (the exponent is never
+        // negative), so only the additions wait on each other.
+        const unsigned long long renorm_bits = kd_bits(SP_RENORM);
+        double* const sls = m.sls;
+        int adv = 0, k = 0;
+        if (sh.pre_adv && seg > 0) {
+          sls[0] = ls;
+          k = 1;
         }
-        if (adv) {
-          if (decay && nc > clock) {
-            ls = KD_ADD(ls, KD_MUL(lambda, KD_SUB(nc, clock)));
-            if (ls > SP_RENORM) {
-              sh.renorm = 1;
-              sh.renorm_clock = nc;
-              break;
+        // Inside one binade [2^e, 2^(e+1)) of the exponent, and unless lambda
+        // sits exactly half-way between two multiples of its ulp u, every step
+        // rounds x + lambda to x + r with the same r: the values form runs
+        // x + r, x + 2r, ... that other threads fill in.  Crossings, ties and
+        // the renormalisation threshold are stepped one at a time.
+        int nr = 0;
+        while (k < seg && nr < SP_RUNS) {
+          const double y = KD_ADD(ls, lambda);
+          if (kd_bits(y) > renorm_bits) break;  // the per-sample loop below handles it
+          const unsigned long long bx = kd_bits(ls);
+          const int ex = (int)((bx >> 52) & 0x7ff);
+          int n = 1;
+          double r = KD_SUB(y, ls);
+          if (ls > 0.0 && ex > 53 && ex < 2000) {
+            const double top = KD_SUB(kd_pow2i(ex - 1022), kd_pow2i(ex - 1075));  // 2^(e+1) - u
+            const double t = KD_MUL(lambda, kd_pow2i(1075 - ex));  // lambda / u, exact
+            const bool tie = KD_SUB(t, floor(t)) == 0.5;
+            if (!tie && y <= top) {
+              const double D = KD_SUB(top, ls);  // exact: multiples of u
+              if (r == 0.0) {
+                n = seg - k;  // below half an ulp: the exponent no longer moves
+              } else {
+                // largest m with x + m r + lambda < top, and x + (m + 1) r <= 400
+                double mf = floor(KD_DIV(KD_SUB(D, lambda), r));
+                const double mr = floor(KD_DIV(KD_SUB(SP_RENORM, ls), r)) - 1.0;
+                if (mr < mf) mf = mr;
+                long long mm = mf > 1e9 ? 1000000000LL : (long long)mf;
+                while (mm > 0 && !(lambda < KD_SUB(D, KD_MUL((double)mm, r)))) --mm;
+                while (mm > 0 && KD_ADD(ls, KD_MUL((double)(mm + 1), r)) > SP_RENORM) --mm;
+                if (mm < 0) mm = 0;
+                n = (int)((long long)(seg - k) < mm + 1 ? (long long)(seg - k) : mm + 1);
+              }
             }
           }
-          clock = nc;
+          m.rk[nr] = k;
+          m.rn[nr] = n;
+          m.rx[nr] = ls;
+          m.rr[nr] = r;
+          ++nr;
+          ls = KD_ADD(ls, KD_MUL((double)n, r));
+          k += n;
+          adv += n;
         }
-        m.sls[k] = ls;
-        cut = k + 1;
+        sh.nruns = nr;
+        for (; k < seg; ++k) {
+          const double nl = KD_ADD(ls, lambda);
+          if (kd_bits(nl) > renorm_bits) {
+            ls = nl;
+            sh.renorm = 1;
+            sh.renorm_clock = KD_ADD(clock, (double)(adv + 1));
+            break;
+          }
+          ls = nl;
+          ++adv;
+          sls[k] = ls;
+        }
+        cut = k;
+        clock = KD_ADD(clock, (double)adv);
+      } else {
+        for (int k = 0; k < seg; ++k) {
+          const long long j = i + k;
+          bool advance;
+          double nc = clock;
+          if (sh.pre_adv && k == 0) {
+            advance = false;  // this sample's clock step ran before the renormalisation
+          } else if (a.ts) {
+            advance = a.ts[j] > clock;
+            nc = a.ts[j];
+          } else {
+            advance = true;
+            nc = KD_ADD(clock, 1.0);
+          }
+          if (advance) {
+            if (nc > clock) {
+              ls = KD_ADD(ls, KD_MUL(lambda, KD_SUB(nc, clock)));
+              if (ls > SP_RENORM) {
+                sh.renorm = 1;
+                sh.renorm_clock = nc;
+                break;
+              }
+            }
+            clock = nc;
+          }
+          m.sls[k] = ls;
+          cut = k + 1;
+        }
       }
       sh.pre_adv = 0;
       sh.clock = clock;
       sh.ls = ls;
       sh.cut = cut;
+    }
+    __syncthreads();
+    for (int q = 0; q < sh.nruns; ++q) {  // the exponent runs: x + j r, exact
+      const int k0 = m.rk[q], n = m.rn[q];
+      const double x = m.rx[q], r = m.rr[q];
+      for (int j = threadIdx.x; j < n; j += SP_T) m.sls[k0 + j] = KD_ADD(x, KD_MUL((double)(j + 1), r));
     }
     __syncthreads();
     const int cut = sh.cut;
@@ -1072,7 +1187,9 @@ __device__ __noinline__ void sp_add_decay(const SpArgs& a, const SpMem& m, SpSh&
         if (exact) tot = KD_ADD(tot, (double)sum);
         if (!exact) {
           tot = sh.st;
-          for (int k = 0; k < cut; ++k) tot = KD_ADD(tot, m.bw[B0 + k]);
+          const double* const bw = m.bw + B0;
+#pragma unroll 8
+          for (int k = 0; k < cut; ++k) tot = KD_ADD(tot, bw[k]);
         }
         sh.st = tot;
         sh.B = B0 + cut;
