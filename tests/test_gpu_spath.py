@@ -268,3 +268,61 @@ def test_server_over_single_digest_merges_the_buffer(kd, oracle):
     srv.close()
     od.merge()
     _same(d, od)
+
+
+def test_one_call_many_merges_below_crossover(kd, oracle):
+    """59,999 samples (just below the crossover) in one call: 119 merge passes."""
+    d = kd.TDigest(100.0, kd.K3)
+    od = oracle.Digest(oracle.K3, 100.0, 0.0)
+    v = np.random.default_rng(40).standard_cauchy(59_999)
+    d.add_batch(v)
+    od.add_many(v)
+    _same(d, od)
+    _same_queries(d, od, xs=(-10.0, 0.0, 0.1, 10.0))
+
+
+def test_add_at_odd_timestamps_and_renormalisation(kd, oracle):
+    """NaN stamps never move the clock; a long gap renormalises (time decay)."""
+    dec = kd.Decay.rate(0.9)
+    d = kd.TDigest(50.0, kd.K2, decay=dec)
+    od = oracle.Digest(oracle.K2, 50.0, dec.rate_lambda)
+    rng = np.random.default_rng(41)
+    t = 0.0
+    for i in range(5000):
+        if i == 2500:
+            t += 600.0  # lambda * gap > 400: renormalise inside the loop
+        elif i % 50 == 7:
+            ts = float("nan")
+        else:
+            t += float(rng.exponential(0.01))
+        ts = float("nan") if i % 50 == 7 else t
+        v = float(rng.normal())
+        d.add_at(v, ts)
+        od.add_at(v, ts)
+    _same(d, od)
+    _same_queries(d, od)
+
+
+def test_time_clock_without_decay(kd, oracle):
+    d = kd.TDigest(100.0, kd.K1)
+    od = oracle.Digest(oracle.K1, 100.0, 0.0)
+    rng = np.random.default_rng(42)
+    ts = np.cumsum(rng.exponential(1.0, 3000))
+    ts[::17] = ts[::17] - 5.0  # late stamps
+    for v, t in zip(rng.normal(size=3000), ts):
+        d.add_at(float(v), float(t))
+        od.add_at(float(v), float(t))
+    _same(d, od)
+
+
+def test_restore_then_single_samples(kd, oracle):
+    """A digest restored from bytes continues on the single-sample path."""
+    rng = np.random.default_rng(43)
+    od = oracle.Digest(oracle.K1, 100.0, 0.0)
+    od.add_many(rng.normal(size=7000))
+    d = kd.TDigest.from_bytes(od.to_bytes(), scale=kd.K1)
+    v = rng.normal(size=3333)
+    d.add_batch(v)
+    od.add_many(v)
+    _same(d, od)
+    _same_queries(d, od)
