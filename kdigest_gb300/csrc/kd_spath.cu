@@ -1526,6 +1526,7 @@ int sp_ensure(KdSession* s, KdStore* st) {
   KdStoreDev& d = st->d;
   if (d.K != 1) return sp_fail(s, KD_EINVAL, "the single-sample path serves one-digest stores");
   if (d.bcount) return KD_OK;
+  if (!(d.compression < 1e6)) return sp_fail(s, KD_EINVAL, "compression too large for the single-sample path");
   long long L = (long long)d.compression * 5;  // Int(compression) * _BUFFER_FACTOR
   if (L < 1) L = 1;
   if (L > (1 << 20)) return sp_fail(s, KD_EINVAL, "compression too large for the single-sample path");
