@@ -679,6 +679,38 @@ def run_config4(args) -> int:
                 acc.append(e0.elapsed_time(e1))
     ms_q, ms_c = statistics.median(tq), statistics.median(tc)
     qps = 2 * C4_QUERIES / ((ms_q + ms_c) / 1e3)
+    # plain form: one call per group digest (host arrays), on 64 groups
+    plain = None
+    if not args.no_plain:
+        groups = [(ids[ids == k], qs[ids == k]) for k in range(64)]
+        nq = sum(len(g[0]) for g in groups)
+        t0 = time.perf_counter()
+        for gk, gqs in groups:
+            lvl2.quantiles(gk, gqs)
+        dt = time.perf_counter() - t0
+        plain = {"value": nq / dt, "unit": "queries/s",
+                 "sample": f"{nq} quantile queries of 64 groups, one call per group"}
+    # CPU baseline and parity: the oracle answers the first 2^22 quantile and cdf
+    # queries on the same 1024 groups (restored from their bytes), on all host threads
+    cpu = None
+    parity = None
+    if not args.no_cpu:
+        from oracle import pyoracle as po
+
+        po.build()
+        data, offs = lvl2.export()
+        ods = [po.Digest.from_bytes(data[offs[k]:offs[k + 1]], po.K2) for k in range(1024)]
+        ns = 1 << 22
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        oq = po.query_batch(ods, ids[:ns], qs[:ns], False, threads)
+        oc = po.query_batch(ods, cids[:ns], xs[:ns], True, threads)
+        dt = time.perf_counter() - t0
+        parity = bool(np.array_equal(out_q[:ns].cpu().numpy(), oq, equal_nan=True) and
+                      np.array_equal(out_c[:ns].cpu().numpy(), oc, equal_nan=True))
+        cpu = {"value": 2 * ns / dt, "unit": "queries/s", "cores": threads, "kind": "port",
+               "sample": f"the first 2^22 quantile and 2^22 cdf queries ({dt:.2f} s, C oracle, "
+                         f"queries split over {threads} threads)"}
     peaks = measured_peaks()
     qbytes = 20 * C4_QUERIES  # key 4 B + q 8 B + result 8 B per query
     achieved = qbytes / (ms_q / 1e3) / 1e9
@@ -702,6 +734,9 @@ def run_config4(args) -> int:
                      "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
                      "algorithmic_bytes": qbytes},
+        "cpu_baseline": cpu,
+        "queries_bit_identical_to_oracle": parity,
+        "plain_form": plain,
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -873,3 +873,57 @@ double kdo_k(int scale, double q, double nrm) { return kd_k(scale, q, nrm); }
 int32_t kdo_bucket(int scale, double cum, double tot, double nrm) {
   return kd_bucket(scale, cum, tot, nrm);
 }
+
+typedef struct {
+  kdo_digest** digests;
+  int64_t nd;
+  const int32_t* ids;
+  const double* x;
+  int64_t i0, i1;
+  int is_cdf;
+  double* out;
+  int err;
+} qry_job;
+
+static void* qry_worker(void* p) {
+  qry_job* j = (qry_job*)p;
+  for (int64_t i = j->i0; i < j->i1; ++i) {
+    const int32_t id = j->ids[i];
+    int e = KDO_EINVAL;
+    double v = kd_from_bits(0x7ff8000000000000ULL);
+    if (id >= 0 && id < j->nd) {
+      e = j->is_cdf ? kdo_cdf(j->digests[id], j->x[i], &v) : kdo_quantile(j->digests[id], j->x[i], &v);
+      if (e) v = kd_from_bits(0x7ff8000000000000ULL);
+    }
+    j->out[i] = v;
+    if (e && !j->err) j->err = e;
+  }
+  return NULL;
+}
+
+int kdo_query_batch(kdo_digest** digests, int64_t nd, const int32_t* ids, const double* x,
+                    int64_t n, int is_cdf, double* out, int threads) {
+  for (int64_t k = 0; k < nd; ++k) kdo_merge(digests[k]);
+  if (threads < 1) threads = 1;
+  if (threads > 256) threads = 256;
+  qry_job jobs[256];
+  pthread_t tids[256];
+  const int64_t per = (n + threads - 1) / threads;
+  int used = 0;
+  for (int t = 0; t < threads; ++t) {
+    const int64_t i0 = (int64_t)t * per, i1 = i0 + per < n ? i0 + per : n;
+    if (i0 >= i1) break;
+    jobs[t] = (qry_job){digests, nd, ids, x, i0, i1, is_cdf, out, 0};
+    ++used;
+  }
+  if (used == 1) {
+    qry_worker(&jobs[0]);
+  } else {
+    for (int t = 0; t < used; ++t) pthread_create(&tids[t], NULL, qry_worker, &jobs[t]);
+    for (int t = 0; t < used; ++t) pthread_join(tids[t], NULL);
+  }
+  int err = KDO_OK;
+  for (int t = 0; t < used; ++t)
+    if (jobs[t].err && !err) err = jobs[t].err;
+  return err;
+}

@@ -96,6 +96,13 @@ int kdo_grouped_add_batch(kdo_digest** digests, int64_t num_keys, const uint32_t
  * and compressed once with the P-path into `dst` (which is reset first). */
 int kdo_merge_parts_p(kdo_digest* dst, kdo_digest** parts, int64_t nparts);
 
+/* Batched queries: out[i] = quantile (is_cdf = 0) or cdf of digests[ids[i]] at
+ * x[i] (tdigest.mojo:485-587), split over `threads` threads.  Every digest is
+ * merged first, so the queries only read.  A failing query gives NaN; the
+ * first failing status is returned. */
+int kdo_query_batch(kdo_digest** digests, int64_t nd, const int32_t* ids, const double* x,
+                    int64_t n, int is_cdf, double* out, int threads);
+
 /* Exports of the shared FP64 scale arithmetic (kd_math.h), for accuracy tests. */
 double kdo_log(double x);
 double kdo_exp(double x);

@@ -73,6 +73,7 @@ def lib():
         L.kdo_set_state.argtypes = [_P, _P, _P, _I64, _D, _D, _D, _D, _D]
         L.kdo_grouped_add_batch.argtypes = [_P, _I64, _P, _P, _I64, ctypes.c_int, _D, ctypes.c_int]
         L.kdo_merge_parts_p.argtypes = [_P, _P, _I64]
+        L.kdo_query_batch.argtypes = [_P, _I64, _P, _P, _I64, ctypes.c_int, _P, ctypes.c_int]
         for name in ("kdo_log", "kdo_exp", "kdo_asin"):
             getattr(L, name).restype = _D
             getattr(L, name).argtypes = [_D]
@@ -234,6 +235,17 @@ def merge_parts(dst: Digest, parts):
     rc = lib().kdo_merge_parts_p(dst._h, arr, len(parts))
     if rc:
         raise OracleError(rc, "merge_parts")
+
+
+def query_batch(digests, ids, xs, is_cdf: bool, threads: int = 1):
+    """Batched quantile / cdf over digests[ids[i]] at xs[i] (NaN where a query fails)."""
+    arr = (ctypes.c_void_p * len(digests))(*[d._h for d in digests])
+    k = np.ascontiguousarray(ids, dtype=np.int32)
+    x = np.ascontiguousarray(xs, dtype=np.float64)
+    out = np.empty(len(x))
+    lib().kdo_query_batch(arr, len(digests), _ptr(k), _ptr(x), len(x), int(is_cdf), _ptr(out),
+                          threads)
+    return out
 
 
 def log(x): return lib().kdo_log(x)
