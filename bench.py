@@ -1077,11 +1077,29 @@ def run_gpu(args):
         del store3
 
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, done, t, _ = cpu_ingest_rate(keys, vals, threads)
+        v, done, t, odig = cpu_ingest_rate(keys, vals, threads)
         cpu = {"value": v, "unit": "samples/s", "cores": threads, "kind": "port",
                "sample": f"first {done} batches of 2^22 pairs ({t:.1f} s, C oracle P-path, key-partitioned threads)"}
+        if ingested == list(range(done)):
+            # the oracle ingested exactly the GPU store's batches: centroid counts
+            # of every key, and 256 keys' centroids, header and quantiles, bit for bit
+            gcounts = store.centroid_counts()
+            counts_ok = all(int(gcounts[k]) == len(odig[k]) for k in range(NUM_KEYS))
+            sample = np.random.default_rng(SEED + 7).choice(NUM_KEYS, 256, replace=False)
+            cent_ok = q_ok = True
+            for k in sample.tolist():
+                gm, gw = store.centroids(k)
+                om, ow = odig[k].centroids()
+                cent_ok = cent_ok and np.array_equal(gm, om) and np.array_equal(gw, ow)
+                if len(om):
+                    for q in QUANTILES:
+                        q_ok = q_ok and store.quantile(k, q) == odig[k].quantile(q)
+            parity = {"batches": done, "counts_equal_all_keys": bool(counts_ok), "sample_keys": 256,
+                      "centroids_bit_identical": bool(cent_ok),
+                      "quantiles_bit_identical": bool(q_ok)}
 
     serving = None
     if not args.no_serve and rank == 0 and world == 1:
@@ -1101,6 +1119,7 @@ def run_gpu(args):
                           "frac": round(step_gbs / peaks["hbm_gbs"], 4)},
         "roofline": roofline,
         "cpu_baseline": cpu,
+        "parity_vs_oracle": parity,
         "plain_form": plain,
         "e2e": e2e,
         "gpu_launches": st["launches"],
