@@ -130,18 +130,26 @@ int run(kd_keymap* m, const uint64_t* keys, int64_t n, uint32_t* ids, int flags,
       kd_set_msg(s, "key map staging allocation failed");
       return KD_ENOMEM;
     }
-    cudaMemcpyAsync(tmp, keys, (size_t)n * 8, cudaMemcpyHostToDevice, str);
+  }
+  KdErrHost init{0, 0, -1}, got{};
+  cudaError_t e = cudaSuccess;
+  if (!dev) e = cudaMemcpyAsync(tmp, keys, (size_t)n * 8, cudaMemcpyHostToDevice, str);
+  if (!dev) {
     dk = (const unsigned long long*)tmp;
     dout = (unsigned*)((char*)tmp + (size_t)n * 8);
   }
-  KdErrHost init{0, 0, -1}, got{};
-  cudaMemcpyAsync(m->err, &init, sizeof init, cudaMemcpyHostToDevice, str);
-  const int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
-  k_keymap<<<grid, 256, 0, str>>>(m->keys, m->ids, m->counter, m->size, m->capacity, dk, n, dout,
-                                  insert ? 1 : 0, m->err);
-  cudaMemcpyAsync(&got, m->err, sizeof got, cudaMemcpyDeviceToHost, str);
-  if (!dev) cudaMemcpyAsync(ids, dout, (size_t)n * 4, cudaMemcpyDeviceToHost, str);
-  cudaError_t e = cudaStreamSynchronize(str);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->err, &init, sizeof init, cudaMemcpyHostToDevice, str);
+  if (e == cudaSuccess) {
+    const int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
+    k_keymap<<<grid, 256, 0, str>>>(m->keys, m->ids, m->counter, m->size, m->capacity, dk, n,
+                                    dout, insert ? 1 : 0, m->err);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&got, m->err, sizeof got, cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess && !dev)
+    e = cudaMemcpyAsync(ids, dout, (size_t)n * 4, cudaMemcpyDeviceToHost, str);
+  const cudaError_t es = cudaStreamSynchronize(str);
+  if (e == cudaSuccess) e = es;
   if (tmp) cudaFree(tmp);
   if (e != cudaSuccess) return kd_cuda_fail(s, e, "key map");
   if (got.code) {

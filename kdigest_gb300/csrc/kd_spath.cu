@@ -1543,7 +1543,13 @@ int sp_ensure(KdSession* s, KdStore* st) {
     cudaFree(bm);
     return sp_fail(s, KD_ENOMEM, "sample buffer allocation failed");
   }
-  cudaMemsetAsync(bc, 0, 64, s->stream);
+  if (cudaMemsetAsync(bc, 0, 64, s->stream) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(bc);
+    cudaFree(bm);
+    cudaFree(bw);
+    return sp_fail(s, KD_ENOMEM, "sample buffer initialisation failed");
+  }
   d.bcount = bc;
   d.buf_m = bm;
   d.buf_w = bw;
@@ -1795,17 +1801,22 @@ KD_API int kd_store_add(kd_store* h, const double* values, const double* weights
       return sp_fail(s, KD_ENOMEM, "sample staging allocation failed");
     }
     double* p = (double*)tmp;
-    cudaMemcpyAsync(p, values, (size_t)n * 8, cudaMemcpyHostToDevice, str);
+    cudaError_t e = cudaMemcpyAsync(p, values, (size_t)n * 8, cudaMemcpyHostToDevice, str);
     dv = p;
     p += n;
-    if (weights) {
-      cudaMemcpyAsync(p, weights, (size_t)n * 8, cudaMemcpyHostToDevice, str);
+    if (weights && e == cudaSuccess) {
+      e = cudaMemcpyAsync(p, weights, (size_t)n * 8, cudaMemcpyHostToDevice, str);
       dw = p;
       p += n;
     }
-    if (timestamps) {
-      cudaMemcpyAsync(p, timestamps, (size_t)n * 8, cudaMemcpyHostToDevice, str);
+    if (timestamps && e == cudaSuccess) {
+      e = cudaMemcpyAsync(p, timestamps, (size_t)n * 8, cudaMemcpyHostToDevice, str);
       dt = p;
+    }
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(str);
+      cudaFree(tmp);
+      return kd_cuda_fail(s, e, "sample staging");
     }
   }
   SpStatus r{};
