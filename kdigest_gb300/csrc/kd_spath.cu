@@ -135,6 +135,9 @@ struct SpSh {
   double f0, f1;  // the same with normaliser 1: k(q, nrm) = nrm * k(q, 1) at these q
   double nrm01;   // the K0 / K1 normaliser (it does not depend on the total)
   double inv_st;  // 1 / stored total, for approximate q (filters and speculation only)
+  double floor_w; // prune floor 1e-6 * e^{log_scale} of the current merge
+  double tot_u;   // ulp of the stored total's binade
+  long long tot_base;  // the stored total in units of tot_u
   int C, B, err, nc, mismatch, unsorted, exact, cut, renorm, pre_adv, integral, fast, filt;
   int longreach;  // a cluster start whose reach passed 64 candidates
   int bfail;      // a bucket of the buffer merge was too large
@@ -568,6 +571,7 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
   if (sh.err) return;
   const int W = C + B;
   // 2. totals: k limits use the effective total, q positions the stored one
+  if (threadIdx.x == 32 && decay) sh.floor_w = KD_MUL(SP_PRUNE_EPS, kd_exp(sh.ls));
   if (threadIdx.x == 0) {
     if (scale <= KD_SCALE_K1) {
       sh.nrm = sh.nrm01;
@@ -921,11 +925,18 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
     __syncthreads();
     nc = sh.nc;
   }
-  // 9. prune decayed mass (tdigest.mojo:441-458)
+  // 9. prune decayed mass (tdigest.mojo:441-458): a parallel test first; the
+  //    serial removal (its sum is in centroid order) only when something goes
+  if (threadIdx.x == 0) sh.bfail = 0;  // here: some centroid falls below the floor
+  __syncthreads();
+  if (decay)
+    for (int i = threadIdx.x; i < nc; i += SP_T)
+      if (!(m.cw[i] >= sh.floor_w)) sh.bfail = 1;
+  __syncthreads();
   if (threadIdx.x == 0) {
     int c = nc;
-    if (decay) {
-      const double floor_w = KD_MUL(SP_PRUNE_EPS, kd_exp(sh.ls));
+    if (decay && sh.bfail) {
+      const double floor_w = sh.floor_w;
       int k = 0;
       double removed = 0.0;
       for (int i = 0; i < c; ++i) {
@@ -1019,6 +1030,77 @@ __device__ void sp_reduce_minmax(SpPick& mn, SpPick& mx, SpPick* red) {
 // The add loop over samples [0, n_eff) (tdigest.mojo:153-175, 334-350): each
 // sample advances the clock, is buffered with its decay-scaled weight, and a
 // full buffer runs the merge pass.
+// st += w_0 + w_1 + ... (bw[B0 .. B0 + cut)), added in order.  Inside the
+// binade [2^E, 2^(E+1)) of st every sum st + w rounds to st + round(w / u) * u
+// with u = 2^(E-52), the same rounding for every st, unless w / u lies exactly
+// half-way between integers.  So while st stays below 2^(E+1) - 2u the serial
+// sum is st plus the integer prefix of round(w / u), in units of u: one block
+// scan.  A step that would leave the binade, a tie, and what follows them are
+// added one at a time.
+__device__ void sp_add_total(const SpMem& m, SpSh& sh, int B0, int cut) {
+  if (threadIdx.x == 0) {
+    const double st = sh.st;
+    const unsigned long long b = kd_bits(st);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    sh.fast = st > 0.0 && ex > 53 && ex < 2000;  // normal, positive, u a normal power of two
+    if (sh.fast) {
+      sh.tot_u = kd_pow2i(ex - 1075);                        // u
+      sh.tot_base = (long long)KD_MUL(st, kd_pow2i(1075 - ex)); // st / u, in [2^52, 2^53)
+    }
+  }
+  __syncthreads();
+  const double* const bw = m.bw + B0;
+  long long* const nk = m.pi;  // free outside merges
+  int first_bad = cut;
+  if (sh.fast) {
+    const double inv_u = kd_pow2i(1075 - (int)((kd_bits(sh.st) >> 52) & 0x7ff));
+    const int per = (cut + SP_T - 1) / SP_T;
+    const int k0 = threadIdx.x * per, k1 = min(cut, k0 + per);
+    long long sum = 0;
+    int bad = cut;
+    for (int k = k0; k < k1; ++k) {
+      const double t = KD_MUL(bw[k], inv_u);  // exact: a power-of-two scale
+      long long n = 0;
+      if (!(t < 1099511627776.0)) {           // 2^40: far beyond the binade anyway
+        if (bad == cut) bad = k;
+        n = 1LL << 40;
+      } else {
+        const double f = floor(t);
+        const double fr = KD_SUB(t, f);  // exact
+        if (fr == 0.5 && bad == cut) bad = k;  // a tie: rounding depends on st
+        n = (long long)f + (fr > 0.5 ? 1 : 0);
+      }
+      nk[k] = n;
+      sum += n;
+    }
+    if (bad < cut) atomicMin(&sh.cut, bad);  // sh.cut is free here: reused as "first bad"
+    long long total;
+    long long run = sp_iscan(sum, sh, &total);
+    const long long limit = (1LL << 53) - 2 - sh.tot_base;
+    for (int k = k0; k < k1; ++k) {
+      run += nk[k];
+      if (run > limit) {
+        atomicMin(&sh.cut, k);
+        break;
+      }
+      nk[k] = run;  // inclusive prefix
+    }
+    __syncthreads();
+    first_bad = sh.cut;
+  }
+  if (threadIdx.x == 0) {
+    double st = sh.st;
+    int k = 0;
+    if (sh.fast && first_bad > 0) {  // exact: st + prefix * u stays below 2^(E+1) - u
+      st = KD_MUL((double)(sh.tot_base + nk[first_bad - 1]), sh.tot_u);
+      k = first_bad;
+    }
+    for (; k < cut; ++k) st = KD_ADD(st, bw[k]);
+    sh.st = st;
+  }
+  __syncthreads();
+}
+
 __device__ __noinline__ void sp_add_decay(const SpArgs& a, const SpMem& m, SpSh& sh, long long n_eff,
                              SpPick* red) {
   const bool decay = true;
@@ -1164,36 +1246,19 @@ __device__ __noinline__ void sp_add_decay(const SpArgs& a, const SpMem& m, SpSh&
         mn = SpPick{kd_order_key(sh.mn), -1, sh.mn};
         mx = SpPick{kd_order_key(sh.mx), -1, sh.mx};
       }
-      long long part = 0;  // integral weights sum exactly in integers
       for (int k = threadIdx.x; k < cut; k += SP_T) {
         const double v = m.bm[B0 + k];
         const SpPick p{kd_order_key(v), (long long)k, v};
         mn = sp_pick_min(mn, p);
         mx = sp_pick_max(mx, p);
-        long long x = 0;
-        sp_int53(m.bw[B0 + k], &x);
-        part += x;
       }
       sp_reduce_minmax(mn, mx, red);
-      const bool int_w = sh.integral && !decay;
-      const long long sum = int_w ? sp_isum(part, sh) : 0;
       if (threadIdx.x == 0) {
         sh.mn = mn.v;
         sh.mx = mx.v;
-        double tot = sh.st;
-        // an exact total: integral weights and a total below 2^53 sum in any order
-        bool exact = int_w && tot == floor(tot) && tot >= 0.0 && tot <= 4503599627370496.0 &&
-                     sum <= (1LL << 52);
-        if (exact) tot = KD_ADD(tot, (double)sum);
-        if (!exact) {
-          tot = sh.st;
-          const double* const bw = m.bw + B0;
-#pragma unroll 8
-          for (int k = 0; k < cut; ++k) tot = KD_ADD(tot, bw[k]);
-        }
-        sh.st = tot;
-        sh.B = B0 + cut;
       }
+      sp_add_total(m, sh, B0, cut);  // the stored total, as the serial sum gives it
+      if (threadIdx.x == 0) sh.B = B0 + cut;
       __syncthreads();
     }
     i += cut;
