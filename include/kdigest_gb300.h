@@ -62,6 +62,7 @@ extern "C" {
 #define KD_OPT_SMALL_TILE_CAP 5       /* largest tile for the small-tile kernel, 1..128 */
 #define KD_OPT_LARGE_BLOCKS_PER_SM 6  /* grid of the large-tile kernel, blocks per SM */
 #define KD_OPT_SMALL_BLOCKS_PER_SM 7  /* grid of the small-tile kernel, blocks per SM */
+#define KD_OPT_CONCURRENT_TILES 8     /* run the two tile kernels of a level on two streams */
 
 typedef struct kd_session kd_session;
 typedef struct kd_store kd_store;

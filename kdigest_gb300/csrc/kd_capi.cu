@@ -62,7 +62,8 @@ void kd_ws_free(KdWorkspace& w) {
                   w.tkey, w.tstart, w.tm, w.tprior, w.tbuf, w.tsf, w.tpscale, w.tmap,
                   w.st_clock, w.st_ls, w.st_min, w.st_max, w.st_count, w.lv_storage,
                   w.work[0], w.work[1], w.work[2], w.work[3], w.dx[0], w.dx[1], w.dw[0], w.dw[1], w.scr_m, w.scr_w,
-                  w.tcount, w.doff, w.needs, w.totals, w.d_call, w.rs_epoch_base, w.fix};
+                  w.tcount, w.doff, w.needs, w.totals, w.d_call, w.rs_epoch_base, w.fix,
+                  w.kfirst, w.kstamp, w.kepoch};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (w.h_call) cudaFreeHost(w.h_call);
@@ -83,7 +84,7 @@ static size_t ws_bytes(long long n, long long keys, long long inter, long long w
   b += (size_t)kd_rs_blocks(n) * 256 * 8 + KD_RS_MAXPASS * 256 * 4 + 8;
   b += (size_t)partials * sizeof(int4);
   b += (size_t)keys * (4 * 4 + 1 + 8 * 6) + (size_t)keys * 8 * 4 * 2;
-  b += (size_t)tmap * 4;
+  b += (size_t)tmap * (4 + 4 + 8) + 8;
   b += (size_t)work * 8 * 4;
   b += (size_t)merged * 16 * 2;
   b += (size_t)inter * (KD_TILE * 16 + 8);
@@ -158,6 +159,13 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
   ok &= A((void**)&w.tsf, sizeof(double) * kk);
   ok &= A((void**)&w.tpscale, sizeof(double) * kk);
   ok &= A((void**)&w.tmap, sizeof(uint32_t) * tt);
+  ok &= A((void**)&w.kfirst, sizeof(int) * tt);
+  ok &= A((void**)&w.kstamp, sizeof(unsigned long long) * tt);
+  ok &= A((void**)&w.kepoch, sizeof(unsigned long long));
+  if (ok) {  // no key carries a stamp; the first step's epoch is 1
+    cudaMemset(w.kstamp, 0, sizeof(unsigned long long) * tt);
+    cudaMemset(w.kepoch, 0, sizeof(unsigned long long));
+  }
   ok &= A((void**)&w.st_clock, sizeof(double) * kk);
   ok &= A((void**)&w.st_ls, sizeof(double) * kk);
   ok &= A((void**)&w.st_min, sizeof(double) * kk);
@@ -369,6 +377,16 @@ KD_API int kd_session_create(int device, size_t mem_budget, kd_session** out) {
     delete h;
     return KD_ECUDA;
   }
+  if (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    if (s->fork_ev) cudaEventDestroy(s->fork_ev);
+    if (s->side) cudaStreamDestroy(s->side);
+    cudaStreamDestroy(s->stream);
+    delete h;
+    return KD_ECUDA;
+  }
   cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, device);
   *out = h;
   return KD_OK;
@@ -400,6 +418,9 @@ KD_API void kd_session_destroy(kd_session* h) {
   kd_ws_free(s->ws);
   for (int i = 0; i <= KD_NSTAGES; ++i)
     if (s->stats.ev[i]) cudaEventDestroy(s->stats.ev[i]);
+  cudaEventDestroy(s->join_ev);
+  cudaEventDestroy(s->fork_ev);
+  cudaStreamDestroy(s->side);
   cudaStreamDestroy(s->stream);
   delete h;
 }
@@ -458,6 +479,8 @@ KD_API int kd_session_set_option(kd_session* h, int option, int value) {
   } else if (option == KD_OPT_SMALL_BLOCKS_PER_SM) {
     if (value < 1 || value > 64) return fail(s, KD_EINVAL, "blocks per SM must be in [1, 64]");
     s->small_bps = value;
+  } else if (option == KD_OPT_CONCURRENT_TILES) {
+    s->concurrent_tiles = value ? 1 : 0;
   } else {
     return fail(s, KD_EINVAL, "unknown option");
   }

@@ -113,6 +113,13 @@ struct KdWorkspace {
   double* tpscale = nullptr;
   uint32_t* tmap = nullptr;  // key -> touched ordinal (valid for touched keys only)
   long long cap_tmap = 0;
+  // Key-level touched detection (cap_tmap entries each): the sort's unpack
+  // stamps every key that starts a run with the step's epoch and records the
+  // run's start; a scan over the keys then lists the touched ones.  Null in
+  // workspaces without them (the element-level scan is used).
+  int* kfirst = nullptr;
+  unsigned long long* kstamp = nullptr;
+  unsigned long long* kepoch = nullptr;  // advanced by every step's k_prep
   double* st_clock = nullptr;
   double* st_ls = nullptr;
   double* st_min = nullptr;
@@ -179,6 +186,11 @@ struct KdSession {
   int small_cap = 128;
   int large_bps = 6;
   int small_bps = 8;
+  // Run a level's two tile kernels on two streams (the second joins back
+  // before anything reads their outputs).  Also a launch setting only.
+  int concurrent_tiles = 1;
+  cudaStream_t side = nullptr;  // second stream for the small-tile kernel
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   char last_error[256] = {0};  // fixed buffer: reporting an error never allocates
   KdWorkspace ws;
   KdStageStats stats;

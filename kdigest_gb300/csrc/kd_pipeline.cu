@@ -761,7 +761,9 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
 // form and the exact order among them.
 __global__ void k_prep(long long n, const KdCallArgs* __restrict__ call, long long K, int kb,
                        uint64_t* __restrict__ k64, uint32_t* __restrict__ kout,
-                       uint32_t* __restrict__ idx, KdErrHost* err) {
+                       uint32_t* __restrict__ idx, KdErrHost* err,
+                       unsigned long long* __restrict__ kepoch) {
+  if (kepoch && blockIdx.x == 0 && threadIdx.x == 0) *kepoch += 1;  // this step's stamp
   const uint32_t* __restrict__ keys = call->keys;
   const double* __restrict__ vals = call->vals;
   const double* __restrict__ wts = call->wts;
@@ -813,6 +815,32 @@ struct TouchedDst {
   }
 };
 
+// Key-level form of the same list, used when the batch has at least as many
+// samples as the store has keys: k_unpack stamped every key that starts a
+// run of the sorted batch, so the touched keys are the stamped ones, listed in
+// key order - which is the order of their runs.
+struct KeyTouchedSrc {
+  const unsigned long long* kstamp;
+  const unsigned long long* kepoch;
+  __device__ int4 operator()(long long k) const {
+    return make_int4(kstamp[k] == *kepoch ? 1 : 0, 0, 0, 0);
+  }
+};
+struct KeyTouchedDst {
+  const int* kfirst;
+  uint32_t* tkey;
+  int* tstart;
+  uint32_t* tmap;
+  long long cap;
+  __device__ void operator()(long long k, int4 excl, int4 v) const {
+    if (v.x && excl.x < cap) {
+      tkey[excl.x] = (uint32_t)k;
+      tstart[excl.x] = kfirst[k];
+      tmap[k] = (uint32_t)excl.x;
+    }
+  }
+};
+
 struct PrepareArgs {
   KdStoreDev s;
   long long n;
@@ -842,21 +870,31 @@ struct PrepareArgs {
 // Samples of one key that agree in the sorted bits form a run in input order;
 // an element smaller than its left neighbour inside such a run is recorded in
 // the repair list (fix[0] = count, fix[1..cap]).  Runs of equal values record
-// nothing.  A full list sends the step to the full sort.
+// nothing.  A full list sends the step to the full sort.  With kstamp set, the
+// first element of every key's run stamps the key with the step's epoch and
+// records its position in kfirst.
 __global__ void k_unpack(long long n, int kb, int shift, const uint64_t* __restrict__ sk,
                          const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx,
                          uint64_t* __restrict__ dk, uint32_t* __restrict__ dkey,
                          uint32_t* __restrict__ didx, int* __restrict__ fix, int cap_fix,
-                         KdErrHost* err) {
+                         KdErrHost* err, long long K, int* __restrict__ kfirst,
+                         unsigned long long* __restrict__ kstamp,
+                         const unsigned long long* __restrict__ kepoch) {
+  const unsigned long long epoch = kstamp ? *kepoch : 0ull;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const uint64_t p = sk[i];
     const uint64_t ok = (p << kb) | (uint64_t)skey[i];
+    const uint32_t key = kb > 0 ? (uint32_t)(p >> (64 - kb)) : 0u;
     dk[i] = ok;
-    dkey[i] = kb > 0 ? (uint32_t)(p >> (64 - kb)) : 0u;
+    dkey[i] = key;
     if (didx) didx[i] = sidx[i];
+    const uint64_t pp = i > 0 ? sk[i - 1] : 0ull;
+    if (kstamp && (long long)key < K && (i == 0 || (kb > 0 && (uint32_t)(pp >> (64 - kb)) != key))) {
+      kfirst[key] = (int)i;
+      kstamp[key] = epoch;
+    }
     if (i > 0) {
-      const uint64_t pp = sk[i - 1];
       if ((pp >> shift) == (p >> shift) && ((pp << kb) | (uint64_t)skey[i - 1]) > ok) {
         const int slot = atomicAdd(&fix[0], 1);
         if (slot < cap_fix) fix[1 + slot] = (int)i;
@@ -1875,8 +1913,19 @@ static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, co
     ta.totals = level0->totals;
     ta.n = level0->n;
   }
-  k_tiles_blk<<<s->num_sms * s->large_bps, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
-  k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * s->small_bps, 128, tile_smem_small(), str>>>(ta);
+  if (s->concurrent_tiles && s->side) {
+    // fork: the small-tile kernel on the side stream, joined back before the
+    // next launch on the session stream (inside a capture: a graph branch)
+    v.note(cudaEventRecord(s->fork_ev, str));
+    v.note(cudaStreamWaitEvent(s->side, s->fork_ev, 0));
+    k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * s->small_bps, 128, tile_smem_small(), s->side>>>(ta);
+    v.note(cudaEventRecord(s->join_ev, s->side));
+    k_tiles_blk<<<s->num_sms * s->large_bps, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
+    v.note(cudaStreamWaitEvent(str, s->join_ev, 0));
+  } else {
+    k_tiles_blk<<<s->num_sms * s->large_bps, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
+    k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * s->small_bps, 128, tile_smem_small(), str>>>(ta);
+  }
   v.launches += 2;
 }
 
@@ -1934,7 +1983,7 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   {
     int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
     k_prep<<<grid, 256, 0, str>>>(n, w.d_call, sd.K, full_sort ? 0 : key_bits, w.k64[0], w.key[0],
-                                  with_idx ? w.idx[0] : nullptr, w.err);
+                                  with_idx ? w.idx[0] : nullptr, w.err, w.kepoch);
     v.launches += 1;
   }
   stage_mark(s, 1);
@@ -1945,12 +1994,17 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   const int sort_bits = full_sort ? key_bits : 0;  // packed keys need no key passes
   int r = kd_radix_sort(sb, n, sort_bits, with_idx, s->num_sms, str, first_digit);
   v.launches += kd_radix_sort_launches(n, sort_bits, first_digit);
+  // Touched keys from the key-level stamps when the batch has at least as
+  // many samples as the store has keys (a scan over K instead of over n).
+  const bool key_level = !full_sort && w.kstamp && sd.K <= n && sd.K <= w.cap_tmap;
   if (!full_sort) {  // also for n == 1: the key is still packed
     const int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
     const int shift = 8 * first_digit;
     k_unpack<<<grid, 256, 0, str>>>(n, key_bits, shift, w.k64[r], w.key[r],
                                     with_idx ? w.idx[r] : nullptr, w.k64[r ^ 1], w.key[r ^ 1],
-                                    with_idx ? w.idx[r ^ 1] : nullptr, w.fix, (int)w.cap_fix, w.err);
+                                    with_idx ? w.idx[r ^ 1] : nullptr, w.fix, (int)w.cap_fix, w.err,
+                                    sd.K, key_level ? w.kfirst : nullptr,
+                                    key_level ? w.kstamp : nullptr, w.kepoch);
     k_repair<<<s->num_sms, 256, 0, str>>>(n, key_bits, shift, w.k64[r], w.key[r], w.k64[r ^ 1],
                                           with_idx ? w.idx[r ^ 1] : nullptr, w.fix, (int)w.cap_fix,
                                           w.err);
@@ -1961,8 +2015,13 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   const uint64_t* k64 = w.k64[r];
   const uint32_t* skey = w.key[r];
   const uint32_t* sidx = with_idx ? w.idx[r] : nullptr;
-  kd_scan(TouchedSrc{skey}, TouchedDst{skey, w.tkey, w.tstart, w.tmap, w.cap_keys, sd.K}, n,
-          w.partials, &w.totals[0], str);
+  if (key_level)
+    kd_scan(KeyTouchedSrc{w.kstamp, w.kepoch},
+            KeyTouchedDst{w.kfirst, w.tkey, w.tstart, w.tmap, w.cap_keys}, sd.K, w.partials,
+            &w.totals[0], str);
+  else
+    kd_scan(TouchedSrc{skey}, TouchedDst{skey, w.tkey, w.tstart, w.tmap, w.cap_keys, sd.K}, n,
+            w.partials, &w.totals[0], str);
   {
     PrepareArgs pa{sd, n, k64, w.tkey, w.tstart, w.totals, mode, w.d_call, w.tm, w.tprior,
                    w.tbuf, w.tsf, w.tpscale, w.st_clock, w.st_ls, w.st_min, w.st_max, w.err};
@@ -2046,7 +2105,7 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
   key.scale = sd.scale;
   key.compression = sd.compression;
   key.generation = w.generation;
-  key.tuning = s->small_cap | (s->large_bps << 8) | (s->small_bps << 16);
+  key.tuning = s->small_cap | (s->large_bps << 8) | (s->small_bps << 16) | (s->concurrent_tiles << 24);
   KdStepView v;
   bool ran = false;
   if (s->use_graphs && w.generation != 0) {

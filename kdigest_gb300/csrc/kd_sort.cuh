@@ -18,9 +18,16 @@
 
 #include "kd_scan.cuh"
 
+#ifndef KD_RS_THREADS
 #define KD_RS_THREADS 256
+#endif
+#ifndef KD_RS_MIN_BLOCKS
+#define KD_RS_MIN_BLOCKS 3
+#endif
 #define KD_RS_WARPS (KD_RS_THREADS / 32)
+#ifndef KD_RS_PER_WARP
 #define KD_RS_PER_WARP 512
+#endif
 #define KD_RS_ROUNDS (KD_RS_PER_WARP / 32)
 #define KD_RS_TILE (KD_RS_WARPS * KD_RS_PER_WARP)
 #define KD_RS_MAXPASS 12
@@ -82,10 +89,12 @@ struct KdRsPass {
   int* err_code;  // device status word (KdErr.code)
 };
 
+#ifndef KD_LB_WINDOW
 #define KD_LB_WINDOW 16
+#endif
 
 template <bool kIdx>
-__global__ void __launch_bounds__(KD_RS_THREADS, 3) kd_rs_onesweep(KdRsPass a) {
+__global__ void __launch_bounds__(KD_RS_THREADS, KD_RS_MIN_BLOCKS) kd_rs_onesweep(KdRsPass a) {
   extern __shared__ __align__(16) unsigned char rs_smem[];
   uint64_t* sk = reinterpret_cast<uint64_t*>(rs_smem);
   uint32_t* skey = reinterpret_cast<uint32_t*>(sk + KD_RS_TILE);

@@ -13,6 +13,7 @@ up), then runs a coordinate descent over
     small tile cap   in {32, 64, 96, 128}
     large blocks/SM  in {4, 5, 6, 7, 8}
     small blocks/SM  in {4, 6, 8, 12, 16}
+    concurrent tiles in {0, 1} (the two kernels of a level on two streams)
 timing each candidate as the median device time (CUDA events on the session
 stream) of several ingest steps, and writes the measurements and the choice to
 tuning/gb300.json.  GpuSession applies that file's choice; the library's
@@ -33,9 +34,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TUNING_FILE = os.path.join(HERE, "tuning", "gb300.json")
 PARAMS = (("small_tile_cap", 5, (32, 64, 96, 128)),
           ("large_blocks_per_sm", 6, (4, 5, 6, 7, 8)),
-          ("small_blocks_per_sm", 7, (4, 6, 8, 12, 16)))
+          ("small_blocks_per_sm", 7, (4, 6, 8, 12, 16)),
+          ("concurrent_tiles", 8, (0, 1)))
 # the starting point of the search (the launch shapes before tuning)
-DEFAULTS = {"small_tile_cap": 128, "large_blocks_per_sm": 6, "small_blocks_per_sm": 8}
+DEFAULTS = {"small_tile_cap": 128, "large_blocks_per_sm": 6, "small_blocks_per_sm": 8,
+            "concurrent_tiles": 0}
 
 
 def load_tuning(path: str = TUNING_FILE) -> dict:

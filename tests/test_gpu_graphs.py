@@ -122,16 +122,19 @@ def test_replays_with_stage_timing(kd):
 
 
 def test_launch_tuning_never_changes_results(kd):
-    """Every tile-kernel split and grid gives the same digests."""
+    """Every tile-kernel split and grid, serial or on two streams, eager or
+    replayed, gives the same digests."""
     nk, n = 500, 60000
     rng = np.random.default_rng(7)
     batches = [(rng.zipf(1.2, n) % nk, rng.standard_normal(n) * 3.0) for _ in range(4)]
     ref = None
-    for cap, lb, sb in ((128, 6, 8), (32, 4, 16), (64, 8, 4), (1, 1, 1)):
+    for cap, lb, sb, cc in ((128, 6, 8, 0), (32, 4, 16, 0), (64, 8, 4, 0), (1, 1, 1, 0),
+                            (128, 6, 8, 1), (64, 4, 16, 1)):
         s = kd.GpuSession(tuned=False)
         s.set_option(5, cap)
         s.set_option(6, lb)
         s.set_option(7, sb)
+        s.set_option(8, cc)  # KD_OPT_CONCURRENT_TILES: the two tile kernels on two streams
         g = kd.GroupedTDigest(nk, 100.0, scale=kd.K3, session=s)
         for k, v in batches:
             g.add_batch(k, v)

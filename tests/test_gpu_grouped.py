@@ -131,6 +131,38 @@ def test_device_side_validation_leaves_state_unchanged(kd):
         assert np.array_equal(g.centroids(k)[0], before[k][0])
 
 
+def test_touched_keys_key_level_and_element_level(kd, oracle):
+    """Batches with at least as many samples as keys list their touched keys
+    from per-key stamps, smaller ones by a scan over the samples.  Two stores
+    of one session alternate (their steps share the stamp array), a batch
+    holds a key in [K, 2^ceil(log2 K)) that only the device check sees, and
+    every store still equals the oracle bit for bit."""
+    import kdigest_gb300._native as N
+    sess = kd.GpuSession()
+    sizes = (1000, 50)
+    stores = [kd.GroupedTDigest(k, 100.0, scale=kd.K1, session=sess) for k in sizes]
+    refs = [[oracle.Digest(oracle.K1, 100.0, 0.0) for _ in range(k)] for k in sizes]
+    rng = np.random.default_rng(0x70C)
+    for step in range(6):
+        for g, r, nk in zip(stores, refs, sizes):
+            n = 3000 if step % 2 == 0 else 400  # above / below the key count of the first store
+            keys = (rng.zipf(1.3, n) - 1) % nk
+            vals = rng.standard_normal(n) + keys % 11
+            g.add_batch(keys, vals)
+            oracle.grouped_add_batch(r, keys, vals)
+        if step == 2:
+            before = stores[0].centroid_counts().copy()
+            keys = (np.arange(2000) % 1000).astype(np.uint32)
+            keys[1234] = 1010  # below 2^10, above the store's 1000 keys
+            vals = rng.standard_normal(2000)
+            rc = N.load().kd_store_ingest(stores[0]._store._h, N.ptr(keys), N.ptr(vals), 2000, 0,
+                                          0.0, 0)
+            assert rc == N.KD_EINVAL
+            assert np.array_equal(stores[0].centroid_counts(), before)
+    for g, r, nk in zip(stores, refs, sizes):
+        _assert_same(g, r, range(nk), f"K={nk}")
+
+
 def test_time_clock_decay(kd, oracle):
     lam = oracle.log(2.0) / 60.0
     nk = 20
