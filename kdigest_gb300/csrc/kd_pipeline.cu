@@ -1555,22 +1555,28 @@ struct CommitArgs {
 
 // _gpu_batch_finish (tdigest.mojo:298-315) + _prune (:441-458) per key, the
 // quantile-walk prefix (:526-536), then publication of the new slot.
-// One lane per key keeps every lane of a warp on useful FP64 work.
-__global__ void k_commit(CommitArgs a) {
-  const int U = a.totals[0].x;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j == 0 && *a.remaining > 0) kd_err_set(a.err, KD_EMORE_LEVELS, *a.remaining);
-  if (j >= U) return;
-  if (kd_err_get(a.err) || *a.remaining > 0) return;
-  const KdStoreDev& s = a.s;
-  const uint32_t key = a.tkey[j];
-  const int b = a.tbuf[j];
+__device__ __forceinline__ void commit_header(const KdStoreDev& s, const CommitArgs& a, long long j,
+                                              uint32_t key, int b, int cnt, double total) {
+  const double ls = a.st_ls[j];
+  s.count[key] = cnt;
+  s.total[key] = total;
+  s.log_scale[key] = ls;
+  s.clock[key] = a.st_clock[j];
+  s.min_v[key] = a.st_min[j];
+  s.max_v[key] = a.st_max[j];
+  s.dfac[key] = s.lambda > 0.0 ? kd_exp(-ls) : 1.0;
+  if (s.bcount) s.bcount[key] = 0;  // a carried batch consumed the buffer
+  s.cur[key] = (unsigned char)b;
+}
+
+// The serial form: stored total, prune (decay only), walk prefix; returns the
+// count after the prune.
+__device__ int commit_serial(const KdStoreDev& s, uint32_t key, int b, int cnt, double ls,
+                             double* total_out) {
   double* m = s.slot_m + slot_base(s.K, b, key);
   double* w = s.slot_w + slot_base(s.K, b, key);
-  int cnt = a.st_count[j];
   double total = 0.0;
   for (int i = 0; i < cnt; ++i) total = KD_ADD(total, w[i]);
-  const double ls = a.st_ls[j];
   if (s.lambda > 0.0) {
     const double floor_w = KD_MUL(1e-6, kd_exp(ls));
     int k = 0;
@@ -1599,15 +1605,70 @@ __global__ void k_commit(CommitArgs a) {
       P[i + 1] = run;
     }
   }
-  s.count[key] = cnt;
-  s.total[key] = total;
-  s.log_scale[key] = ls;
-  s.clock[key] = a.st_clock[j];
-  s.min_v[key] = a.st_min[j];
-  s.max_v[key] = a.st_max[j];
-  s.dfac[key] = s.lambda > 0.0 ? kd_exp(-ls) : 1.0;
-  if (s.bcount) s.bcount[key] = 0;  // a carried batch consumed the buffer
-  s.cur[key] = (unsigned char)b;
+  *total_out = total;
+  return cnt;
+}
+
+// With decay: one lane per key, so that the serial FP64 sums keep every lane
+// of a warp busy.
+__global__ void __launch_bounds__(128) k_commit(CommitArgs a) {
+  const int U = a.totals[0].x;
+  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j == 0 && *a.remaining > 0) kd_err_set(a.err, KD_EMORE_LEVELS, *a.remaining);
+  if (j >= U) return;
+  if (kd_err_get(a.err) || *a.remaining > 0) return;
+  const uint32_t key = a.tkey[j];
+  const int b = a.tbuf[j];
+  double total = 0.0;
+  const int cnt = commit_serial(a.s, key, b, a.st_count[j], a.st_ls[j], &total);
+  commit_header(a.s, a, j, key, b, cnt, total);
+}
+
+// Without decay (no prune): one warp per key.  When all of a key's weights are
+// integral (every unit-weight ingest), its stored total and walk prefix are
+// exact in integers: prefix[i] = sum(w[0..i)) + w[i] / 2 with total < 1024 *
+// 2^42, so every partial sum and half-sum the serial form computes is exact
+// and a warp scan over the centroids gives the same bits.  Other keys take
+// the serial form on lane 0.
+__global__ void __launch_bounds__(256) k_commit_warp(CommitArgs a) {
+  const int U = a.totals[0].x;
+  const int lane = threadIdx.x & 31;
+  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  if (warp0 == 0 && lane == 0 && *a.remaining > 0) kd_err_set(a.err, KD_EMORE_LEVELS, *a.remaining);
+  int stop = 0;
+  if (lane == 0) stop = (kd_err_get(a.err) || *a.remaining > 0) ? 1 : 0;
+  if (__shfl_sync(0xffffffffu, stop, 0)) return;  // warp-uniform
+  const KdStoreDev& s = a.s;
+  for (long long j = warp0; j < U; j += nwarps) {
+    const uint32_t key = a.tkey[j];
+    const int b = a.tbuf[j];
+    int cnt = a.st_count[j];
+    const double* w = s.slot_w + slot_base(s.K, b, key);
+    bool integral = true;
+    for (int i = lane; i < cnt; i += 32) integral = integral && kd_is_small_int(w[i]);
+    double total = 0.0;
+    if (__all_sync(0xffffffffu, integral)) {
+      double* P = s.prefix + (size_t)key * KD_TILE;
+      long long carry = 0;
+      for (int i0 = 0; i0 < cnt; i0 += 32) {
+        const int i = i0 + lane;
+        const long long wi = i < cnt ? kd_small_int(w[i]) : 0;
+        long long incl = wi;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const long long t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        if (i < cnt) P[i] = KD_MUL((double)(2 * (carry + incl - wi) + wi), 0.5);
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      total = (double)carry;
+    } else if (lane == 0) {
+      cnt = commit_serial(s, key, b, cnt, a.st_ls[j], &total);
+    }
+    if (lane == 0) commit_header(s, a, j, key, b, cnt, total);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1957,7 +2018,11 @@ static void enqueue_tail(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, lon
   stage_mark(s, 5);
   CommitArgs ca{sd, w.totals, w.tkey, w.tbuf, w.st_count, w.st_clock, w.st_ls, w.st_min,
                 w.st_max, v.curA, w.err};
-  k_commit<<<(int)((keys_max + 127) / 128), 128, 0, str>>>(ca);
+  if (sd.lambda > 0.0)
+    k_commit<<<(int)((keys_max + 127) / 128), 128, 0, str>>>(ca);
+  else
+    k_commit_warp<<<(int)std::min<long long>((keys_max + 7) / 8, (long long)s->num_sms * 16), 256, 0,
+                    str>>>(ca);
   v.launches += 1;
   stage_mark(s, 6);
   v.note(cudaGetLastError());
