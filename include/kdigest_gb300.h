@@ -106,6 +106,19 @@ KD_API void kd_store_destroy(kd_store* st);
  * The whole batch is validated before any digest changes. */
 KD_API int kd_store_ingest(kd_store* st, const uint32_t* keys, const double* values, int64_t n,
                            int clock_mode, double timestamp, int flags);
+/* A sequence of GroupedTDigest.add_batch calls (grouped.mojo:60-162), batch i
+ * being keys[i] / values[i] / n[i] (keys NULL, or keys[i] NULL: all key 0) at
+ * timestamps[i] (KD_CLOCK_TIME only).  Results are those of one
+ * kd_store_ingest per batch, in order; the sort of each batch overlaps the
+ * compress of the one before.  Stops at the first failing batch: the batches
+ * before it stay committed, it and every later one change nothing, and
+ * *batches_done (may be NULL) receives its position (nbatch on success).
+ * Device pointers (KD_PTR_DEVICE) or pinned host memory are read in place;
+ * pageable host memory runs one kd_store_ingest per batch.  No reference
+ * counterpart beyond the add_batch loop it replaces. */
+KD_API int kd_store_ingest_many(kd_store* st, int64_t nbatch, const uint32_t* const* keys,
+                                const double* const* values, const int64_t* n, int clock_mode,
+                                const double* timestamps, int flags, int64_t* batches_done);
 
 /* The single-sample path of a one-key store (TDigest.add / add_at,
  * tdigest.mojo:153-175, 324-458): the reference's add loop over n samples in

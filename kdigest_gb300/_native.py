@@ -34,7 +34,7 @@ EXPORTED = (
     "kd_server_flush", "kd_server_stats", "kd_server_destroy",
     "kd_store_export", "kd_store_import",
     "kd_keymap_create", "kd_keymap_map", "kd_keymap_lookup", "kd_keymap_size", "kd_keymap_destroy",
-    "kd_store_add", "kd_store_flush", "kd_store_merge_into",
+    "kd_store_add", "kd_store_flush", "kd_store_merge_into", "kd_store_ingest_many",
 )
 KD_REQ_INGEST, KD_REQ_QUANTILE, KD_REQ_CDF = 0, 1, 2
 
@@ -83,6 +83,8 @@ def load(path: str = LIB_PATH):
     L.kd_store_create.argtypes = [_P, _I64, ctypes.c_int, _D, _D, ctypes.POINTER(_P)]
     L.kd_store_destroy.argtypes = [_P]
     L.kd_store_ingest.argtypes = [_P, _P, _P, _I64, ctypes.c_int, _D, ctypes.c_int]
+    L.kd_store_ingest_many.argtypes = [_P, _I64, _P, _P, _P, ctypes.c_int, _P, ctypes.c_int,
+                                       ctypes.POINTER(_I64)]
     L.kd_store_quantile.argtypes = [_P, _P, _P, _I64, _P, ctypes.c_int]
     L.kd_store_cdf.argtypes = [_P, _P, _P, _I64, _P, ctypes.c_int]
     L.kd_store_merge.argtypes = [_P, _P, _P, _P, _I64]

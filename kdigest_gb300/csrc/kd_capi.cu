@@ -63,7 +63,7 @@ void kd_ws_free(KdWorkspace& w) {
                   w.st_clock, w.st_ls, w.st_min, w.st_max, w.st_count, w.lv_storage,
                   w.work[0], w.work[1], w.work[2], w.work[3], w.dx[0], w.dx[1], w.dw[0], w.dw[1], w.scr_m, w.scr_w,
                   w.tcount, w.doff, w.needs, w.totals, w.d_call, w.rs_epoch_base, w.fix,
-                  w.kfirst, w.kstamp, w.kepoch};
+                  w.kfirst, w.kstamp, w.kepoch, w.chain};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (w.h_call) cudaFreeHost(w.h_call);
@@ -84,7 +84,7 @@ static size_t ws_bytes(long long n, long long keys, long long inter, long long w
   b += (size_t)kd_rs_blocks(n) * 256 * 8 + KD_RS_MAXPASS * 256 * 4 + 8;
   b += (size_t)partials * sizeof(int4);
   b += (size_t)keys * (4 * 4 + 1 + 8 * 6) + (size_t)keys * 8 * 4 * 2;
-  b += (size_t)tmap * (4 + 4 + 8) + 8;
+  b += (size_t)tmap * (4 + 4 + 8) + 8 + 4;
   b += (size_t)work * 8 * 4;
   b += (size_t)merged * 16 * 2;
   b += (size_t)inter * (KD_TILE * 16 + 8);
@@ -93,8 +93,8 @@ static size_t ws_bytes(long long n, long long keys, long long inter, long long w
 }
 
 int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, long long work,
-                  long long merged, long long tmap) {
-  KdWorkspace& w = s->ws;
+                  long long merged, long long tmap, KdWorkspace* wp) {
+  KdWorkspace& w = wp ? *wp : s->ws;
   if (w.err && n <= w.cap_n && keys <= w.cap_keys && inter <= w.cap_inter && work <= w.cap_work &&
       merged <= w.cap_merged && tmap <= w.cap_tmap)
     return KD_OK;
@@ -162,6 +162,7 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
   ok &= A((void**)&w.kfirst, sizeof(int) * tt);
   ok &= A((void**)&w.kstamp, sizeof(unsigned long long) * tt);
   ok &= A((void**)&w.kepoch, sizeof(unsigned long long));
+  ok &= A((void**)&w.chain, sizeof(int));
   if (ok) {  // no key carries a stamp; the first step's epoch is 1
     cudaMemset(w.kstamp, 0, sizeof(unsigned long long) * tt);
     cudaMemset(w.kepoch, 0, sizeof(unsigned long long));
@@ -298,6 +299,11 @@ void kd_store_drop_graphs(KdStore* st) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = KdGraphEntry();
   }
+  for (auto& row : st->pipe_graphs)
+    for (KdGraphEntry& g : row) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g = KdGraphEntry();
+    }
   st->last_eager = KdGraphKey();
 }
 
@@ -416,6 +422,12 @@ KD_API void kd_session_destroy(kd_session* h) {
   if (s->ws.d_in) cudaFree(s->ws.d_in);
   s->ws.d_in = nullptr;
   kd_ws_free(s->ws);
+  for (KdWorkspace& w : s->ws_more) kd_ws_free(w);
+  for (cudaEvent_t e : s->pipe_ev)
+    if (e) cudaEventDestroy(e);
+  if (s->ahead) cudaStreamDestroy(s->ahead);
+  if (s->h_many) cudaFreeHost(s->h_many);
+  if (s->h_many_scalars) cudaFreeHost(s->h_many_scalars);
   for (int i = 0; i <= KD_NSTAGES; ++i)
     if (s->stats.ev[i]) cudaEventDestroy(s->stats.ev[i]);
   cudaEventDestroy(s->join_ev);
@@ -576,6 +588,63 @@ KD_API int kd_store_ingest(kd_store* h, const uint32_t* keys, const double* valu
   if (st->carry && st->d.K == 1)  // the digest came from the single-sample path
     return kd_spath_carry_ingest(s, st, dv, n, mode, timestamp);
   return kd_pipeline_ingest(s, st, dk, dv, nullptr, n, mode, timestamp, nullptr, nullptr, nullptr);
+}
+
+KD_API int kd_store_ingest_many(kd_store* h, int64_t nbatch, const uint32_t* const* keys,
+                                const double* const* values, const int64_t* n, int clock_mode,
+                                const double* timestamps, int flags, int64_t* batches_done) {
+  if (batches_done) *batches_done = 0;
+  if (!h) return KD_EINVAL;
+  KdStore* st = &h->st;
+  KdSession* s = st->sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
+  if (nbatch < 0 || (nbatch > 0 && (!values || !n))) return fail(s, KD_EINVAL, "null batch arrays");
+  if (clock_mode != KD_CLOCK_COUNT && clock_mode != KD_CLOCK_TIME) return fail(s, KD_EINVAL, "unknown clock mode");
+  if (clock_mode == KD_CLOCK_TIME && nbatch > 0 && !timestamps) return fail(s, KD_EINVAL, "timestamps must be non-null");
+  for (int64_t i = 0; i < nbatch; ++i) {
+    if (n[i] < 0 || (n[i] > 0 && !values[i])) return fail(s, KD_EINVAL, "values must be non-null");
+    if (clock_mode == KD_CLOCK_TIME && !kd_isfinite(timestamps[i])) return fail(s, KD_EINVAL, "timestamp must be finite");
+  }
+  if (nbatch == 0) return KD_OK;
+  cudaSetDevice(s->device);
+  // Pointers the kernels can read: device memory, or pinned host memory read
+  // in place.  Pageable host memory, and a one-key digest carried from the
+  // single-sample path, take one call per batch instead.
+  bool each = st->carry && st->d.K == 1;
+  std::vector<const uint32_t*> dk((size_t)nbatch, nullptr);
+  std::vector<const double*> dv((size_t)nbatch, nullptr);
+  for (int64_t i = 0; i < nbatch && !each; ++i) {
+    if (n[i] == 0) continue;
+    const uint32_t* kp = keys ? keys[i] : nullptr;
+    if (flags & KD_PTR_DEVICE) {
+      dk[i] = kp;
+      dv[i] = values[i];
+      continue;
+    }
+    const void* mk = kp ? mapped_view(kp) : nullptr;
+    const void* mv = mapped_view(values[i]);
+    if (!mv || (kp && !mk)) each = true;
+    dk[i] = (const uint32_t*)mk;
+    dv[i] = (const double*)mv;
+  }
+  if (each) {
+    for (int64_t i = 0; i < nbatch; ++i) {
+      const int rc = kd_store_ingest(h, keys ? keys[i] : nullptr, values[i], n[i], clock_mode,
+                                     timestamps ? timestamps[i] : 0.0, flags);
+      if (rc) {
+        if (batches_done) *batches_done = i;
+        return rc;
+      }
+    }
+    if (batches_done) *batches_done = nbatch;
+    return KD_OK;
+  }
+  const int mode = clock_mode == KD_CLOCK_TIME ? KD_MODE_TIME : KD_MODE_COUNT;
+  long long done = 0;
+  const int rc = kd_pipeline_ingest_many(s, st, nbatch, dk.data(), dv.data(), (const long long*)n, mode,
+                                         clock_mode == KD_CLOCK_TIME ? timestamps : nullptr, &done);
+  if (batches_done) *batches_done = done;
+  return rc;
 }
 
 static int query_common(kd_store* h, const uint32_t* keys, const double* q, int64_t nq,

@@ -120,6 +120,7 @@ struct KdWorkspace {
   int* kfirst = nullptr;
   unsigned long long* kstamp = nullptr;
   unsigned long long* kepoch = nullptr;  // advanced by every step's k_prep
+  int* chain = nullptr;  // batch chain flag of a pipelined multi-batch ingest
   double* st_clock = nullptr;
   double* st_ls = nullptr;
   double* st_min = nullptr;
@@ -193,6 +194,17 @@ struct KdSession {
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   char last_error[256] = {0};  // fixed buffer: reporting an error never allocates
   KdWorkspace ws;
+  // Pipelined multi-batch ingest: two more workspaces, so that batches sort
+  // (on `ahead`, up to two ahead) while an earlier one compresses (on
+  // `stream`); events ordering the two; pinned host slots for every batch's
+  // status.
+#define KD_PIPE_WS 3
+  KdWorkspace ws_more[KD_PIPE_WS - 1];
+  cudaStream_t ahead = nullptr;
+  cudaEvent_t pipe_ev[1 + 3 * KD_PIPE_WS] = {};  // start; per workspace: front done, free, call block copied
+  KdErrHost* h_many = nullptr;
+  int* h_many_scalars = nullptr;
+  long long cap_many = 0;
   KdStageStats stats;
   struct KdStore* scratch_store = nullptr;  // 1-key store for stateless compress
   std::vector<struct KdStore*> stores;         // live stores of this session
@@ -244,6 +256,10 @@ struct KdStore {
   KdGraphEntry graphs[KD_GRAPH_CACHE];
   int graph_next = 0;
   KdGraphKey last_eager;
+  // The pipelined multi-batch ingest's graphs: per workspace, its front and
+  // its back (with the chain flag the back's commit was captured with).
+  KdGraphEntry pipe_graphs[KD_PIPE_WS][2];
+  const int* pipe_chain[KD_PIPE_WS] = {};
   // Single-sample path state (one-key stores).  `pending`: samples wait in the
   // buffer.  `carry`: the next batch must carry the centroids and buffer in
   // its input (their order is the sequential pass's, not the batch path's).
@@ -285,7 +301,14 @@ int kd_pipeline_merge(KdSession* s, KdStore* dst, KdStore* src, const long long*
 int kd_store_alloc(KdSession* s, KdStore* st);
 void kd_store_free(KdStore* st);
 int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, long long work,
-                  long long merged, long long tmap);
+                  long long merged, long long tmap, KdWorkspace* wp = nullptr);
+// Batches folded in order as if by one kd_pipeline_ingest each (unit weights),
+// with the front of batch i + 1 (prep, sort) overlapping the back of batch i.
+// On failure *done is the failing batch: batches before it are committed, it
+// and every later one are not.
+int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint32_t* const* d_keys,
+                            const double* const* d_vals, const long long* ns, int mode,
+                            const double* timestamps, long long* done);
 void kd_ws_free(KdWorkspace& ws);
 void kd_store_drop_graphs(KdStore* st);
 int kd_cuda_fail(KdSession* s, cudaError_t e, const char* what);

@@ -1551,6 +1551,9 @@ struct CommitArgs {
   const double* st_max;
   const int* remaining;  // active keys left after the last level
   KdErrHost* err;
+  // Batch chain of a pipelined multi-batch ingest (null otherwise): set by the
+  // first batch that fails; no later batch of the chain commits.
+  int* chain;
 };
 
 // _gpu_batch_finish (tdigest.mojo:298-315) + _prune (:441-458) per key, the
@@ -1614,9 +1617,12 @@ __device__ int commit_serial(const KdStoreDev& s, uint32_t key, int b, int cnt, 
 __global__ void __launch_bounds__(128) k_commit(CommitArgs a) {
   const int U = a.totals[0].x;
   const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j == 0 && *a.remaining > 0) kd_err_set(a.err, KD_EMORE_LEVELS, *a.remaining);
+  if (j == 0) {
+    if (*a.remaining > 0) kd_err_set(a.err, KD_EMORE_LEVELS, *a.remaining);
+    if (a.chain && (kd_err_get(a.err) || *a.remaining > 0)) *a.chain = 1;
+  }
   if (j >= U) return;
-  if (kd_err_get(a.err) || *a.remaining > 0) return;
+  if (kd_err_get(a.err) || *a.remaining > 0 || (a.chain && *a.chain)) return;
   const uint32_t key = a.tkey[j];
   const int b = a.tbuf[j];
   double total = 0.0;
@@ -1635,9 +1641,12 @@ __global__ void __launch_bounds__(256) k_commit_warp(CommitArgs a) {
   const int lane = threadIdx.x & 31;
   const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  if (warp0 == 0 && lane == 0 && *a.remaining > 0) kd_err_set(a.err, KD_EMORE_LEVELS, *a.remaining);
+  if (warp0 == 0 && lane == 0) {
+    if (*a.remaining > 0) kd_err_set(a.err, KD_EMORE_LEVELS, *a.remaining);
+    if (a.chain && (kd_err_get(a.err) || *a.remaining > 0)) *a.chain = 1;
+  }
   int stop = 0;
-  if (lane == 0) stop = (kd_err_get(a.err) || *a.remaining > 0) ? 1 : 0;
+  if (lane == 0) stop = (kd_err_get(a.err) || *a.remaining > 0 || (a.chain && *a.chain)) ? 1 : 0;
   if (__shfl_sync(0xffffffffu, stop, 0)) return;  // warp-uniform
   const KdStoreDev& s = a.s;
   for (long long j = warp0; j < U; j += nwarps) {
@@ -2011,13 +2020,23 @@ static void enqueue_levels(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, i
   }
 }
 
+// Where a step's commit reports: the batch chain of a pipelined multi-batch
+// ingest and the host slots its status and scratch needs are read back into
+// (null: no chain, the workspace's own slots).
+struct KdTailOut {
+  int* chain = nullptr;
+  KdErrHost* h_err = nullptr;
+  int* h_scalars = nullptr;
+  bool no_readback = false;  // the caller copies the status back itself
+};
+
 // Commit (prune, prefix, slot flip) and the status readback.
 static void enqueue_tail(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, long long keys_max,
-                         KdStepView& v) {
+                         KdStepView& v, const KdTailOut* out = nullptr) {
   cudaStream_t str = s->stream;
   stage_mark(s, 5);
   CommitArgs ca{sd, w.totals, w.tkey, w.tbuf, w.st_count, w.st_clock, w.st_ls, w.st_min,
-                w.st_max, v.curA, w.err};
+                w.st_max, v.curA, w.err, out ? out->chain : nullptr};
   if (sd.lambda > 0.0)
     k_commit<<<(int)((keys_max + 127) / 128), 128, 0, str>>>(ca);
   else
@@ -2026,57 +2045,74 @@ static void enqueue_tail(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, lon
   v.launches += 1;
   stage_mark(s, 6);
   v.note(cudaGetLastError());
-  v.note(cudaMemcpyAsync(w.h_err, w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, str));
-  v.note(cudaMemcpyAsync(w.h_scalars, w.needs, sizeof(int) * 4, cudaMemcpyDeviceToHost, str));
+  if (out && out->no_readback) return;
+  v.note(cudaMemcpyAsync(out && out->h_err ? out->h_err : w.h_err, w.err, sizeof(KdErrHost),
+                         cudaMemcpyDeviceToHost, str));
+  v.note(cudaMemcpyAsync(out && out->h_scalars ? out->h_scalars : w.h_scalars, w.needs,
+                         sizeof(int) * 4, cudaMemcpyDeviceToHost, str));
 }
 
 // One whole ingest step as device work only (so it can be captured): the
 // per-call block, prep, sort, planning, level 0, `levels` hierarchy levels,
-// commit and readback.
+// commit and readback.  `part` selects the front (bit 0: per-call block, prep,
+// sort, unpack and repair, which read only the batch) and the back (bit 1:
+// everything from the touched-key scan on, which reads and writes the store),
+// so that a pipelined multi-batch ingest can sort one batch while the previous
+// one compresses.  The back finds the sorted batch where the front left it.
+#define KD_PART_FRONT 1
+#define KD_PART_BACK 2
 static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long long n, int mode,
-                               bool with_idx, int levels, int id_last, bool full_sort) {
+                               bool with_idx, int levels, int id_last, bool full_sort,
+                               int part = KD_PART_FRONT | KD_PART_BACK,
+                               const KdTailOut* out = nullptr) {
   cudaStream_t str = s->stream;
   const KdStoreDev sd = st->d;
   const long long keys_max = std::min<long long>(n, sd.K);
   const int key_bits = key_bits_for(sd.K);
   KdStepView v;
-  v.note(cudaMemcpyAsync(w.d_call, w.h_call, sizeof(KdCallArgs), cudaMemcpyHostToDevice, str));
-  v.note(cudaMemsetAsync(w.totals, 0, sizeof(int4) * 8, str));
-  v.note(cudaMemsetAsync(w.needs, 0, sizeof(int) * 4, str));
-  v.note(cudaMemsetAsync(w.fix, 0, sizeof(int), str));  // repair-list count
-  stage_mark(s, 0);
-  {
-    int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
-    k_prep<<<grid, 256, 0, str>>>(n, w.d_call, sd.K, full_sort ? 0 : key_bits, w.k64[0], w.key[0],
-                                  with_idx ? w.idx[0] : nullptr, w.err, w.kepoch);
-    v.launches += 1;
-  }
-  stage_mark(s, 1);
-  KdSortBufs sb = sort_bufs(w);
   // Packed form: the sort covers the key bits and at least KD_PACK_VALUE_BITS
   // value bits; lower digits are left to the repair (runs of near-equal values).
   const int first_digit = full_sort ? 0 : std::max(0, (64 - key_bits - KD_PACK_VALUE_BITS) / 8);
   const int sort_bits = full_sort ? key_bits : 0;  // packed keys need no key passes
-  int r = kd_radix_sort(sb, n, sort_bits, with_idx, s->num_sms, str, first_digit);
-  v.launches += kd_radix_sort_launches(n, sort_bits, first_digit);
   // Touched keys from the key-level stamps when the batch has at least as
   // many samples as the store has keys (a scan over K instead of over n).
   const bool key_level = !full_sort && w.kstamp && sd.K <= n && sd.K <= w.cap_tmap;
-  if (!full_sort) {  // also for n == 1: the key is still packed
-    const int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
-    const int shift = 8 * first_digit;
-    k_unpack<<<grid, 256, 0, str>>>(n, key_bits, shift, w.k64[r], w.key[r],
-                                    with_idx ? w.idx[r] : nullptr, w.k64[r ^ 1], w.key[r ^ 1],
-                                    with_idx ? w.idx[r ^ 1] : nullptr, w.fix, (int)w.cap_fix, w.err,
-                                    sd.K, key_level ? w.kfirst : nullptr,
-                                    key_level ? w.kstamp : nullptr, w.kepoch);
-    k_repair<<<s->num_sms, 256, 0, str>>>(n, key_bits, shift, w.k64[r], w.key[r], w.k64[r ^ 1],
-                                          with_idx ? w.idx[r ^ 1] : nullptr, w.fix, (int)w.cap_fix,
-                                          w.err);
-    v.launches += 2;
-    r ^= 1;
+  int r = kd_radix_sort_result(n, sort_bits, first_digit) ^ (full_sort ? 0 : 1);
+  if (part & KD_PART_FRONT) {
+    v.note(cudaMemcpyAsync(w.d_call, w.h_call, sizeof(KdCallArgs), cudaMemcpyHostToDevice, str));
+    v.note(cudaMemsetAsync(w.totals, 0, sizeof(int4) * 8, str));
+    v.note(cudaMemsetAsync(w.needs, 0, sizeof(int) * 4, str));
+    v.note(cudaMemsetAsync(w.fix, 0, sizeof(int), str));  // repair-list count
+    stage_mark(s, 0);
+    {
+      int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
+      k_prep<<<grid, 256, 0, str>>>(n, w.d_call, sd.K, full_sort ? 0 : key_bits, w.k64[0], w.key[0],
+                                    with_idx ? w.idx[0] : nullptr, w.err, w.kepoch);
+      v.launches += 1;
+    }
+    stage_mark(s, 1);
+    KdSortBufs sb = sort_bufs(w);
+    int rs = kd_radix_sort(sb, n, sort_bits, with_idx, s->num_sms, str, first_digit);
+    v.launches += kd_radix_sort_launches(n, sort_bits, first_digit);
+    if (!full_sort) {  // also for n == 1: the key is still packed
+      const int r0 = rs;
+      const int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
+      const int shift = 8 * first_digit;
+      k_unpack<<<grid, 256, 0, str>>>(n, key_bits, shift, w.k64[r0], w.key[r0],
+                                      with_idx ? w.idx[r0] : nullptr, w.k64[r0 ^ 1], w.key[r0 ^ 1],
+                                      with_idx ? w.idx[r0 ^ 1] : nullptr, w.fix, (int)w.cap_fix, w.err,
+                                      sd.K, key_level ? w.kfirst : nullptr,
+                                      key_level ? w.kstamp : nullptr, w.kepoch);
+      k_repair<<<s->num_sms, 256, 0, str>>>(n, key_bits, shift, w.k64[r0], w.key[r0], w.k64[r0 ^ 1],
+                                            with_idx ? w.idx[r0 ^ 1] : nullptr, w.fix, (int)w.cap_fix,
+                                            w.err);
+      v.launches += 2;
+      rs ^= 1;
+    }
+    if (rs != r) v.note(cudaErrorInvalidValue);  // the back would read the wrong buffers
+    stage_mark(s, 2);
   }
-  stage_mark(s, 2);
+  if (!(part & KD_PART_BACK)) return v;
   const uint64_t* k64 = w.k64[r];
   const uint32_t* skey = w.key[r];
   const uint32_t* sidx = with_idx ? w.idx[r] : nullptr;
@@ -2124,8 +2160,26 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   v.curA = a1;
   v.Iprev = l0.I;
   enqueue_levels(s, w, sd, 0, levels, id_last, v);
-  enqueue_tail(s, w, sd, keys_max, v);
+  enqueue_tail(s, w, sd, keys_max, v, out);
   return v;
+}
+
+// What a captured step depends on besides the per-call block.
+static KdGraphKey step_key(const KdSession* s, const KdStoreDev& sd, const KdWorkspace& w,
+                           long long n, bool with_idx, int mode, int L) {
+  KdGraphKey key;
+  key.n = n;
+  key.key_bits = key_bits_for(sd.K);
+  key.with_idx = with_idx;
+  key.mode = mode;
+  key.levels = L;
+  key.force_exact = s->force_exact;
+  key.timing = s->stats.enabled;
+  key.scale = sd.scale;
+  key.compression = sd.compression;
+  key.generation = w.generation;
+  key.tuning = s->small_cap | (s->large_bps << 8) | (s->small_bps << 16) | (s->concurrent_tiles << 24);
+  return key;
 }
 
 int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_t* d_keys,
@@ -2159,18 +2213,7 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
   kd_rs_epoch_reserve(sb, str);
   int L = std::max(1, std::min(st->levels_hint, s->max_levels));
 
-  KdGraphKey key;
-  key.n = n;
-  key.key_bits = key_bits_for(sd.K);
-  key.with_idx = with_idx;
-  key.mode = mode;
-  key.levels = L;
-  key.force_exact = s->force_exact;
-  key.timing = s->stats.enabled;
-  key.scale = sd.scale;
-  key.compression = sd.compression;
-  key.generation = w.generation;
-  key.tuning = s->small_cap | (s->large_bps << 8) | (s->small_bps << 16) | (s->concurrent_tiles << 24);
+  const KdGraphKey key = step_key(s, sd, w, n, with_idx, mode, L);
   KdStepView v;
   bool ran = false;
   if (s->use_graphs && w.generation != 0) {
@@ -2293,6 +2336,198 @@ int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const 
   }
   kd_set_msg(s, "ingest scratch could not be sized");
   return KD_ENOMEM;
+}
+
+// Pipelined multi-batch ingest.  Batch i uses workspace i mod 3.  Its front
+// (per-call block, prep, sort, unpack, repair: reads only the batch) runs on the
+// `ahead` stream once the back of batch i - 3 has released that workspace; its
+// back (touched keys, prepare, levels, commit: reads and writes the store) runs
+// on the session stream after the back of batch i - 1 and its own front.  So
+// the sort of one batch overlaps the compress of the previous one, and the
+// store sees the batches in order, exactly as from one call each.  The commit
+// of a batch that fails (or must be retried) sets the chain flag, and no later
+// batch commits; the host then retries from that batch one call at a time
+// (full sort, more levels, larger scratch) or reports its error.
+static int pipe_fail(KdSession* s, cudaError_t e) { return kd_cuda_fail(s, e, "pipelined ingest"); }
+
+int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint32_t* const* d_keys,
+                            const double* const* d_vals, const long long* ns, int mode,
+                            const double* timestamps, long long* done) {
+  *done = 0;
+  if (nb <= 0) return KD_OK;
+  long long nmax = 0;
+  for (long long i = 0; i < nb; ++i) {
+    if (ns[i] > (1LL << 31) - 1) {
+      kd_set_msg(s, "batch too large (limit 2^31 - 1 samples per call)");
+      *done = i;
+      return KD_ERANGE;
+    }
+    nmax = std::max(nmax, ns[i]);
+  }
+  if (nmax == 0) {
+    *done = nb;
+    return KD_OK;
+  }
+  int rc = kd_pipeline_prepare_device(s);
+  if (rc) return rc;
+  const KdStoreDev sd = st->d;
+  const long long keys_max = std::min<long long>(nmax, sd.K);
+  if (!s->ahead) {
+    if (cudaStreamCreateWithFlags(&s->ahead, cudaStreamNonBlocking) != cudaSuccess) return pipe_fail(s, cudaGetLastError());
+    for (cudaEvent_t& e : s->pipe_ev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return pipe_fail(s, cudaGetLastError());
+  }
+  if (s->cap_many < nb) {
+    if (s->h_many) cudaFreeHost(s->h_many);
+    if (s->h_many_scalars) cudaFreeHost(s->h_many_scalars);
+    s->h_many = nullptr;
+    s->h_many_scalars = nullptr;
+    s->cap_many = 0;
+    const long long cap = std::max<long long>(nb, 64);
+    if (cudaHostAlloc((void**)&s->h_many, sizeof(KdErrHost) * cap, cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc((void**)&s->h_many_scalars, sizeof(int) * 4 * cap, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      kd_set_msg(s, "pinned status slots for a multi-batch ingest could not be allocated");
+      return KD_ENOMEM;
+    }
+    s->cap_many = cap;
+  }
+  const int id_last = sd.scale <= KD_SCALE_K1
+                          ? (int)kd_bucket(sd.scale, 1.0, 1.0, kd_normalizer(sd.scale, sd.compression, 1.0))
+                          : 0;
+  cudaStream_t M = s->stream, A = s->ahead;
+  cudaEvent_t ev_start = s->pipe_ev[0];
+  cudaEvent_t* ev_front = &s->pipe_ev[1];
+  cudaEvent_t* ev_free = &s->pipe_ev[1 + KD_PIPE_WS];
+  cudaEvent_t* ev_copied = &s->pipe_ev[1 + 2 * KD_PIPE_WS];
+  KdWorkspace* ws[KD_PIPE_WS];
+  ws[0] = &s->ws;
+  for (int q = 1; q < KD_PIPE_WS; ++q) ws[q] = &s->ws_more[q - 1];
+  long long base = 0;  // batches before it are committed
+  while (base < nb) {
+    // Every workspace sized as the one-call path sizes its own for the
+    // largest batch, and at least as large as any already is (a retry on the
+    // one-call path may have grown the first).
+    long long ci = std::max(64LL, 2 * (nmax / KD_TILE) + 64);
+    long long cw = 2 * keys_max + nmax / KD_TILE + 64;
+    long long cm = 2 * nmax + 64 * keys_max + 1024;
+    for (KdWorkspace* wp : ws) {
+      ci = std::max(ci, wp->cap_inter);
+      cw = std::max(cw, wp->cap_work);
+      cm = std::max(cm, wp->cap_merged);
+    }
+    for (KdWorkspace* wp : ws) {
+      rc = kd_ws_reserve(s, nmax, keys_max, ci, cw, cm, sd.K, wp);
+      if (rc) {
+        *done = base;
+        return rc;
+      }
+    }
+    int* chain = s->ws.chain;
+    const int L = std::max(1, std::min(st->levels_hint, s->max_levels));
+    // One part of a batch's step on stream `str`: replayed from the store's
+    // graph for this workspace and part when its shape was captured, else
+    // captured now (eager if capture fails).
+    auto run_part = [&](int part, int q, KdWorkspace& w, long long n, cudaStream_t str,
+                        const KdTailOut* out, KdStepView& v) {
+      const KdGraphKey key = step_key(s, sd, w, n, false, mode, L);
+      KdGraphEntry& g = st->pipe_graphs[q][part == KD_PART_FRONT ? 0 : 1];
+      const bool chain_ok = part == KD_PART_FRONT || st->pipe_chain[q] == chain;
+      s->stream = str;
+      if (!(g.exec && g.key == key && chain_ok) && s->use_graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = KdGraphEntry();
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(str, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+          const KdStepView cv = enqueue_step(s, st, w, n, mode, false, L, id_last, false, part, out);
+          const bool ended = cudaStreamEndCapture(str, &graph) == cudaSuccess;
+          cudaGraphExec_t ex = nullptr;
+          if (ended && graph && cv.err == cudaSuccess &&
+              cudaGraphInstantiate(&ex, graph, 0) == cudaSuccess) {
+            g.key = key;
+            g.exec = ex;
+            g.launches = cv.launches;
+            if (part != KD_PART_FRONT) st->pipe_chain[q] = chain;
+          }
+          if (graph) cudaGraphDestroy(graph);
+        }
+        cudaGetLastError();  // a capture that failed runs eagerly below
+      }
+      if (g.exec && g.key == key) {
+        v.note(cudaGraphLaunch(g.exec, str));
+        v.launches += g.launches;
+      } else {
+        const KdStepView e = enqueue_step(s, st, w, n, mode, false, L, id_last, false, part, out);
+        v.note(e.err);
+        v.launches += e.launches;
+      }
+      s->stream = M;
+    };
+    const int stats_on = s->stats.enabled;
+    s->stats.enabled = 0;  // stage events belong to one stream
+    KdStepView v;
+    v.note(cudaMemsetAsync(chain, 0, sizeof(int), M));
+    v.note(cudaEventRecord(ev_start, M));  // the ahead stream starts after all earlier work
+    v.note(cudaStreamWaitEvent(A, ev_start, 0));
+    for (long long i = base; i < nb; ++i) {
+      s->h_many[i] = KdErrHost{0, 0, 0};
+      if (ns[i] == 0) continue;  // an empty batch changes nothing
+      const int k = (int)(i % KD_PIPE_WS);
+      KdWorkspace& w = *ws[k];
+      if (i >= base + KD_PIPE_WS) v.note(cudaEventSynchronize(ev_copied[k]));  // its last user read this block
+      KdCallArgs& c = *w.h_call;
+      c = KdCallArgs();
+      c.keys = d_keys ? d_keys[i] : nullptr;
+      c.vals = d_vals[i];
+      c.timestamp = timestamps ? timestamps[i] : 0.0;
+      c.err = KdErrHost{0, 0, 0x7fffffffffffffffLL};
+      if (i >= base + KD_PIPE_WS) v.note(cudaStreamWaitEvent(A, ev_free[k], 0));
+      KdSortBufs sb = sort_bufs(w);
+      kd_rs_epoch_reserve(sb, A);
+      run_part(KD_PART_FRONT, k, w, ns[i], A, nullptr, v);
+      v.note(cudaEventRecord(ev_copied[k], A));
+      v.note(cudaEventRecord(ev_front[k], A));
+      v.note(cudaStreamWaitEvent(M, ev_front[k], 0));
+      KdTailOut out{chain, nullptr, nullptr, true};
+      run_part(KD_PART_BACK, k, w, ns[i], M, &out, v);
+      v.note(cudaMemcpyAsync(&s->h_many[i], w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, M));
+      v.note(cudaEventRecord(ev_free[k], M));
+    }
+    s->stats.enabled = stats_on;
+    v.note(cudaStreamSynchronize(M));
+    if (v.err != cudaSuccess) {
+      *done = base;
+      return pipe_fail(s, v.err);
+    }
+    s->stats.launches += v.launches;
+    long long bad = nb;
+    for (long long i = base; i < nb && bad == nb; ++i)
+      if (s->h_many[i].code != 0) bad = i;
+    s->stats.ingests += bad - base;
+    if (bad == nb) break;
+    const KdErrHost e = s->h_many[bad];
+    if (e.code == KD_ERESORT || e.code == KD_EMORE_LEVELS || e.code == KD_ERANGE_SCRATCH) {
+      // Nothing from this batch on was committed: run it alone (the one-call
+      // path owns these retries: full sort, more levels, larger scratch), then
+      // pipeline the rest.
+      const int r = kd_pipeline_ingest(s, st, d_keys ? d_keys[bad] : nullptr, d_vals[bad], nullptr,
+                                       ns[bad], mode, timestamps ? timestamps[bad] : 0.0, nullptr,
+                                       nullptr, nullptr);
+      if (r) {
+        *done = bad;
+        return r;
+      }
+      base = bad + 1;
+      continue;
+    }
+    char buf[256];
+    snprintf(buf, sizeof buf, "%s (batch %lld, at index %lld)", err_text(e.code), bad, e.index);
+    kd_set_msg(s, buf);
+    *done = bad;
+    return e.code;
+  }
+  *done = nb;
+  return KD_OK;
 }
 
 int kd_pipeline_quantile(KdSession* s, KdStore* st, const uint32_t* d_keys, const double* d_q,

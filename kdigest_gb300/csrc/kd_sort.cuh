@@ -295,6 +295,12 @@ static inline int kd_radix_sort(KdSortBufs& b, long long n, int key_bits, bool w
   return src;
 }
 
+// The buffer set kd_radix_sort leaves its result in (0/1), without sorting.
+static inline int kd_radix_sort_result(long long n, int key_bits, int first_digit = 0) {
+  if (n <= 1) return 0;
+  return ((8 - first_digit) + (key_bits + 7) / 8) & 1;
+}
+
 static inline int kd_radix_sort_launches(long long n, int key_bits, int first_digit = 0) {
   return n > 1 ? 1 + (8 - first_digit) + (key_bits + 7) / 8 : 0;
 }

@@ -196,6 +196,21 @@ class _Store:
             raise IndexError("key out of range [0, num_keys)")
         self._chk(rc)
 
+    def ingest_many(self, keys: list, values: list, device: bool):
+        """kd_store_ingest_many over arrays that stay alive for the call:
+        numpy arrays (host) or CUDA tensors (device, read in place)."""
+        nb = len(values)
+        if nb == 0:
+            return
+        addr = (lambda a: a.data_ptr()) if device else (lambda a: a.ctypes.data)
+        kp = (ctypes.c_void_p * nb)(*[addr(k) if k is not None else None for k in keys])
+        vp = (ctypes.c_void_p * nb)(*[addr(v) for v in values])
+        ns = (ctypes.c_int64 * nb)(*[len(v) for v in values])
+        done = ctypes.c_int64(0)
+        rc = N.load().kd_store_ingest_many(self._h, nb, kp, vp, ns, N.KD_CLOCK_COUNT, None,
+                                           N.KD_PTR_DEVICE if device else 0, ctypes.byref(done))
+        self._chk(rc)
+
     def query(self, keys, xs, is_cdf: bool):
         x = np.ascontiguousarray(xs, dtype=np.float64)
         k = None if keys is None else np.ascontiguousarray(keys, dtype=np.uint32)
@@ -504,6 +519,46 @@ class GroupedTDigest:
         k = self._check_keys(k)
         v = _validate_values(v)
         self._store.ingest(k, v, N.KD_CLOCK_TIME, float(timestamp))
+
+    def add_batches(self, batches):
+        """A sequence of add_batch calls in one: the results are those of the
+        calls one by one, in order, while the sort of each batch overlaps the
+        compress of the one before.  `batches` holds (keys, values) pairs,
+        either numpy arrays (checked on the host) or CUDA tensors (uint32 or
+        int32 keys, float64 values; read in place, checked on the device).  A
+        failing batch raises; the batches before it stay applied."""
+        batches = list(batches)
+        if not batches:
+            return
+        dev = [getattr(v, "is_cuda", False) for _, v in batches]
+        if any(dev):
+            if not all(dev) or not all(getattr(k, "is_cuda", False) for k, _ in batches):
+                raise ValueError("batches must be all host arrays or all CUDA tensors")
+            ks, vs = [], []
+            for k, v in batches:
+                if len(k) != len(v):
+                    raise ValueError("keys and values must have equal length")
+                if str(v.dtype) != "torch.float64" or str(k.dtype) not in ("torch.int32", "torch.uint32"):
+                    raise TypeError("CUDA batches need int32/uint32 keys and float64 values")
+                ks.append(k.contiguous())
+                vs.append(v.contiguous())
+            self._store.ingest_many(ks, vs, device=True)
+            return
+        ks, vs, err = [], [], None
+        for k, v in batches:  # host checks, in batch order: apply what precedes a bad batch
+            try:
+                k = np.asarray(k)
+                v = np.asarray(v)
+                if len(k) != len(v):
+                    raise ValueError("keys and values must have equal length")
+                ks.append(self._check_keys(k))
+                vs.append(_validate_values(v))
+            except (ValueError, IndexError) as e:
+                err = e
+                break
+        self._store.ingest_many(ks, vs, device=False)
+        if err is not None:
+            raise err
 
     def _key(self, key: int) -> int:
         if key < 0 or key >= self.num_keys:
