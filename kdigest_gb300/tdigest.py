@@ -357,6 +357,36 @@ class TDigest:
             return
         self._store.ingest(None, v, N.KD_CLOCK_COUNT, 0.0)
 
+    def add_batches(self, batches):
+        """A sequence of add_batch_p calls in one (the batch path for every
+        batch, as add_batch takes from the crossover up): the results are those
+        of the calls one by one, in order, while the sort of each batch overlaps
+        the compress of the one before.  `batches` holds numpy arrays (checked
+        on the host) or CUDA float64 tensors (read in place, checked on the
+        device).  A failing batch raises; the batches before it stay applied."""
+        self._sync()
+        batches = list(batches)
+        if not batches:
+            return
+        if any(getattr(v, "is_cuda", False) for v in batches):
+            if not all(getattr(v, "is_cuda", False) for v in batches):
+                raise ValueError("batches must be all host arrays or all CUDA tensors")
+            if any(str(v.dtype) != "torch.float64" for v in batches):
+                raise TypeError("CUDA batches need float64 values")
+            vs = [v.contiguous() for v in batches]
+            self._store.ingest_many([None] * len(vs), vs, device=True)
+            return
+        vs, err = [], None
+        for v in batches:
+            try:
+                vs.append(_validate_values(v))
+            except ValueError as e:
+                err = e
+                break
+        self._store.ingest_many([None] * len(vs), vs, device=False)
+        if err is not None:
+            raise err
+
     def add_batch_at(self, values, timestamp: float):
         """Batch form of add_at on the batch path: the clock moves to
         `timestamp` once when later, then every sample is inserted."""

@@ -161,3 +161,27 @@ def test_time_clock_through_the_c_abi(kd):
     for (k, v), t in zip(batches, ts):
         b.add_batch_at(k, v, t)
     _same(a, b, nk)
+
+
+def test_single_digest_batches(kd):
+    """TDigest.add_batches equals add_batch_p per batch, with decay, and after
+    single-sample adds (the buffer is carried into the first batch)."""
+    import torch
+
+    rng = np.random.default_rng(41)
+    vals = [rng.lognormal(0.0, 1.5, n) for n in (70000, 65536, 100000, 80000)]
+    for pre in (0, 300):
+        a = kd.TDigest(200.0, kd.K2, decay=kd.Decay.half_life(1e5), session=kd.GpuSession())
+        b = kd.TDigest(200.0, kd.K2, decay=kd.Decay.half_life(1e5), session=kd.GpuSession())
+        if pre:
+            head = rng.standard_normal(pre)
+            a.add_batch(head)
+            b.add_batch(head)
+        a.add_batches([torch.from_numpy(v).cuda() for v in vals])
+        for v in vals:
+            b.add_batch_p(v)
+        ma, wa = a.centroids()
+        mb, wb = b.centroids()
+        assert np.array_equal(ma, mb) and np.array_equal(wa, wb), f"pre={pre}"
+        assert a.state() == b.state()
+        assert a.to_bytes() == b.to_bytes()
