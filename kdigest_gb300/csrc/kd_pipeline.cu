@@ -2416,12 +2416,30 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
       cw = std::max(cw, wp->cap_work);
       cm = std::max(cm, wp->cap_merged);
     }
+    bool room = true;
     for (KdWorkspace* wp : ws) {
       rc = kd_ws_reserve(s, nmax, keys_max, ci, cw, cm, sd.K, wp);
+      if (rc == KD_ENOMEM && wp != &s->ws) {
+        room = false;  // no memory for the extra workspaces: one call per batch
+        break;
+      }
       if (rc) {
         *done = base;
         return rc;
       }
+    }
+    if (!room) {
+      for (long long t = base; t < nb; ++t) {
+        const int r = kd_pipeline_ingest(s, st, d_keys ? d_keys[t] : nullptr, d_vals[t], nullptr,
+                                         ns[t], mode, timestamps ? timestamps[t] : 0.0, nullptr,
+                                         nullptr, nullptr);
+        if (r) {
+          *done = t;
+          return r;
+        }
+      }
+      *done = nb;
+      return KD_OK;
     }
     int* chain = s->ws.chain;
     const int L = std::max(1, std::min(st->levels_hint, s->max_levels));

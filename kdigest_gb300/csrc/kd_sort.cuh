@@ -49,7 +49,7 @@ __device__ __forceinline__ unsigned long long lb_pack(unsigned epoch, unsigned l
 
 static __global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_hist_all(
     const uint64_t* __restrict__ k64, const uint32_t* __restrict__ key, long long n,
-    int key_passes, unsigned* __restrict__ ghist, unsigned* __restrict__ epoch_base) {
+    int key_passes, int first_digit, unsigned* __restrict__ ghist, unsigned* __restrict__ epoch_base) {
   __shared__ unsigned h[KD_RS_MAXPASS][256];
   if (blockIdx.x == 0 && threadIdx.x == 0) *epoch_base += KD_RS_EPOCH_STRIDE;
   for (int t = threadIdx.x; t < KD_RS_MAXPASS * 256; t += KD_RS_THREADS) (&h[0][0])[t] = 0;
@@ -57,8 +57,7 @@ static __global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_hist_all(
   for (long long i = (long long)blockIdx.x * KD_RS_THREADS + threadIdx.x; i < n;
        i += (long long)gridDim.x * KD_RS_THREADS) {
     const uint64_t v = k64[i];
-#pragma unroll
-    for (int p = 0; p < 8; ++p) atomicAdd(&h[p][(unsigned)(v >> (8 * p)) & 255u], 1u);
+    for (int p = first_digit; p < 8; ++p) atomicAdd(&h[p][(unsigned)(v >> (8 * p)) & 255u], 1u);
     const uint32_t kk = key[i];
     for (int p = 0; p < key_passes; ++p) atomicAdd(&h[8 + p][(kk >> (8 * p)) & 255u], 1u);
   }
@@ -276,8 +275,8 @@ static inline int kd_radix_sort(KdSortBufs& b, long long n, int key_bits, bool w
   cudaMemsetAsync(b.ghist, 0, sizeof(unsigned) * KD_RS_MAXPASS * 256, st);
   cudaMemsetAsync(b.ticket, 0, sizeof(unsigned long long), st);
   unsigned long long ticket_base = 0;
-  kd_rs_hist_all<<<num_sms * 8, KD_RS_THREADS, 0, st>>>(b.k64[0], b.key[0], n, key_passes, b.ghist,
-                                                        b.epoch_base);
+  kd_rs_hist_all<<<num_sms * 8, KD_RS_THREADS, 0, st>>>(b.k64[0], b.key[0], n, key_passes,
+                                                        first_digit, b.ghist, b.epoch_base);
   auto pass = [&](int shift, int from_key, int pidx) {
     const int dst = src ^ 1;
     KdRsPass a{b.k64[src], b.key[src], b.idx[src], b.k64[dst], b.key[dst], b.idx[dst], n, shift,
