@@ -113,9 +113,10 @@ KD_API int kd_store_ingest(kd_store* st, const uint32_t* keys, const double* val
  * compress of the one before.  Stops at the first failing batch: the batches
  * before it stay committed, it and every later one change nothing, and
  * *batches_done (may be NULL) receives its position (nbatch on success).
- * Device pointers (KD_PTR_DEVICE) or pinned host memory are read in place;
- * pageable host memory runs one kd_store_ingest per batch.  No reference
- * counterpart beyond the add_batch loop it replaces. */
+ * Device pointers (KD_PTR_DEVICE) are read in place; host memory (pinned or
+ * pageable) is copied batch by batch into device staging buffers by the copy
+ * engine while earlier batches compute.  No reference counterpart beyond the
+ * add_batch loop it replaces. */
 KD_API int kd_store_ingest_many(kd_store* st, int64_t nbatch, const uint32_t* const* keys,
                                 const double* const* values, const int64_t* n, int clock_mode,
                                 const double* timestamps, int flags, int64_t* batches_done);

@@ -426,6 +426,9 @@ KD_API void kd_session_destroy(kd_session* h) {
   for (cudaEvent_t e : s->pipe_ev)
     if (e) cudaEventDestroy(e);
   if (s->ahead) cudaStreamDestroy(s->ahead);
+  if (s->copy) cudaStreamDestroy(s->copy);
+  for (void* p : s->d_stage)
+    if (p) cudaFree(p);
   if (s->h_many) cudaFreeHost(s->h_many);
   if (s->h_many_scalars) cudaFreeHost(s->h_many_scalars);
   for (int i = 0; i <= KD_NSTAGES; ++i)
@@ -607,25 +610,15 @@ KD_API int kd_store_ingest_many(kd_store* h, int64_t nbatch, const uint32_t* con
   }
   if (nbatch == 0) return KD_OK;
   cudaSetDevice(s->device);
-  // Pointers the kernels can read: device memory, or pinned host memory read
-  // in place.  Pageable host memory, and a one-key digest carried from the
-  // single-sample path, take one call per batch instead.
-  bool each = st->carry && st->d.K == 1;
+  // Device pointers are read in place; host memory (pinned or pageable) is
+  // staged batch by batch by the copy engine.  A one-key digest carried from
+  // the single-sample path takes one call per batch.
+  const bool each = st->carry && st->d.K == 1;
   std::vector<const uint32_t*> dk((size_t)nbatch, nullptr);
   std::vector<const double*> dv((size_t)nbatch, nullptr);
-  for (int64_t i = 0; i < nbatch && !each; ++i) {
-    if (n[i] == 0) continue;
-    const uint32_t* kp = keys ? keys[i] : nullptr;
-    if (flags & KD_PTR_DEVICE) {
-      dk[i] = kp;
-      dv[i] = values[i];
-      continue;
-    }
-    const void* mk = kp ? mapped_view(kp) : nullptr;
-    const void* mv = mapped_view(values[i]);
-    if (!mv || (kp && !mk)) each = true;
-    dk[i] = (const uint32_t*)mk;
-    dv[i] = (const double*)mv;
+  for (int64_t i = 0; i < nbatch; ++i) {
+    dk[i] = keys ? keys[i] : nullptr;
+    dv[i] = values[i];
   }
   if (each) {
     for (int64_t i = 0; i < nbatch; ++i) {
@@ -642,7 +635,21 @@ KD_API int kd_store_ingest_many(kd_store* h, int64_t nbatch, const uint32_t* con
   const int mode = clock_mode == KD_CLOCK_TIME ? KD_MODE_TIME : KD_MODE_COUNT;
   long long done = 0;
   const int rc = kd_pipeline_ingest_many(s, st, nbatch, dk.data(), dv.data(), (const long long*)n, mode,
-                                         clock_mode == KD_CLOCK_TIME ? timestamps : nullptr, &done);
+                                         clock_mode == KD_CLOCK_TIME ? timestamps : nullptr, &done,
+                                         !(flags & KD_PTR_DEVICE));
+  if (rc == KD_ENOMEM && done == 0) {
+    // no room for the pipeline's extra buffers: one call per batch
+    for (int64_t i = 0; i < nbatch; ++i) {
+      const int r = kd_store_ingest(h, keys ? keys[i] : nullptr, values[i], n[i], clock_mode,
+                                    timestamps ? timestamps[i] : 0.0, flags);
+      if (r) {
+        if (batches_done) *batches_done = i;
+        return r;
+      }
+    }
+    if (batches_done) *batches_done = nbatch;
+    return KD_OK;
+  }
   if (batches_done) *batches_done = done;
   return rc;
 }

@@ -201,7 +201,13 @@ struct KdSession {
 #define KD_PIPE_WS 3
   KdWorkspace ws_more[KD_PIPE_WS - 1];
   cudaStream_t ahead = nullptr;
-  cudaEvent_t pipe_ev[1 + 3 * KD_PIPE_WS] = {};  // start; per workspace: front done, free, call block copied
+  // start; per workspace: front done, free, call block copied, inputs staged
+  cudaEvent_t pipe_ev[1 + 4 * KD_PIPE_WS] = {};
+  // Host inputs of a multi-batch ingest are copied by the copy engine (on
+  // `copy`) into one device staging buffer per workspace, ahead of the front.
+  cudaStream_t copy = nullptr;
+  void* d_stage[KD_PIPE_WS] = {};
+  size_t stage_bytes = 0;  // bytes of each staging buffer
   KdErrHost* h_many = nullptr;
   int* h_many_scalars = nullptr;
   long long cap_many = 0;
@@ -306,9 +312,11 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
 // with the front of batch i + 1 (prep, sort) overlapping the back of batch i.
 // On failure *done is the failing batch: batches before it are committed, it
 // and every later one are not.
+// With `host_inputs`, the key and value pointers are host memory (pinned or
+// pageable): each batch is first copied into a device staging buffer.
 int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint32_t* const* d_keys,
                             const double* const* d_vals, const long long* ns, int mode,
-                            const double* timestamps, long long* done);
+                            const double* timestamps, long long* done, bool host_inputs = false);
 void kd_ws_free(KdWorkspace& ws);
 void kd_store_drop_graphs(KdStore* st);
 int kd_cuda_fail(KdSession* s, cudaError_t e, const char* what);

@@ -2352,7 +2352,7 @@ static int pipe_fail(KdSession* s, cudaError_t e) { return kd_cuda_fail(s, e, "p
 
 int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint32_t* const* d_keys,
                             const double* const* d_vals, const long long* ns, int mode,
-                            const double* timestamps, long long* done) {
+                            const double* timestamps, long long* done, bool host_inputs) {
   *done = 0;
   if (nb <= 0) return KD_OK;
   long long nmax = 0;
@@ -2373,9 +2373,38 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
   const KdStoreDev sd = st->d;
   const long long keys_max = std::min<long long>(nmax, sd.K);
   if (!s->ahead) {
-    if (cudaStreamCreateWithFlags(&s->ahead, cudaStreamNonBlocking) != cudaSuccess) return pipe_fail(s, cudaGetLastError());
+    if (cudaStreamCreateWithFlags(&s->ahead, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking) != cudaSuccess)
+      return pipe_fail(s, cudaGetLastError());
     for (cudaEvent_t& e : s->pipe_ev)
       if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return pipe_fail(s, cudaGetLastError());
+  }
+  // Staging of host inputs: keys (16-byte aligned) then values, per workspace.
+  const size_t key_bytes = ((size_t)nmax * 4 + 15) / 16 * 16;
+  if (host_inputs && s->stage_bytes < key_bytes + (size_t)nmax * 8) {
+    const size_t need = key_bytes + (size_t)nmax * 8;
+    for (void*& p : s->d_stage) {
+      if (p) cudaFree(p);
+      p = nullptr;
+    }
+    s->mem_used -= std::min(s->mem_used, s->stage_bytes * KD_PIPE_WS);
+    s->stage_bytes = 0;
+    if (s->mem_budget && s->mem_used + need * KD_PIPE_WS > s->mem_budget) {
+      kd_set_msg(s, "device-memory budget exceeded by the multi-batch staging buffers");
+      return KD_ENOMEM;
+    }
+    for (void*& p : s->d_stage)
+      if (cudaMalloc(&p, need) != cudaSuccess) {
+        cudaGetLastError();
+        for (void*& q : s->d_stage) {
+          if (q) cudaFree(q);
+          q = nullptr;
+        }
+        kd_set_msg(s, "multi-batch staging buffers could not be allocated");
+        return KD_ENOMEM;
+      }
+    s->stage_bytes = need;
+    s->mem_used += need * KD_PIPE_WS;
   }
   if (s->cap_many < nb) {
     if (s->h_many) cudaFreeHost(s->h_many);
@@ -2400,6 +2429,34 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
   cudaEvent_t* ev_front = &s->pipe_ev[1];
   cudaEvent_t* ev_free = &s->pipe_ev[1 + KD_PIPE_WS];
   cudaEvent_t* ev_copied = &s->pipe_ev[1 + 2 * KD_PIPE_WS];
+  cudaEvent_t* ev_staged = &s->pipe_ev[1 + 3 * KD_PIPE_WS];
+  cudaStream_t C = s->copy;
+  // Batch t's inputs as the kernels read them: in place, or copied on `str`
+  // into staging buffer q (after `after`, when given).
+  auto stage = [&](long long t, int q, cudaStream_t str, cudaEvent_t after, KdStepView& v,
+                   const uint32_t** kout, const double** vout) {
+    *kout = d_keys ? d_keys[t] : nullptr;
+    *vout = d_vals[t];
+    if (!host_inputs) return;
+    if (after) v.note(cudaStreamWaitEvent(str, after, 0));
+    char* base_p = (char*)s->d_stage[q];
+    if (*kout) {
+      v.note(cudaMemcpyAsync(base_p, *kout, (size_t)ns[t] * 4, cudaMemcpyHostToDevice, str));
+      *kout = (const uint32_t*)base_p;
+    }
+    v.note(cudaMemcpyAsync(base_p + key_bytes, *vout, (size_t)ns[t] * 8, cudaMemcpyHostToDevice, str));
+    *vout = (const double*)(base_p + key_bytes);
+  };
+  // One batch alone through the one-call path (which owns the retries).
+  auto single = [&](long long t) -> int {
+    KdStepView v;
+    const uint32_t* kk = nullptr;
+    const double* vv = nullptr;
+    stage(t, 0, M, nullptr, v, &kk, &vv);
+    if (v.err != cudaSuccess) return pipe_fail(s, v.err);
+    return kd_pipeline_ingest(s, st, kk, vv, nullptr, ns[t], mode, timestamps ? timestamps[t] : 0.0,
+                              nullptr, nullptr, nullptr);
+  };
   KdWorkspace* ws[KD_PIPE_WS];
   ws[0] = &s->ws;
   for (int q = 1; q < KD_PIPE_WS; ++q) ws[q] = &s->ws_more[q - 1];
@@ -2430,9 +2487,7 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
     }
     if (!room) {
       for (long long t = base; t < nb; ++t) {
-        const int r = kd_pipeline_ingest(s, st, d_keys ? d_keys[t] : nullptr, d_vals[t], nullptr,
-                                         ns[t], mode, timestamps ? timestamps[t] : 0.0, nullptr,
-                                         nullptr, nullptr);
+        const int r = ns[t] > 0 ? single(t) : KD_OK;
         if (r) {
           *done = t;
           return r;
@@ -2493,10 +2548,18 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
       const int k = (int)(i % KD_PIPE_WS);
       KdWorkspace& w = *ws[k];
       if (i >= base + KD_PIPE_WS) v.note(cudaEventSynchronize(ev_copied[k]));  // its last user read this block
+      const uint32_t* kk = nullptr;
+      const double* vv = nullptr;
+      // the staging buffer is free once the front of its last batch has run
+      stage(i, k, C, i >= base + KD_PIPE_WS ? ev_front[k] : nullptr, v, &kk, &vv);
+      if (host_inputs) {
+        v.note(cudaEventRecord(ev_staged[k], C));
+        v.note(cudaStreamWaitEvent(A, ev_staged[k], 0));
+      }
       KdCallArgs& c = *w.h_call;
       c = KdCallArgs();
-      c.keys = d_keys ? d_keys[i] : nullptr;
-      c.vals = d_vals[i];
+      c.keys = kk;
+      c.vals = vv;
       c.timestamp = timestamps ? timestamps[i] : 0.0;
       c.err = KdErrHost{0, 0, 0x7fffffffffffffffLL};
       if (i >= base + KD_PIPE_WS) v.note(cudaStreamWaitEvent(A, ev_free[k], 0));
@@ -2528,9 +2591,7 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
       // Nothing from this batch on was committed: run it alone (the one-call
       // path owns these retries: full sort, more levels, larger scratch), then
       // pipeline the rest.
-      const int r = kd_pipeline_ingest(s, st, d_keys ? d_keys[bad] : nullptr, d_vals[bad], nullptr,
-                                       ns[bad], mode, timestamps ? timestamps[bad] : 0.0, nullptr,
-                                       nullptr, nullptr);
+      const int r = single(bad);
       if (r) {
         *done = bad;
         return r;

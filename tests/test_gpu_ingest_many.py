@@ -69,7 +69,7 @@ def test_host_batches_pinned_and_pageable(kd):
     pinned = [(torch.from_numpy(k.astype(np.int32)).pin_memory().numpy().view(np.uint32),
                torch.from_numpy(v).pin_memory().numpy()) for k, v in batches]
     a.add_batches(pinned)
-    a.add_batches(batches)  # pageable: one call per batch inside
+    a.add_batches(batches)  # pageable: staged by the copy engine too
     for _ in range(2):
         for k, v in batches:
             b.add_batch(k, v)
