@@ -63,6 +63,7 @@ extern "C" {
 #define KD_OPT_LARGE_BLOCKS_PER_SM 6  /* grid of the large-tile kernel, blocks per SM */
 #define KD_OPT_SMALL_BLOCKS_PER_SM 7  /* grid of the small-tile kernel, blocks per SM */
 #define KD_OPT_CONCURRENT_TILES 8     /* run the two tile kernels of a level on two streams */
+#define KD_OPT_FRONT_STREAMS 9        /* multi-batch ingest: fronts (prep, sort) on 1 or 2 streams */
 
 typedef struct kd_session kd_session;
 typedef struct kd_store kd_store;

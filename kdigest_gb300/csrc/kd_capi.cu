@@ -426,6 +426,7 @@ KD_API void kd_session_destroy(kd_session* h) {
   for (cudaEvent_t e : s->pipe_ev)
     if (e) cudaEventDestroy(e);
   if (s->ahead) cudaStreamDestroy(s->ahead);
+  if (s->ahead2) cudaStreamDestroy(s->ahead2);
   if (s->copy) cudaStreamDestroy(s->copy);
   for (void* p : s->d_stage)
     if (p) cudaFree(p);
@@ -496,6 +497,9 @@ KD_API int kd_session_set_option(kd_session* h, int option, int value) {
     s->small_bps = value;
   } else if (option == KD_OPT_CONCURRENT_TILES) {
     s->concurrent_tiles = value ? 1 : 0;
+  } else if (option == KD_OPT_FRONT_STREAMS) {
+    if (value < 1 || value > 2) return fail(s, KD_EINVAL, "front streams must be 1 or 2");
+    s->front_streams = value;
   } else {
     return fail(s, KD_EINVAL, "unknown option");
   }

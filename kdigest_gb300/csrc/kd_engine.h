@@ -200,7 +200,8 @@ struct KdSession {
   // status.
 #define KD_PIPE_WS 3
   KdWorkspace ws_more[KD_PIPE_WS - 1];
-  cudaStream_t ahead = nullptr;
+  cudaStream_t ahead = nullptr, ahead2 = nullptr;  // fronts alternate between the two
+  int front_streams = 2;  // 1: every front on `ahead` (a launch setting only)
   // start; per workspace: front done, free, call block copied, inputs staged
   cudaEvent_t pipe_ev[1 + 4 * KD_PIPE_WS] = {};
   // Host inputs of a multi-batch ingest are copied by the copy engine (on

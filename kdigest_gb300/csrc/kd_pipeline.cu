@@ -2339,8 +2339,9 @@ int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const 
 }
 
 // Pipelined multi-batch ingest.  Batch i uses workspace i mod 3.  Its front
-// (per-call block, prep, sort, unpack, repair: reads only the batch) runs on the
-// `ahead` stream once the back of batch i - 3 has released that workspace; its
+// (per-call block, prep, sort, unpack, repair: reads only the batch) runs on one
+// of two `ahead` streams (alternating, so that consecutive fronts may overlap)
+// once the back of batch i - 3 has released that workspace; its
 // back (touched keys, prepare, levels, commit: reads and writes the store) runs
 // on the session stream after the back of batch i - 1 and its own front.  So
 // the sort of one batch overlaps the compress of the previous one, and the
@@ -2374,6 +2375,7 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
   const long long keys_max = std::min<long long>(nmax, sd.K);
   if (!s->ahead) {
     if (cudaStreamCreateWithFlags(&s->ahead, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->ahead2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking) != cudaSuccess)
       return pipe_fail(s, cudaGetLastError());
     for (cudaEvent_t& e : s->pipe_ev)
@@ -2542,11 +2544,14 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
     v.note(cudaMemsetAsync(chain, 0, sizeof(int), M));
     v.note(cudaEventRecord(ev_start, M));  // the ahead stream starts after all earlier work
     v.note(cudaStreamWaitEvent(A, ev_start, 0));
+    v.note(cudaStreamWaitEvent(s->ahead2, ev_start, 0));
     for (long long i = base; i < nb; ++i) {
       s->h_many[i] = KdErrHost{0, 0, 0};
       if (ns[i] == 0) continue;  // an empty batch changes nothing
       const int k = (int)(i % KD_PIPE_WS);
       KdWorkspace& w = *ws[k];
+      // consecutive fronts on two streams, so that they may overlap each other too
+      cudaStream_t A = (s->front_streams > 1 && (i & 1)) ? s->ahead2 : s->ahead;
       if (i >= base + KD_PIPE_WS) v.note(cudaEventSynchronize(ev_copied[k]));  // its last user read this block
       const uint32_t* kk = nullptr;
       const double* vv = nullptr;
