@@ -185,3 +185,26 @@ def test_single_digest_batches(kd):
         assert np.array_equal(ma, mb) and np.array_equal(wa, wb), f"pre={pre}"
         assert a.state() == b.state()
         assert a.to_bytes() == b.to_bytes()
+
+
+def test_two_stores_share_the_pipeline(kd):
+    """Stores of one session take turns (they share the workspaces and the
+    streams, each keeps its own graphs), with batch sizes that change between
+    calls; every store equals its one-call-per-batch twin."""
+    import torch
+
+    sess = kd.GpuSession()
+    ref_sess = kd.GpuSession()
+    sizes = (700, 5000)
+    stores = [kd.GroupedTDigest(k, 100.0, scale=kd.K1, session=sess) for k in sizes]
+    refs = [kd.GroupedTDigest(k, 100.0, scale=kd.K1, session=ref_sess) for k in sizes]
+    for rnd in range(3):
+        for j, nk in enumerate(sizes):
+            n = (30000, 8000, 30000)[rnd] + j
+            batches = _batches(nk, [n] * (2 + rnd), 100 * rnd + j)
+            stores[j].add_batches([(torch.from_numpy(k).cuda(), torch.from_numpy(v).cuda())
+                                   for k, v in batches])
+            for k, v in batches:
+                refs[j].add_batch(k, v)
+    for g, r, nk in zip(stores, refs, sizes):
+        _same(g, r, nk)
