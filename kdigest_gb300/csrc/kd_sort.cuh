@@ -58,8 +58,10 @@ static __global__ void __launch_bounds__(KD_RS_THREADS) kd_rs_hist_all(
        i += (long long)gridDim.x * KD_RS_THREADS) {
     const uint64_t v = k64[i];
     for (int p = first_digit; p < 8; ++p) atomicAdd(&h[p][(unsigned)(v >> (8 * p)) & 255u], 1u);
-    const uint32_t kk = key[i];
-    for (int p = 0; p < key_passes; ++p) atomicAdd(&h[8 + p][(kk >> (8 * p)) & 255u], 1u);
+    if (key_passes > 0) {  // the packed form carries no key digits: skip the read
+      const uint32_t kk = key[i];
+      for (int p = 0; p < key_passes; ++p) atomicAdd(&h[8 + p][(kk >> (8 * p)) & 255u], 1u);
+    }
   }
   __syncthreads();
   const int used = (8 + key_passes) * 256;
