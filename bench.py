@@ -1087,9 +1087,9 @@ def run_gpu(args):
     # the top 40 value bits in 8-bit digits (7 passes), the unpack repairs the rest
     passes = 7
     alg = {
-        # one histogram read of the 12 B pairs for all passes, per pass a read
+        # one histogram read of the 8 B packed keys for all passes, per pass a read
         # and a write of every pair, then the unpack (read + write)
-        "sort": (12 + passes * 24 + 24) * BATCH,
+        "sort": (8 + passes * 24 + 24) * BATCH,
         "level0": 8 * BATCH + touched_avg * 16 * 2 * prior_avg,
         "prep": 12 * BATCH + 12 * BATCH,
     }
