@@ -1097,7 +1097,7 @@ def run_gpu(args):
     # 2^22-pair batch: `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum`
     # on GB300 (profiles/launches_dram_grouped_ingest_65536keys_batch2p22.md).
     # Below the algorithmic bytes: the ping-pong buffers largely stay in L2.
-    traffic = {"sort": 473.1e6 * BATCH / (1 << 22)}
+    traffic = {"sort": 474.7e6 * BATCH / (1 << 22)}
     dom_bytes = alg.get(dom, comp_bytes)
     achieved = dom_bytes / (stage_ms[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
