@@ -267,6 +267,7 @@ struct KdStore {
   // its back (with the chain flag the back's commit was captured with).
   KdGraphEntry pipe_graphs[KD_PIPE_WS][2];
   const int* pipe_chain[KD_PIPE_WS] = {};
+  long long pipe_last_n = -1;  // size of the last batch of the last multi-batch call
   // Single-sample path state (one-key stores).  `pending`: samples wait in the
   // buffer.  `carry`: the next batch must carry the centroids and buffer in
   // its input (their order is the sequential pass's, not the batch path's).

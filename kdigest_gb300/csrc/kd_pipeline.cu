@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <unordered_map>
 #include <atomic>
 #include <cstdio>
 #include <cstddef>
@@ -2459,6 +2460,18 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
     return kd_pipeline_ingest(s, st, kk, vv, nullptr, ns[t], mode, timestamps ? timestamps[t] : 0.0,
                               nullptr, nullptr, nullptr);
   };
+  // again[i]: batch i's size recurs in this call (or the batch before it,
+  // possibly the last batch of the previous call, had the same size)
+  std::vector<char> again((size_t)nb, 0);
+  {
+    std::unordered_map<long long, long long> last;
+    for (long long i = nb - 1; i >= 0; --i) {
+      const long long prev = i > 0 ? ns[i - 1] : st->pipe_last_n;
+      again[(size_t)i] = (last.count(ns[i]) || prev == ns[i]) ? 1 : 0;
+      last[ns[i]] = i;
+    }
+  }
+  st->pipe_last_n = ns[nb - 1];
   KdWorkspace* ws[KD_PIPE_WS];
   ws[0] = &s->ws;
   for (int q = 1; q < KD_PIPE_WS; ++q) ws[q] = &s->ws_more[q - 1];
@@ -2504,12 +2517,12 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
     // graph for this workspace and part when its shape was captured, else
     // captured now (eager if capture fails).
     auto run_part = [&](int part, int q, KdWorkspace& w, long long n, cudaStream_t str,
-                        const KdTailOut* out, KdStepView& v) {
+                        const KdTailOut* out, KdStepView& v, bool capture) {
       const KdGraphKey key = step_key(s, sd, w, n, false, mode, L);
       KdGraphEntry& g = st->pipe_graphs[q][part == KD_PART_FRONT ? 0 : 1];
       const bool chain_ok = part == KD_PART_FRONT || st->pipe_chain[q] == chain;
       s->stream = str;
-      if (!(g.exec && g.key == key && chain_ok) && s->use_graphs) {
+      if (!(g.exec && g.key == key && chain_ok) && s->use_graphs && capture) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g = KdGraphEntry();
         cudaGraph_t graph = nullptr;
@@ -2528,7 +2541,7 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
         }
         cudaGetLastError();  // a capture that failed runs eagerly below
       }
-      if (g.exec && g.key == key) {
+      if (g.exec && g.key == key && chain_ok) {
         v.note(cudaGraphLaunch(g.exec, str));
         v.launches += g.launches;
       } else {
@@ -2570,12 +2583,15 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
       if (i >= base + KD_PIPE_WS) v.note(cudaStreamWaitEvent(A, ev_free[k], 0));
       KdSortBufs sb = sort_bufs(w);
       kd_rs_epoch_reserve(sb, A);
-      run_part(KD_PART_FRONT, k, w, ns[i], A, nullptr, v);
+      // capture only a batch size that comes again in this call (a new
+      // size for every batch would pay a capture per batch)
+      const bool capture = again[i];
+      run_part(KD_PART_FRONT, k, w, ns[i], A, nullptr, v, capture);
       v.note(cudaEventRecord(ev_copied[k], A));
       v.note(cudaEventRecord(ev_front[k], A));
       v.note(cudaStreamWaitEvent(M, ev_front[k], 0));
       KdTailOut out{chain, nullptr, nullptr, true};
-      run_part(KD_PART_BACK, k, w, ns[i], M, &out, v);
+      run_part(KD_PART_BACK, k, w, ns[i], M, &out, v, capture);
       v.note(cudaMemcpyAsync(&s->h_many[i], w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, M));
       v.note(cudaEventRecord(ev_free[k], M));
     }
