@@ -63,3 +63,28 @@ def test_full_size_grouped_ingest_properties(kd):
     h = kd.GroupedTDigest(nk, bench.COMPRESSION, scale=kd.K3)
     h.import_records(data, offs)
     assert h.export()[0] == data
+
+
+def test_full_size_pipelined_equals_one_call_per_batch(kd):
+    """The whole 2^27-sample stream through one pipelined add_batches call ends
+    bit for bit where one kd_store_ingest per 2^22 batch ends."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    torch = pytest.importorskip("torch")
+    from kdigest_gb300 import _native as N
+
+    nk, batch, total = bench.NUM_KEYS, bench.BATCH, bench.TOTAL
+    keys, vals = bench.make_workload(total=total)
+    dk = torch.from_numpy(keys.view(np.int32)).cuda()
+    dv = torch.from_numpy(vals).cuda()
+    nb = total // batch
+    a = kd.GroupedTDigest(nk, bench.COMPRESSION, scale=kd.K3)
+    b = kd.GroupedTDigest(nk, bench.COMPRESSION, scale=kd.K3)
+    a.add_batches([(dk[i * batch:(i + 1) * batch], dv[i * batch:(i + 1) * batch]) for i in range(nb)])
+    L = N.load()
+    for i in range(nb):
+        rc = L.kd_store_ingest(b._store._h, dk.data_ptr() + 4 * i * batch, dv.data_ptr() + 8 * i * batch,
+                               batch, N.KD_CLOCK_COUNT, 0.0, N.KD_PTR_DEVICE)
+        assert rc == 0
+    assert a.export()[0] == b.export()[0]  # every key's header and centroids
