@@ -155,15 +155,19 @@ def measured_peaks() -> dict:
 # ----------------------------------------------------------------------------
 # CPU arms (oracle = CPU restatement of the reference path)
 # ----------------------------------------------------------------------------
-def cpu_ingest_rate(keys, vals, threads: int, target_s: float = 12.0):
+def cpu_ingest_rate(keys, vals, threads: int, target_s: float = 12.0, max_batches: int | None = None):
     """Time the oracle's grouped P-path ingest on whole batches of the stream
-    until about target_s seconds of CPU work; returns samples/s and the sample."""
+    until about target_s seconds of CPU work (or max_batches batches, the ones
+    the GPU store ingested, so that the two can be compared); returns
+    samples/s and the sample."""
     from oracle import pyoracle as o
 
     digests = [o.Digest(o.K3, COMPRESSION, 0.0) for _ in range(NUM_KEYS)]
     done = 0
     t_total = 0.0
     nb = len(vals) // BATCH
+    if max_batches is not None:
+        nb = min(nb, max_batches)
     for b in range(nb):
         sl = slice(b * BATCH, (b + 1) * BATCH)
         t0 = time.perf_counter()
@@ -1189,7 +1193,7 @@ def run_gpu(args):
     parity = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, done, t, odig = cpu_ingest_rate(keys, vals, threads)
+        v, done, t, odig = cpu_ingest_rate(keys, vals, threads, max_batches=len(ingested))
         cpu = {"value": v, "unit": "samples/s", "cores": threads, "kind": "port",
                "sample": f"first {done} batches of 2^22 pairs ({t:.1f} s, C oracle P-path, key-partitioned threads)"}
         if ingested == list(range(done)):
