@@ -209,8 +209,9 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
         "ms_per_step": 1e3 * sum(per_step) / k, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy, host)",
-        "config": {"workload": WORKLOAD, "keys": NUM_KEYS, "batch": BATCH, "scale": "K3",
-                   "compression": COMPRESSION},
+        "config": {"workload": WORKLOAD, "keys": NUM_KEYS, "batch": BATCH, "total": TOTAL, "scale": "K3",
+                   "compression": COMPRESSION, "parallelism": "single",
+                   "timing": "host wall clock around each batch's grouped ingest in the C oracle"},
         "cpu_baseline": {"value": v, "unit": "samples/s", "cores": threads, "kind": "port",
                          "sample": f"{k} batches of 2^22 pairs of the stream (C oracle, P-path, key-partitioned threads)"},
         "e2e": {"value": v, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
