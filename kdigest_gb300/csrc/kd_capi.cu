@@ -113,7 +113,8 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
                            : 0;
   kd_ws_free(w);
   s->mem_used -= std::min(s->mem_used, old_bytes);
-  long long parts = kd_scan_partials_needed(std::max(nn, kk)) + 4;
+  // room for a one-item-per-thread scan over the keys as well as the default one over the samples
+  long long parts = std::max(kd_scan_partials_needed(nn), kd_scan_partials_needed(kk, 1)) + 4;
   size_t need = ws_bytes(nn, kk, ii, ww, mm, tt, parts);
   if (s->mem_budget && s->mem_used + need > s->mem_budget) {
     char buf[200];

@@ -2117,7 +2117,13 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   const uint64_t* k64 = w.k64[r];
   const uint32_t* skey = w.key[r];
   const uint32_t* sidx = with_idx ? w.idx[r] : nullptr;
-  if (key_level)
+  // scans with one entry per key: one item per thread when the partials fit
+  const bool key_items1 = kd_scan_partials_needed(std::max<long long>(sd.K, keys_max), 1) <= w.cap_partials;
+  if (key_level && key_items1)
+    kd_scan<1>(KeyTouchedSrc{w.kstamp, w.kepoch},
+               KeyTouchedDst{w.kfirst, w.tkey, w.tstart, w.tmap, w.cap_keys}, sd.K, w.partials,
+               &w.totals[0], str);
+  else if (key_level)
     kd_scan(KeyTouchedSrc{w.kstamp, w.kepoch},
             KeyTouchedDst{w.kfirst, w.tkey, w.tstart, w.tmap, w.cap_keys}, sd.K, w.partials,
             &w.totals[0], str);
@@ -2137,9 +2143,14 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   l0.M = (int*)&w.totals[1] + 3;
   l0.I = (int*)&w.totals[2] + 0;
   int* a1 = (int*)&w.totals[1] + 2;
-  kd_scan(Plan0Src{w.totals, w.tm, s->small_cap},
-          Plan0Dst{w.totals, w.tm, l0, w.lv[1], w.cap_work, w.cap_keys, s->small_cap}, keys_max,
-          w.partials, &w.totals[1], str);
+  if (key_items1)
+    kd_scan<1>(Plan0Src{w.totals, w.tm, s->small_cap},
+               Plan0Dst{w.totals, w.tm, l0, w.lv[1], w.cap_work, w.cap_keys, s->small_cap}, keys_max,
+               w.partials, &w.totals[1], str);
+  else
+    kd_scan(Plan0Src{w.totals, w.tm, s->small_cap},
+            Plan0Dst{w.totals, w.tm, l0, w.lv[1], w.cap_work, w.cap_keys, s->small_cap}, keys_max,
+            w.partials, &w.totals[1], str);
   {
     InterArgs ia{a1, l0, w.lv[1], l0.I, w.cap_inter, w.needs, w.err};
     k_inter0<<<1, 1024, 0, str>>>(ia);

@@ -51,13 +51,13 @@ __device__ __forceinline__ int4 block_scan_incl(int4 v, int4* smem_warp, int4* t
   return v;
 }
 
-template <class Src>
+template <class Src, int ITEMS = KD_SCAN_ITEMS>
 __global__ void __launch_bounds__(KD_SCAN_THREADS) kd_scan_reduce(Src src, long long n, int4* partials) {
   __shared__ int4 sw[32];
-  long long base = (long long)blockIdx.x * KD_SCAN_TILE + (long long)threadIdx.x * KD_SCAN_ITEMS;
+  long long base = (long long)blockIdx.x * (KD_SCAN_THREADS * ITEMS) + (long long)threadIdx.x * ITEMS;
   int4 acc = make_int4(0, 0, 0, 0);
 #pragma unroll
-  for (int k = 0; k < KD_SCAN_ITEMS; ++k) {
+  for (int k = 0; k < ITEMS; ++k) {
     long long i = base + k;
     if (i < n) acc = i4add(acc, src(i));
   }
@@ -84,15 +84,15 @@ static __global__ void __launch_bounds__(1024) kd_scan_partials(int4* partials, 
   if (threadIdx.x == 0 && total) *total = tot;
 }
 
-template <class Src, class Dst>
+template <class Src, class Dst, int ITEMS = KD_SCAN_ITEMS>
 __global__ void __launch_bounds__(KD_SCAN_THREADS) kd_scan_apply(Src src, Dst dst, long long n,
                                                                  const int4* partials) {
   __shared__ int4 sw[32];
-  long long base = (long long)blockIdx.x * KD_SCAN_TILE + (long long)threadIdx.x * KD_SCAN_ITEMS;
-  int4 vals[KD_SCAN_ITEMS];
+  long long base = (long long)blockIdx.x * (KD_SCAN_THREADS * ITEMS) + (long long)threadIdx.x * ITEMS;
+  int4 vals[ITEMS];
   int4 acc = make_int4(0, 0, 0, 0);
 #pragma unroll
-  for (int k = 0; k < KD_SCAN_ITEMS; ++k) {
+  for (int k = 0; k < ITEMS; ++k) {
     long long i = base + k;
     vals[k] = i < n ? src(i) : make_int4(0, 0, 0, 0);
     acc = i4add(acc, vals[k]);
@@ -102,27 +102,31 @@ __global__ void __launch_bounds__(KD_SCAN_THREADS) kd_scan_apply(Src src, Dst ds
   int4 run = i4add(partials[blockIdx.x],
                    make_int4(incl.x - acc.x, incl.y - acc.y, incl.z - acc.z, incl.w - acc.w));
 #pragma unroll
-  for (int k = 0; k < KD_SCAN_ITEMS; ++k) {
+  for (int k = 0; k < ITEMS; ++k) {
     long long i = base + k;
     if (i < n) dst(i, run, vals[k]);
     run = i4add(run, vals[k]);
   }
 }
 
-// Host launcher.  `partials` must hold ceil(n_max / KD_SCAN_TILE) int4s.
-template <class Src, class Dst>
+// Host launcher.  `partials` must hold ceil(n_max / (KD_SCAN_THREADS * ITEMS))
+// int4s.  Fewer items per thread give more blocks: for short scans (one entry
+// per key) that spreads them over the GPU instead of a few blocks.
+template <int ITEMS = KD_SCAN_ITEMS, class Src, class Dst>
 static inline void kd_scan(Src src, Dst dst, long long n_max, int4* partials, int4* total,
                            cudaStream_t st) {
   if (n_max <= 0) {
     if (total) cudaMemsetAsync(total, 0, sizeof(int4), st);
     return;
   }
-  int nb = (int)((n_max + KD_SCAN_TILE - 1) / KD_SCAN_TILE);
-  kd_scan_reduce<Src><<<nb, KD_SCAN_THREADS, 0, st>>>(src, n_max, partials);
+  constexpr long long tile = (long long)KD_SCAN_THREADS * ITEMS;
+  int nb = (int)((n_max + tile - 1) / tile);
+  kd_scan_reduce<Src, ITEMS><<<nb, KD_SCAN_THREADS, 0, st>>>(src, n_max, partials);
   kd_scan_partials<<<1, 1024, 0, st>>>(partials, nb, total);
-  kd_scan_apply<Src, Dst><<<nb, KD_SCAN_THREADS, 0, st>>>(src, dst, n_max, partials);
+  kd_scan_apply<Src, Dst, ITEMS><<<nb, KD_SCAN_THREADS, 0, st>>>(src, dst, n_max, partials);
 }
 
-static inline long long kd_scan_partials_needed(long long n_max) {
-  return (n_max + KD_SCAN_TILE - 1) / KD_SCAN_TILE + 1;
+static inline long long kd_scan_partials_needed(long long n_max, int items = KD_SCAN_ITEMS) {
+  const long long tile = (long long)KD_SCAN_THREADS * items;
+  return (n_max + tile - 1) / tile + 1;
 }
