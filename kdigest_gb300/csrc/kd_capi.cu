@@ -432,7 +432,6 @@ KD_API void kd_session_destroy(kd_session* h) {
   for (void* p : s->d_stage)
     if (p) cudaFree(p);
   if (s->h_many) cudaFreeHost(s->h_many);
-  if (s->h_many_scalars) cudaFreeHost(s->h_many_scalars);
   for (int i = 0; i <= KD_NSTAGES; ++i)
     if (s->stats.ev[i]) cudaEventDestroy(s->stats.ev[i]);
   cudaEventDestroy(s->join_ev);

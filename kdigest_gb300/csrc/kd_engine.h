@@ -210,7 +210,6 @@ struct KdSession {
   void* d_stage[KD_PIPE_WS] = {};
   size_t stage_bytes = 0;  // bytes of each staging buffer
   KdErrHost* h_many = nullptr;
-  int* h_many_scalars = nullptr;
   long long cap_many = 0;
   KdStageStats stats;
   struct KdStore* scratch_store = nullptr;  // 1-key store for stateless compress

@@ -2021,14 +2021,12 @@ static void enqueue_levels(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, i
   }
 }
 
-// Where a step's commit reports: the batch chain of a pipelined multi-batch
-// ingest and the host slots its status and scratch needs are read back into
-// (null: no chain, the workspace's own slots).
+// How a step's commit reports inside a pipelined multi-batch ingest: the batch
+// chain flag, and no readback into the workspace's host slots (the caller
+// copies each batch's status into a slot of its own).
 struct KdTailOut {
   int* chain = nullptr;
-  KdErrHost* h_err = nullptr;
-  int* h_scalars = nullptr;
-  bool no_readback = false;  // the caller copies the status back itself
+  bool no_readback = false;
 };
 
 // Commit (prune, prefix, slot flip) and the status readback.
@@ -2047,10 +2045,8 @@ static void enqueue_tail(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, lon
   stage_mark(s, 6);
   v.note(cudaGetLastError());
   if (out && out->no_readback) return;
-  v.note(cudaMemcpyAsync(out && out->h_err ? out->h_err : w.h_err, w.err, sizeof(KdErrHost),
-                         cudaMemcpyDeviceToHost, str));
-  v.note(cudaMemcpyAsync(out && out->h_scalars ? out->h_scalars : w.h_scalars, w.needs,
-                         sizeof(int) * 4, cudaMemcpyDeviceToHost, str));
+  v.note(cudaMemcpyAsync(w.h_err, w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, str));
+  v.note(cudaMemcpyAsync(w.h_scalars, w.needs, sizeof(int) * 4, cudaMemcpyDeviceToHost, str));
 }
 
 // One whole ingest step as device work only (so it can be captured): the
@@ -2422,13 +2418,10 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
   }
   if (s->cap_many < nb) {
     if (s->h_many) cudaFreeHost(s->h_many);
-    if (s->h_many_scalars) cudaFreeHost(s->h_many_scalars);
     s->h_many = nullptr;
-    s->h_many_scalars = nullptr;
     s->cap_many = 0;
     const long long cap = std::max<long long>(nb, 64);
-    if (cudaHostAlloc((void**)&s->h_many, sizeof(KdErrHost) * cap, cudaHostAllocDefault) != cudaSuccess ||
-        cudaHostAlloc((void**)&s->h_many_scalars, sizeof(int) * 4 * cap, cudaHostAllocDefault) != cudaSuccess) {
+    if (cudaHostAlloc((void**)&s->h_many, sizeof(KdErrHost) * cap, cudaHostAllocDefault) != cudaSuccess) {
       cudaGetLastError();
       kd_set_msg(s, "pinned status slots for a multi-batch ingest could not be allocated");
       return KD_ENOMEM;
@@ -2601,7 +2594,7 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
       v.note(cudaEventRecord(ev_copied[k], A));
       v.note(cudaEventRecord(ev_front[k], A));
       v.note(cudaStreamWaitEvent(M, ev_front[k], 0));
-      KdTailOut out{chain, nullptr, nullptr, true};
+      KdTailOut out{chain, true};
       run_part(KD_PART_BACK, k, w, ns[i], M, &out, v, capture);
       v.note(cudaMemcpyAsync(&s->h_many[i], w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, M));
       v.note(cudaEventRecord(ev_free[k], M));
