@@ -1155,7 +1155,8 @@ def run_gpu(args):
         e2e = {"value": args.steps * BATCH / t_many, "unit": "samples/s",
                "h2d_bytes_per_step": 12 * BATCH, "d2h_bytes_per_step": 16,
                "timing": "host wall clock around one kd_store_ingest_many over the timed steps "
-                         "(pinned host inputs read in place; status read back per batch)",
+                         "(pinned host inputs copied to HBM batch by batch by the copy engine, "
+                         "overlapping earlier batches; status read back per batch)",
                "per_call": e2e_per_call}
 
     # Plain per-digest form: one digest per call, no graph (one batch).
