@@ -1139,7 +1139,7 @@ def run_gpu(args):
                         "h2d_bytes_per_step": 12 * BATCH, "d2h_bytes_per_step": 16,
                         "timing": "host wall clock around each kd_store_ingest (pinned host inputs)"}
         del store2
-        # the pipelined call from pinned host buffers (read in place over the host link)
+        # the pipelined call from pinned host buffers (staged to HBM by the copy engine)
         store4 = kd.GroupedTDigest(NUM_KEYS, COMPRESSION, scale=kd.K3, session=sess)
         h4 = store4._store._h
         warm_h = slices(0, args.warmup, pk, pv)
