@@ -208,3 +208,22 @@ def test_two_stores_share_the_pipeline(kd):
                 refs[j].add_batch(k, v)
     for g, r, nk in zip(stores, refs, sizes):
         _same(g, r, nk)
+
+
+@pytest.mark.parametrize("graphs,fronts", [(0, 2), (1, 1), (0, 1)])
+def test_eager_and_one_front_stream(kd, graphs, fronts):
+    """Graphs off (every part enqueued eagerly) and a single front stream give
+    the same store as one call per batch."""
+    import torch
+
+    import kdigest_gb300._native as N
+
+    nk = 900
+    a, b = _pair(kd, nk)
+    a._store.session.set_option(N.KD_OPT_GRAPHS, graphs)
+    a._store.session.set_option(N.KD_OPT_FRONT_STREAMS, fronts)
+    batches = _batches(nk, [20000] * 5, 77 + graphs + 2 * fronts)
+    a.add_batches([(torch.from_numpy(k).cuda(), torch.from_numpy(v).cuda()) for k, v in batches])
+    for k, v in batches:
+        b.add_batch(k, v)
+    _same(a, b, nk)
