@@ -1234,6 +1234,9 @@ def run_gpu(args):
                    "timing": "CUDA events around one add_batches call over the timed steps "
                              "(sort of batch i+1 overlapping the compress of batch i)"},
         "pipelined_equals_per_call": same,
+        "pipeline": {"workspaces": 3, "front_streams": 2, "graphs": "per workspace, front and back",
+                     "overlap": "prep + sort of later batches beside touched keys, prepare, levels and "
+                                "commit of earlier ones; store updates in batch order"},
         "per_call": per_call,
         "queries_per_s": qps,
         "step_roofline": {"compulsory_bytes": int(comp_bytes), "achieved": round(step_gbs, 1),
