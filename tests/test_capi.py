@@ -59,3 +59,17 @@ def test_decay_constructors():
     for h in (0.0, -1.0):
         with pytest.raises(ValueError):
             Decay.half_life(h)
+
+
+def test_python_constants_match_the_header():
+    """Every KD_OPT_* / KD_CLOCK_* / KD_PTR_* constant the Python side uses has
+    the header's value."""
+    from kdigest_gb300 import _native
+
+    src = open(os.path.join(ROOT, "include", "kdigest_gb300.h")).read()
+    defs = {m.group(1): int(m.group(2))
+            for m in re.finditer(r"#define\s+(KD_(?:OPT|CLOCK|PTR)_\w+)\s+(\d+)", src)}
+    used = {n: getattr(_native, n) for n in dir(_native) if re.fullmatch(r"KD_(OPT|CLOCK|PTR)_\w+", n)}
+    assert used, "no constants found"
+    for name, value in used.items():
+        assert defs.get(name) == value, (name, value, defs.get(name))
