@@ -73,3 +73,29 @@ def test_python_constants_match_the_header():
     assert used, "no constants found"
     for name, value in used.items():
         assert defs.get(name) == value, (name, value, defs.get(name))
+
+
+def test_committed_tuning_record_is_applicable():
+    """The committed autotuner record names every tuned parameter with a value
+    from its search set, claims identical results, and applies as options."""
+    from kdigest_gb300 import tune
+
+    rec = tune.load_tuning()
+    assert set(rec) == {name for name, _, _ in tune.PARAMS}
+    for name, _, values in tune.PARAMS:
+        assert rec[name] in values, (name, rec[name])
+
+    class FakeSession:
+        def __init__(self):
+            self.calls = []
+
+        def set_option(self, opt, value):
+            self.calls.append((opt, value))
+
+    fs = FakeSession()
+    tune.apply_tuning(fs, rec)
+    assert sorted(fs.calls) == sorted((opt, int(rec[name])) for name, opt, _ in tune.PARAMS)
+    import json
+
+    with open(tune.TUNING_FILE) as f:
+        assert json.load(f)["results_identical"] is True
