@@ -99,3 +99,17 @@ def test_committed_tuning_record_is_applicable():
 
     with open(tune.TUNING_FILE) as f:
         assert json.load(f)["results_identical"] is True
+
+
+def test_library_defaults_match_the_tuning_record():
+    """KdSession's built-in launch settings are the committed record's choice,
+    so a session that skips the record (tuned=False) runs the same shapes."""
+    from kdigest_gb300 import tune
+
+    rec = tune.load_tuning()
+    src = open(os.path.join(ROOT, "kdigest_gb300", "csrc", "kd_engine.h")).read()
+    field = {"small_tile_cap": "small_cap", "large_blocks_per_sm": "large_bps",
+             "small_blocks_per_sm": "small_bps", "concurrent_tiles": "concurrent_tiles"}
+    for name, member in field.items():
+        m = re.search(r"int\s+%s\s*=\s*(\d+);" % member, src)
+        assert m and int(m.group(1)) == rec[name], (name, member)
