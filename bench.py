@@ -1099,9 +1099,8 @@ def run_gpu(args):
         "prep": 12 * BATCH + 12 * BATCH,
     }
     # DRAM bytes of one sort stage (histogram, 7 packed passes, unpack, repair) of a
-    # 2^22-pair batch: `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum`
-    # on GB300 (profiles/launches_dram_grouped_ingest_65536keys_batch2p22.md).
-    # Below the algorithmic bytes: the ping-pong buffers largely stay in L2.
+    # 2^22-pair batch, from `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum`
+    # on GB300.  Below the algorithmic bytes: the pass writes largely stay in L2.
     traffic = {"sort": 474.7e6 * BATCH / (1 << 22)}
     dom_bytes = alg.get(dom, comp_bytes)
     achieved = dom_bytes / (stage_ms[dom] / 1e3) / 1e9

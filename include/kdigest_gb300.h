@@ -8,7 +8,7 @@
  *
  * Each declaration cites the reference interface it replaces (paths inside the
  * kdigest project, src/kdigest/...).  The reference's GPU backend is Mojo/MAX;
- * its host code would bind these symbols with external_call (INTEGRATION.md).
+ * its host code would bind these symbols with external_call.
  */
 #ifndef KDIGEST_GB300_H
 #define KDIGEST_GB300_H
@@ -36,7 +36,7 @@ extern "C" {
 #define KD_ECONVERGE 4  /* P-path pass could not shrink a key (the reference loops forever) */
 #define KD_ENOMEM 5     /* over the session's device-memory budget / allocation failure */
 #define KD_ECUDA 6      /* CUDA runtime error */
-#define KD_ETIMEOUT 7   /* a bounded device wait gave up (serving loop) */
+#define KD_ETIMEOUT 7   /* a bounded device wait gave up (sort look-back, key map, serving loop) */
 
 /* Scale functions — src/kdigest/scale.mojo:78-200 (ScaleK0..ScaleK3). */
 #define KD_K0 0
@@ -64,6 +64,14 @@ extern "C" {
 #define KD_OPT_SMALL_BLOCKS_PER_SM 7  /* grid of the small-tile kernel, blocks per SM */
 #define KD_OPT_CONCURRENT_TILES 8     /* run the two tile kernels of a level on two streams */
 #define KD_OPT_FRONT_STREAMS 9        /* multi-batch ingest: fronts (prep, sort) on 1 or 2 streams */
+/* Tests only: with a value v > 0, every radix pass leaves its first tile's
+ * look-back word unpublished, kd_keymap_map leaves the id of its first input
+ * key unpublished when it inserts that key, and the waits on those words give
+ * up after v polls: an ingest returns KD_ETIMEOUT and changes no digest; a map
+ * call returns KD_ETIMEOUT when the key occurs again in the call, and the map
+ * keeps the key without a published id (later lookups of it time out too).
+ * 0 (default) is off. */
+#define KD_OPT_TEST_WAIT 10
 
 typedef struct kd_session kd_session;
 typedef struct kd_store kd_store;
@@ -255,12 +263,17 @@ KD_API void kd_keymap_destroy(kd_keymap* m);
  * the call returns once that work is done.  It allocates nothing: its working
  * memory is one fixed device array of KD_NOALLOC_SCRATCH_BYTES in the library,
  * held on every GPU that loads the library until the process exits.
- * n > KD_NOALLOC_MAX_N returns KD_ERANGE with *out_n = 0.  The first call on a
- * device resolves that array's address and sets kernel attributes; make it
- * before any stream capture.  All calls on a device share the array (it keeps
- * the last call's contents; each call clears what must start at zero), so calls
- * whose GPU work overlaps race and give wrong results.  On failure, msg (may be
- * NULL) receives up to msg_cap bytes of text. */
+ * n > KD_NOALLOC_MAX_N returns KD_ERANGE with *out_n = 0.  KD_ENOMEM would
+ * mean an input needed more working memory than the array's fixed layout; no
+ * input of at most KD_NOALLOC_MAX_N centroids does (each level of the tile
+ * hierarchy holds at most what the level before it held).  The first call on a
+ * device resolves that array's address and sets kernel attributes.  No call
+ * can be captured in a CUDA graph: each one synchronises its stream and reads
+ * results back through host memory, so a call on a capturing stream returns
+ * KD_EINVAL without touching the stream.  All calls on a device share the array
+ * (it keeps the last call's contents; each call clears what must start at
+ * zero), so calls whose GPU work overlaps race and give wrong results.  On
+ * failure, msg (may be NULL) receives up to msg_cap bytes of text. */
 #define KD_NOALLOC_MAX_N 16384
 #define KD_NOALLOC_SCRATCH_BYTES (2 * 1024 * 1024)
 KD_API int kd_compress_noalloc(int scale, double compression, const double* means,

@@ -21,6 +21,7 @@ KD_OPT_FORCE_EXACT_K, KD_OPT_MAX_LEVELS, KD_OPT_STAGE_TIMING, KD_OPT_GRAPHS = 1,
 KD_OPT_SMALL_TILE_CAP, KD_OPT_LARGE_BLOCKS_PER_SM, KD_OPT_SMALL_BLOCKS_PER_SM = 5, 6, 7
 KD_OPT_CONCURRENT_TILES = 8
 KD_OPT_FRONT_STREAMS = 9
+KD_OPT_TEST_WAIT = 10
 STAGES = ("prep", "sort", "plan", "level0", "levels", "commit")
 
 EXPORTED = (

@@ -500,6 +500,9 @@ KD_API int kd_session_set_option(kd_session* h, int option, int value) {
   } else if (option == KD_OPT_FRONT_STREAMS) {
     if (value < 1 || value > 2) return fail(s, KD_EINVAL, "front streams must be 1 or 2");
     s->front_streams = value;
+  } else if (option == KD_OPT_TEST_WAIT) {
+    if (value < 0 || value > (1 << 22)) return fail(s, KD_EINVAL, "test wait limit must be in [0, 2^22]");
+    s->wait_test = value;
   } else {
     return fail(s, KD_EINVAL, "unknown option");
   }

@@ -190,6 +190,10 @@ struct KdSession {
   // Run a level's two tile kernels on two streams (the second joins back
   // before anything reads their outputs).  Also a launch setting only.
   int concurrent_tiles = 1;
+  // Tests only (KD_OPT_TEST_WAIT): when non-zero, one bounded device wait per
+  // sort pass or key-map call waits on a word that nothing publishes, with
+  // this many polls, so that the wait runs out and KD_ETIMEOUT comes back.
+  int wait_test = 0;
   cudaStream_t side = nullptr;  // second stream for the small-tile kernel
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   char last_error[256] = {0};  // fixed buffer: reporting an error never allocates

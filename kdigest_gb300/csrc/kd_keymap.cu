@@ -52,7 +52,8 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
 // is absent (lookup) or cannot be stored (the status word says why).
 __device__ unsigned probe(unsigned long long* __restrict__ tk, unsigned* __restrict__ ti,
                           unsigned long long* counter, long long size, long long capacity,
-                          unsigned long long k, bool insert, KdErrHost* err, long long i) {
+                          unsigned long long k, bool insert, KdErrHost* err, long long i,
+                          int spin_limit, bool stall) {
   unsigned long long h = mix64(k) & (unsigned long long)(size - 1);
   for (long long step = 0; step < size; ++step, h = (h + 1) & (unsigned long long)(size - 1)) {
     // A plain (L1-cached) read: a stale "empty" only sends the thread to the
@@ -69,6 +70,7 @@ __device__ unsigned probe(unsigned long long* __restrict__ tk, unsigned* __restr
           atomicExch(&ti[h], KD_KEYMAP_NOID - 1);  // published as "no id"
           return KD_KEYMAP_NOID;
         }
+        if (stall) return (unsigned)id;  // tests only: the id is never published
         __threadfence();
         atomicExch(&ti[h], (unsigned)id);
         return (unsigned)id;
@@ -81,7 +83,7 @@ __device__ unsigned probe(unsigned long long* __restrict__ tk, unsigned* __restr
         return KD_KEYMAP_NOID;
       }
       if (id0 != KD_KEYMAP_NOID) return id0;
-      for (int spin = 0; spin < KD_KEYMAP_SPIN_LIMIT; ++spin) {
+      for (int spin = 0; spin < spin_limit; ++spin) {
         const unsigned id = *(volatile unsigned*)&ti[h];
         if (id == KD_KEYMAP_NOID - 1) {  // stored when the map was already full
           if (insert && atomicCAS(&err->code, 0, KD_ENOMEM) == 0) err->index = i;
@@ -101,7 +103,8 @@ __device__ unsigned probe(unsigned long long* __restrict__ tk, unsigned* __restr
 __global__ void k_keymap(unsigned long long* tk, unsigned* ti, unsigned long long* counter,
                          long long size,
                          long long capacity, const unsigned long long* __restrict__ in, long long n,
-                         unsigned* __restrict__ out, int insert, KdErrHost* err) {
+                         unsigned* __restrict__ out, int insert, KdErrHost* err, int spin_limit,
+                         int stall_first) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const unsigned long long k = in[i];
@@ -110,7 +113,9 @@ __global__ void k_keymap(unsigned long long* tk, unsigned* ti, unsigned long lon
       out[i] = KD_KEYMAP_NOID;
       continue;
     }
-    out[i] = probe(tk, ti, counter, size, capacity, k, insert != 0, err, i);
+    // tests only: the key of input 0 is claimed without its id being published
+    out[i] = probe(tk, ti, counter, size, capacity, k, insert != 0, err, i, spin_limit,
+                   stall_first && k == in[0]);
   }
 }
 
@@ -141,8 +146,10 @@ int run(kd_keymap* m, const uint64_t* keys, int64_t n, uint32_t* ids, int flags,
   if (e == cudaSuccess) e = cudaMemcpyAsync(m->err, &init, sizeof init, cudaMemcpyHostToDevice, str);
   if (e == cudaSuccess) {
     const int grid = (int)std::min<long long>((n + 255) / 256, (long long)s->num_sms * 16);
+    const int spin_limit = s->wait_test > 0 ? s->wait_test : KD_KEYMAP_SPIN_LIMIT;
     k_keymap<<<grid, 256, 0, str>>>(m->keys, m->ids, m->counter, m->size, m->capacity, dk, n,
-                                    dout, insert ? 1 : 0, m->err);
+                                    dout, insert ? 1 : 0, m->err, spin_limit,
+                                    s->wait_test > 0 && insert ? 1 : 0);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(&got, m->err, sizeof got, cudaMemcpyDeviceToHost, str);

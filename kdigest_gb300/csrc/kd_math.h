@@ -59,8 +59,8 @@
 #define KD_SCALE_K2 2
 #define KD_SCALE_K3 3
 
-/* Tiles of at most this many elements sum their weights serially, left to
- * right; larger tiles use the 32-lane chunked order (one warp per tile). */
+/* Largest tile of the small-tile kernel (one warp per tile, one 32-lane
+ * chunk per 32 elements); larger tiles run on a block of warps. */
 #define KD_SERIAL_TILE_MAX 128
 
 /* Clamp distance from the q = 0 / 1 singularities (scale.mojo:32-47, Float64). */
@@ -177,12 +177,15 @@ KD_HD double kd_asin_series(double y) {
   return KD_FMA(KD_MUL(y, z), p, y);
 }
 
-/* asin(x); arguments outside [-1, 1] are clamped to the interval (the reference
- * would produce NaN there, which only rounding of cum/total above 1 can reach). */
+/* asin(x); NaN outside [-1, 1], as the C library's asin (which the reference's
+ * std.math asin is): rounding can put a prefix sum an ulp above its tile
+ * total, and K1 (which does not clamp q, scale.mojo:114-118) then evaluates
+ * asin slightly above 1.  The NaN reaches the int32 floor, which maps it to 0
+ * (kd_floor_i32), or fails the S-path's k-size test as in the reference. */
 KD_HD double kd_asin(double x) {
   if (kd_isnan(x)) return x;
   double ax = x < 0.0 ? -x : x;
-  if (ax > 1.0) ax = 1.0;
+  if (ax > 1.0) return kd_from_bits(0x7ff8000000000000ULL);
   double r;
   if (ax <= 0.5) {
     r = kd_asin_series(ax);
@@ -195,7 +198,10 @@ KD_HD double kd_asin(double x) {
 }
 
 /* floor(x) converted to int32 with saturation; NaN maps to 0.  This pins the
- * reference's Int32(floor(k)) (add_batch.mojo:110) for every double input. */
+ * reference's Int32(floor(k)) (add_batch.mojo:110) for every double input:
+ * the conversion of an out-of-range or NaN value is left undefined by the
+ * language, and these are the results of the conversion instruction of the
+ * reference's own platform (arm64 / Metal: saturating, NaN -> 0). */
 KD_HD int32_t kd_floor_i32(double x) {
   if (kd_isnan(x)) return 0;
   if (x >= 2147483647.0) return 2147483647;

@@ -107,7 +107,8 @@ size_t carve(uintptr_t base, KdWorkspace& w, KdStoreDev& d, double** stage) {
   w.tcount = c.take<int>(kInter);
   w.doff = c.take<int>(kInter + 1);
   w.needs = c.take<int>(4);
-  w.cap_fix = 2048;  // a fuller list falls back to the full sort
+  w.cap_fix = kN;  // every element fits the repair list (runs longer than
+                   // KD_PACK_RUN_MAX still take the full sort, as on the session path)
   w.fix = c.take<int>(w.cap_fix + 1);
   w.totals = c.take<int4>(8);
   w.d_call = c.take<KdCallArgs>(1);
@@ -235,6 +236,15 @@ KD_API int kd_compress_noalloc(int scale, double compression, const double* mean
     return say(msg, msg_cap, KD_ERANGE, buf);
   }
   if (n == 0) return KD_OK;
+  {
+    // Every call synchronises its stream and reads results back through
+    // pageable host memory, which a stream capture cannot hold: refuse before
+    // touching the stream, so that the caller's capture stays valid.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    KD_NA_CK(cudaStreamIsCapturing((cudaStream_t)stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+      return say(msg, msg_cap, KD_EINVAL, "kd_compress_noalloc cannot be captured in a CUDA graph");
+  }
   int dev = 0;
   KD_NA_CK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices)
@@ -278,6 +288,8 @@ KD_API int kd_compress_noalloc(int scale, double compression, const double* mean
   }
   rc = kd_pipeline_attempt(&s, &st, w, nullptr, dm, dw, n, KD_MODE_REPLACE, 0.0, nullptr, nullptr,
                            nullptr);
+  // Not expected for n <= KD_NOALLOC_MAX_N (no level's input exceeds the
+  // previous level's); reported rather than computed wrongly if it happened.
   if (rc == KD_ERANGE_SCRATCH_INTERNAL)
     return say(msg, msg_cap, KD_ENOMEM, "input needs more working memory than the fixed array holds");
   if (rc) return say(msg, msg_cap, rc, s.last_error);

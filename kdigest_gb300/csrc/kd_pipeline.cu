@@ -50,27 +50,43 @@ __device__ __forceinline__ int kd_err_get(const KdErrHost* e) {
 __device__ __forceinline__ double canon(double v) { return v == 0.0 ? 0.0 : v; }
 
 // ---------------------------------------------------------------------------
-// Warp tile compress (canonical association order; see oracle/kd_oracle.c)
+// Tile compress in the reference's association order
 // ---------------------------------------------------------------------------
-// Shared-memory staging of one tile for one warp.  CAP is the largest tile it
-// holds: KD_SERIAL_TILE_MAX (serial canonical order, one chunk) or KD_TILE
-// (32 lane chunks of E = ceil(n/32) elements).  Element p of the tile lives at
-// slot (p / E) * SE + p % E with SE = E | 1, which keeps the 64-bit accesses of
-// the 32 lanes on distinct banks.
+// The reference compresses a sorted tile of n <= 1024 pairs on 1024 lanes
+// (gpu/add_batch.mojo:45-222, gpu/grouped.mojo:128-276) and its sums have that
+// kernel's Hillis-Steele association:
+//   - cum[i]: the inclusive scan with offsets 1, 2, 4, ... (cum[i] += cum[i-off]);
+//   - the tile total: the scan's lane 1023, i.e. the balanced pairwise tree over
+//     [0, 2^ceil(log2 n)) (the lanes past n add exact zeros);
+//   - a segment's (sum w, sum w*x) at its end element e: the segmented scan,
+//     which is the right-aligned pairwise tree over [head, e] (level-1 pairs
+//     (e, e-1), (e-2, e-3), ...; a node without partner carried up).
+// The kernels compute exactly these values: the prefix by the scan itself
+// (integral weights: any exact order), the total from the window sums the
+// scan passes through, and the segment sums by an up-sweep of that tree,
+// e - head additions per segment.
+//
+// Shared-memory staging of one tile.  CAP is the largest tile it holds:
+// KD_SERIAL_TILE_MAX (the small-tile kernel, a warp per tile) or KD_TILE (a
+// block per tile).  Element p of the tile lives at slot (p / E) * SE + p % E,
+// E = ceil(n / 32), SE = E | 1: the block loader writes 32 contiguous ranges
+// at once, and the odd stride keeps them on distinct banks.  With CAP =
+// KD_SERIAL_TILE_MAX the tile is one chunk (slot p = p).
 template <int CAP>
 struct WarpTileT {
   static constexpr int SLOTS = CAP == KD_TILE ? KD_SMEM_SLOTS : CAP + 1;
   double x[SLOTS];
-  double w[SLOTS];
-  // in-chunk inclusive prefix of w (double, or int64 bits in the integral path);
-  // after the segment pass: the weight sum of each segment at its end element
+  double w[SLOTS];  // weights; after the segment pass: sum(w * x) at each segment end
+  // inclusive prefix of w (double, or int64 bits in the integral path); after
+  // the segment pass: the weight sum of each segment at its end element
   double L[SLOTS];
-  double P[32];                  // exclusive prefix of the chunk totals (bits)
-  // hf/ef also hold a list of up to CAP tile positions (unsigned short) while
-  // they are free: the elements left to the FP64 bucket path, then the
-  // segments whose mean needs a division.
-  unsigned char hf[SLOTS];       // head flags
-  unsigned char ef[SLOTS];       // end flags
+  double P[32];                  // scratch: head ballots per round of 32 (unsigned)
+  // hf/ef hold a list of up to CAP tile positions (unsigned short) while they
+  // are free: the elements left to the FP64 bucket path, the segment end of
+  // every position during the segment pass, then the segments whose mean
+  // needs a division.
+  unsigned char hf[SLOTS];
+  unsigned char ef[SLOTS];
   // headpos/endpos also hold the bucket id (int) of every element until the
   // head pass, which writes headpos[k] only after id k has been read.
   alignas(8) unsigned short headpos[CAP];  // tile position of the first element of segment s
@@ -78,6 +94,7 @@ struct WarpTileT {
 
   __device__ unsigned short* poslist() { return reinterpret_cast<unsigned short*>(hf); }
   __device__ int* ids() { return reinterpret_cast<int*>(headpos); }
+  __device__ unsigned* hbw() { return reinterpret_cast<unsigned*>(P); }
 };
 typedef WarpTileT<KD_TILE> WarpTile;
 typedef WarpTileT<KD_SERIAL_TILE_MAX> WarpTileSmall;
@@ -98,8 +115,8 @@ static_assert(offsetof(WarpTile, endpos) == offsetof(WarpTile, headpos) + 2 * KD
               "bucket ids overlay headpos/endpos");
 
 // Integral weight in [1, 2^42): a tile of such weights has every partial sum
-// exact in FP64 (total < 2^52), so int64 arithmetic reproduces the canonical
-// FP64 sums bit for bit.
+// exact in FP64 (total < 2^52), so int64 arithmetic in any order reproduces
+// the reference's FP64 sums bit for bit.
 __device__ __forceinline__ bool kd_is_small_int(double w) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(w);
   if (b >> 63) return false;
@@ -125,7 +142,6 @@ struct TileAcc<false> {
   __device__ static T shfl(T v, int l) { return __shfl_sync(0xffffffffu, v, l); }
   __device__ static double to_d(T v) { return v; }
   __device__ static float to_f(T v) { return kd_d2f_trunc(v); }
-  __device__ static bool is_zero(T v) { return ((unsigned long long)__double_as_longlong(v) << 1) == 0; }
   // exact comparisons (positive finite operands): a == b, and 2a == b (doubling is exact)
   __device__ static bool eq(T a, T b) { return __double_as_longlong(a) == __double_as_longlong(b); }
   __device__ static bool is_half(T a, T b) { return __double_as_longlong(KD_ADD(a, a)) == __double_as_longlong(b); }
@@ -142,7 +158,6 @@ struct TileAcc<true> {
   __device__ static T shfl(T v, int l) { return __shfl_sync(0xffffffffu, v, l); }
   __device__ static double to_d(T v) { return (double)v; }
   __device__ static float to_f(T v) { return kd_i2f_trunc(v); }
-  __device__ static bool is_zero(T v) { return v == 0; }
   __device__ static bool eq(T a, T b) { return a == b; }
   __device__ static bool is_half(T a, T b) { return a + a == b; }
   __device__ static double store(T v) { return __longlong_as_double(v); }
@@ -153,43 +168,138 @@ __device__ __forceinline__ int tile_slot(int p, int E, int SE, unsigned inv) {
   const int c = (int)(((unsigned)p * inv) >> 16);  // exact p / E for p < 1024, E <= 1024
   return c * SE + (p - c * E);
 }
-// Chunk length of a tile: the whole tile (serial order) up to
-// KD_SERIAL_TILE_MAX elements, else ceil(n / 32).
+// Chunk length of a tile: the whole tile up to KD_SERIAL_TILE_MAX elements,
+// else ceil(n / 32).
 __device__ __forceinline__ int tile_chunk(int n) {
   return n <= KD_SERIAL_TILE_MAX ? n : (n + 31) >> 5;
 }
 __device__ __forceinline__ unsigned tile_inv(int E) {
   return (65536u + (unsigned)E - 1u) / (unsigned)E;
 }
+struct SlotMap {
+  int E, SE;
+  unsigned inv;
+  __device__ explicit SlotMap(int n) : E(tile_chunk(n)), SE(tile_chunk(n) | 1), inv(tile_inv(tile_chunk(n))) {}
+  __device__ int operator()(int p) const { return tile_slot(p, E, SE, inv); }
+};
+struct FlatMap {
+  __device__ int operator()(int p) const { return p; }
+};
 
-// Compresses the n staged elements of `t` (the loader has filled x and w in
-// the slot layout of tile_chunk(n)).  Writes the centroids to om/ow[0..) and
-// returns their number.  Canonical sums: serial within each chunk, Kogge-Stone
-// over the 32 chunk totals for the prefix; for segment sums, serial within a
-// chunk and a segmented Kogge-Stone carry across chunks.  With one chunk
-// (n <= KD_SERIAL_TILE_MAX) both reduce to plain serial sums.
-template <bool kInt, int CAP>
-__device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compression,
+// The tile total in the reference's association from one window sum per set
+// bit of n: bit k of n is the aligned block [s, s + 2^k), s = n with bits <= k
+// cleared, and the balanced tree over [0, 2^ceil(log2 n)) is
+// block(top bit) + (... + (block(next) + block(lowest bit))).
+struct TotalAcc {
+  double v = 0.0;
+  bool have = false;
+  __device__ void push(double b) {
+    v = have ? KD_ADD(b, v) : b;
+    have = true;
+  }
+};
+__device__ __forceinline__ int block_end(int n, int k) {  // last position of bit k's block
+  return (n & ~((2 << k) - 1)) + (1 << k) - 1;
+}
+
+// 2^b * w, exact (w positive and finite; integer exponent arithmetic while the
+// result stays normal, which keeps the FP64 pipe free).
+__device__ __forceinline__ double kd_scale2(double w, int b) {
+  const long long bits = __double_as_longlong(w);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  if (e >= 1 && e + b <= 2046) return __longlong_as_double(bits + ((long long)b << 52));
+  return KD_MUL(w, kd_pow2i(b));
+}
+// Tiles whose weights are all equal (a batch's new samples at one decay
+// factor): every window sum of the reference's scan is a power-of-two multiple
+// of w, exact, so the scan value at j is w, plus 2^b * w for each set bit b of j
+// in increasing order (P(j) = 2^m w + P(j - 2^m), m the top bit of j).  The
+// same value is a segment's sum of j + 1 equal weights.
+__device__ __forceinline__ double hs_uniform(double w, int j) {
+  double acc = w;
+  while (j) {
+    acc = KD_ADD(kd_scale2(w, __ffs(j) - 1), acc);
+    j &= j - 1;
+  }
+  return acc;
+}
+// The same value for j = 32 a + l from lo = hs_uniform(w, l): the bits of l
+// come first in the fold, so only the set bits of a (>= 5) remain, the same
+// for every lane of a round of 32.
+__device__ __forceinline__ double hs_uniform_hi(double w, double lo, int a) {
+  double acc = lo;
+  while (a) {
+    acc = KD_ADD(kd_scale2(w, __ffs(a) + 4), acc);
+    a &= a - 1;
+  }
+  return acc;
+}
+__device__ __forceinline__ double hs_uniform_total(double w, int n) {
+  TotalAcc tot;
+  for (int k = 0; (n >> k) != 0; ++k)
+    if ((n >> k) & 1) tot.push(kd_scale2(w, k));
+  return tot.v;
+}
+
+// Segment end of position p from the head ballots of its rounds of 32: the
+// position before the next head (or n - 1).  nz has bit r set when round r
+// holds a head.
+__device__ __forceinline__ int seg_end(const unsigned* hb, unsigned nz, int p, int n) {
+  const int r = p >> 5, l = p & 31;
+  const unsigned above = hb[r] & ~((2u << l) - 1u);
+  if (above) return (r << 5) + __ffs(above) - 2;
+  const unsigned rr = r >= 31 ? 0u : nz & ~((2u << r) - 1u);
+  if (!rr) return n - 1;
+  const int r2 = __ffs(rr) - 1;
+  return (r2 << 5) + __ffs(hb[r2]) - 2;
+}
+
+// In-place Hillis-Steele scan of v[slot(0 .. n)) by one warp: rounds of
+// offsets 1, 2, 4, ... < n; each round sweeps the 32-element blocks from the
+// top, so that every read sees the value of the previous round.  Returns the
+// tile total (TotalAcc over the window sums the rounds pass through).
+template <class Slot>
+__device__ double hs_scan_warp(double* v, int n, Slot slot) {
+  const int lane = threadIdx.x & 31;
+  TotalAcc tot;
+  if (n & 1) tot.push(v[slot(n - 1)]);
+  int k = 1;
+  for (int d = 1; d < n; d <<= 1, ++k) {
+    for (int r0 = (n - 1) & ~31; r0 >= 0; r0 -= 32) {
+      const int p = r0 + lane;
+      const bool act = p < n && p >= d;
+      double a = 0.0, b = 0.0;
+      if (act) {
+        a = v[slot(p)];
+        b = v[slot(p - d)];
+      }
+      __syncwarp();
+      if (act) v[slot(p)] = KD_ADD(a, b);
+      __syncwarp();
+    }
+    if ((n >> k) & 1) tot.push(v[slot(block_end(n, k))]);  // window of 2^k complete
+  }
+  return tot.v;
+}
+
+// Compresses the n <= KD_SERIAL_TILE_MAX staged elements of `t` (slot p = p)
+// with one warp.  Writes the centroids to om/ow[0..) and returns their number.
+template <bool kInt>
+__device__ int warp_compress(WarpTileSmall& t, int n, int scale, double compression,
                              int force_exact, int32_t id_last, double* __restrict__ om,
                              double* __restrict__ ow) {
   typedef TileAcc<kInt> A;
   typedef typename A::T T;
   const int lane = threadIdx.x & 31;
-  const int E = tile_chunk(n);
-  const int SE = E | 1;
-  const unsigned inv = tile_inv(E);
-  const int lo = lane * E;
-  const int cnt = max(0, min(E, n - lo));
-  const int sb = lane * SE;
+  const unsigned lt_mask = (1u << lane) - 1u;
 
-  // 1. In-chunk inclusive prefix of the weights, serial per lane.  A one-chunk
-  //    tile with integral weights (exact int64 sums, any order gives the same
-  //    values) is scanned by the whole warp, 32 elements per round.
-  T acc = 0;
-  if (kInt && CAP <= KD_SERIAL_TILE_MAX) {
+  // 1-2. Inclusive prefix of the weights in L and the tile total.
+  T tot;
+  bool uniform = false;  // non-integral tile with all weights equal
+  if (kInt) {  // exact int64 sums: a warp scan, 32 elements per round
     T carry = 0;
     for (int r0 = 0; r0 < n; r0 += 32) {
-      const int p = r0 + lane;  // one chunk: slot p holds element p
+      const int p = r0 + lane;
       T v = p < n ? A::from_w(t.w[p]) : (T)0;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -200,28 +310,22 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
       if (p < n) t.L[p] = A::store(v);
       carry = A::shfl(v, 31);
     }
-    acc = carry;  // lane 0 owns the single chunk: its total
+    tot = carry;
   } else {
-    for (int j = 0; j < cnt; ++j) {
-      const T wv = A::from_w(t.w[sb + j]);
-      acc = j == 0 ? wv : A::add(acc, wv);
-      t.L[sb + j] = A::store(acc);
+    const double w0 = t.w[0];
+    bool same = true;
+    for (int p = lane; p < n; p += 32) same = same && __double_as_longlong(t.w[p]) == __double_as_longlong(w0);
+    uniform = __all_sync(0xffffffffu, same);
+    if (uniform) {
+      const double lo = hs_uniform(w0, lane);
+      for (int p = lane; p < n; p += 32) t.L[p] = hs_uniform_hi(w0, lo, p >> 5);
+      tot = A::load(hs_uniform_total(w0, n));
+    } else {
+      for (int p = lane; p < n; p += 32) t.L[p] = t.w[p];
+      __syncwarp();
+      tot = A::load(hs_scan_warp(t.L, n, FlatMap()));
     }
   }
-  // 2. Chunk totals -> Kogge-Stone over lanes -> exclusive chunk prefix.
-  T I = cnt > 0 ? acc : (T)0;
-  if (CAP > KD_SERIAL_TILE_MAX) {
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const T v = A::shfl_up(I, o);
-      if (lane >= o) I = A::add(I, v);
-    }
-    t.P[lane] = A::store(A::shfl_up(I, 1));
-  }
-  const int cl = (n - 1) / E;  // chunk holding the last element
-  T last_cum = 0;
-  if (cnt > 0) last_cum = lane == 0 ? acc : A::add(A::load(t.P[lane]), acc);
-  T tot = A::shfl(last_cum, cl);
   double totd = A::to_d(tot);
   if (!(totd > 0.0)) {  // add_batch.mojo:98-100 (only reachable with non-integral weights)
     totd = 1.0;
@@ -232,21 +336,17 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
 
   // 3a. Bucket ids of all elements in independent rounds.  Exact shortcuts
   //     first: q == 1/2 gives k == 0 exactly for K1..K3 (asin(0), log(1)), and
-  //     the last element of a K0/K1 tile (q == 1) has the launch constant
-  //     id_last.  Then the FP32 filter; positions it cannot resolve go to a
-  //     list for the FP64 path.
+  //     an element with cum == total of a K0/K1 tile (q == 1) has the launch
+  //     constant id_last.  Then the FP32 filter; positions it cannot resolve
+  //     go to a list for the FP64 path.
   int* const ids = t.ids();
   unsigned short* const plist = t.poslist();
-  const unsigned lt_mask = (1u << lane) - 1u;
   int nneed = 0;
   for (int r0 = 0; r0 < n; r0 += 32) {
     const int p = r0 + lane;
     bool need = false;
     if (p < n) {
-      const int c = (int)(((unsigned)p * inv) >> 16);
-      const int slot = c * SE + (p - c * E);
-      const T Lp = A::load(t.L[slot]);
-      const T cum = c == 0 ? Lp : A::add(A::load(t.P[c]), Lp);
+      const T cum = A::load(t.L[p]);
       int32_t id = 0;
       bool ok = false;
       if (!force_exact) {
@@ -275,18 +375,17 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
     const double nrm64 = kd_normalizer(scale, compression, totd);
     for (int k = lane; k < nneed; k += 32) {
       const int p = plist[k];
-      const int c = (int)(((unsigned)p * inv) >> 16);
-      const int slot = c * SE + (p - c * E);
-      const T Lp = A::load(t.L[slot]);
-      const T cum = c == 0 ? Lp : A::add(A::load(t.P[c]), Lp);
-      ids[p] = kd_bucket(scale, A::to_d(cum), totd, nrm64);
+      ids[p] = kd_bucket(scale, A::to_d(A::load(t.L[p])), totd, nrm64);
     }
   }
   __syncwarp();
-  // 3c. Heads (an id change or the first element), compacted by ballot.  Writing
-  //     headpos[k] (k <= p) only clobbers ids of elements already read.
+  // 3c. Heads (an id change or the first element), compacted by ballot, and
+  //     the head ballot of every round.  Writing headpos[k] (k <= p) only
+  //     clobbers ids of elements already read.
+  unsigned* const hb = t.hbw();
   int32_t carry_id = 0;
   int nheads = 0;
+  unsigned nz = 0;
   for (int r0 = 0; r0 < n; r0 += 32) {
     const int p = r0 + lane;
     const bool act = p < n;
@@ -294,110 +393,74 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
     int32_t prev = __shfl_up_sync(0xffffffffu, id, 1);
     if (lane == 0) prev = carry_id;
     const bool head = act && (p == 0 || id != prev);
-    const unsigned hb = __ballot_sync(0xffffffffu, head);
+    const unsigned hbits = __ballot_sync(0xffffffffu, head);
     carry_id = __shfl_sync(0xffffffffu, id, 31);
     __syncwarp();
-    if (head) t.headpos[nheads + __popc(hb & lt_mask)] = (unsigned short)p;
-    nheads += __popc(hb);
+    if (head) t.headpos[nheads + __popc(hbits & lt_mask)] = (unsigned short)p;
+    if (lane == 0) hb[r0 >> 5] = hbits;
+    if (hbits) nz |= 1u << (r0 >> 5);
+    nheads += __popc(hbits);
   }
   __syncwarp();
   const int total_out = nheads;
 
-  // 4. Segment sums; every segment parks its sums at its end element
-  //    (L: weight, w: weight * value) and records its end position.
-  if (CAP <= KD_SERIAL_TILE_MAX || n <= KD_SERIAL_TILE_MAX) {
-    // One chunk: plain serial sums, one lane per segment.
+  // 4. Segment sums, parked at each segment's end element (L: weight, w:
+  //    weight * value).  sum(w): with integral weights every order is exact
+  //    (int64, summed below); other weights take the up-sweep of each
+  //    segment's right-aligned tree, the reference's association: in round r
+  //    a position at distance u = e - p from its segment end, u a multiple of
+  //    2^(r+1), adds the node 2^r below it when that lies in the same segment
+  //    (nodes read in a round are never written in it).  sum(w * x): serial,
+  //    one lane per segment; the reference's tree differs from it by rounding
+  //    only, which reaches no bucket id (means are not summed into any prefix).
+  if (!kInt && uniform) {
+    const double w0 = t.w[0];
     for (int sI = lane; sI < total_out; sI += 32) {
-      const int h = t.headpos[sI];
       const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
-      t.endpos[sI] = (unsigned short)e;
-      if (h == e) {  // a single element: its weight; its mean is its value
-        t.L[e] = A::store(A::from_w(t.w[e]));
-        continue;
-      }
-      T aw = A::from_w(t.w[h]);
-      double awx = KD_MUL(t.w[h], t.x[h]);
-      for (int i = h + 1; i <= e; ++i) {
-        const double wi = t.w[i];
-        aw = A::add(aw, A::from_w(wi));
-        awx = KD_ADD(awx, KD_MUL(wi, t.x[i]));
-      }
-      t.L[e] = A::store(aw);
-      t.w[e] = awx;
+      t.L[e] = hs_uniform(w0, e - (int)t.headpos[sI]);
     }
-  } else {
-    // Lane chunks: flags from the head list, serial pieces per chunk, then a
-    // segmented Kogge-Stone carry of the trailing pieces across lanes.
-    for (int q = lane; q < n; q += 32) {
-      const int sl = tile_slot(q, E, SE, inv);
-      t.hf[sl] = 0;
-      t.ef[sl] = 0;
+  } else if (!kInt) {
+    unsigned short* const send = t.poslist();  // segment end of every position
+    for (int p = lane; p < n; p += 32) {
+      send[p] = (unsigned short)seg_end(hb, nz, p, n);
+      t.L[p] = t.w[p];
     }
-    __syncwarp();
+    int ml = 1;
     for (int sI = lane; sI < total_out; sI += 32) {
-      const int h = t.headpos[sI];
-      t.hf[tile_slot(h, E, SE, inv)] = 1;
       const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
-      t.ef[tile_slot(e, E, SE, inv)] = 1;
-      t.endpos[sI] = (unsigned short)e;
+      ml = max(ml, e - (int)t.headpos[sI] + 1);
     }
-    __syncwarp();
-    // output slot of a segment = number of heads before it; a lane's first end
-    // closes the segment of the last head at or before the chunk start
-    T aw = 0;
-    double awx = 0.0;
-    bool head_seen = false;
-    bool pend = false;
-    T pend_w = 0;
-    double pend_wx = 0.0;
-    int pend_se = 0;
-    for (int j = 0; j < cnt; ++j) {
-      const double wi = t.w[sb + j], xi = t.x[sb + j];
-      const double wx = KD_MUL(wi, xi);
-      const T wv = A::from_w(wi);
-      const bool hd = t.hf[sb + j];
-      if (hd || j == 0) {
-        aw = wv;
-        awx = wx;
-      } else {
-        aw = A::add(aw, wv);
-        awx = KD_ADD(awx, wx);
-      }
-      if (hd) head_seen = true;
-      if (t.ef[sb + j]) {
-        if (head_seen) {
-          t.L[sb + j] = A::store(aw);
-          t.w[sb + j] = awx;
-        } else {
-          pend = true;
-          pend_w = aw;
-          pend_wx = awx;
-          pend_se = sb + j;
-        }
-      }
-    }
-    T Vw = aw;
-    double Vwx = awx;
-    int F = head_seen ? 1 : 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const T tw = A::shfl_up(Vw, o);
-      const double twx = shfl_up_d(Vwx, o);
-      const int tf = __shfl_up_sync(0xffffffffu, F, o);
-      if (lane >= o) {
-        if (!F) {
-          Vw = A::add(Vw, tw);
-          Vwx = KD_ADD(Vwx, twx);
-        }
-        F |= tf;
+    for (int o = 16; o > 0; o >>= 1) ml = max(ml, __shfl_xor_sync(0xffffffffu, ml, o));
+    __syncwarp();
+    for (int r = 0; (1 << r) < ml; ++r) {
+      const int step = 1 << r;
+      const unsigned mask = (2u << r) - 1u;
+      for (int p = lane; p < n; p += 32) {
+        const int e = send[p];
+        if (((unsigned)(e - p) & mask) == 0 && p >= step && send[p - step] == e)
+          t.L[p] = KD_ADD(t.L[p], t.L[p - step]);
       }
+      __syncwarp();
     }
-    const T cw = A::shfl_up(Vw, 1);
-    const double cwx = shfl_up_d(Vwx, 1);
-    if (pend) {
-      t.L[pend_se] = A::store(A::add(cw, pend_w));
-      t.w[pend_se] = KD_ADD(cwx, pend_wx);
+  }
+  for (int sI = lane; sI < total_out; sI += 32) {
+    const int h = t.headpos[sI];
+    const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
+    t.endpos[sI] = (unsigned short)e;
+    if (h == e) {  // a single element: its weight; its mean is its value
+      if (kInt) t.L[e] = A::store(A::from_w(t.w[e]));
+      continue;
     }
+    T aw = A::from_w(t.w[h]);
+    double awx = KD_MUL(t.w[h], t.x[h]);
+    for (int i = h + 1; i <= e; ++i) {
+      const double wi = t.w[i];
+      if (kInt) aw = A::add(aw, A::from_w(wi));
+      awx = KD_ADD(awx, KD_MUL(wi, t.x[i]));
+    }
+    if (kInt) t.L[e] = A::store(aw);
+    t.w[e] = awx;
   }
   __syncwarp();
 
@@ -413,9 +476,8 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
     if (sI < total_out) {
       const int e = t.endpos[sI];
       const int h = t.headpos[sI];
-      const int se = tile_slot(e, E, SE, inv), sh = tile_slot(h, E, SE, inv);
-      const double sw = A::to_d(A::load(t.L[se]));
-      const double lo_v = t.x[sh], hi_v = t.x[se];
+      const double sw = A::to_d(A::load(t.L[e]));
+      const double lo_v = t.x[h], hi_v = t.x[e];
       ow[sI] = sw;
       if (__double_as_longlong(lo_v) == __double_as_longlong(hi_v)) {
         om[sI] = lo_v;
@@ -427,6 +489,7 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
       }
     }
     const unsigned db = __ballot_sync(0xffffffffu, div);
+    __syncwarp();  // every lane read its position before the list overwrites them
     if (div) dlist[ndiv + __popc(db & lt_mask)] = (unsigned short)sI;
     ndiv += __popc(db);
   }
@@ -435,10 +498,9 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
     const int sI = dlist[k];
     const int e = t.endpos[sI];
     const int h = t.headpos[sI];
-    const int se = tile_slot(e, E, SE, inv), sh = tile_slot(h, E, SE, inv);
-    const double sw = A::to_d(A::load(t.L[se]));
-    const double lo_v = t.x[sh], hi_v = t.x[se];
-    double mean = KD_DIV(t.w[se], sw);
+    const double sw = A::to_d(A::load(t.L[e]));
+    const double lo_v = t.x[h], hi_v = t.x[e];
+    double mean = KD_DIV(t.w[e], sw);
     const uint64_t km = kd_order_key(mean);
     if (km < kd_order_key(lo_v)) mean = lo_v;
     else if (km > kd_order_key(hi_v)) mean = hi_v;
@@ -450,17 +512,17 @@ __device__ int warp_compress(WarpTileT<CAP>& t, int n, int scale, double compres
 
 // ---------------------------------------------------------------------------
 // Block-cooperative compress of one tile above the small-tile cap: the same
-// canonical order as warp_compress (the chunk-serial prefix and segment sums
-// stay on warp 0), with the element-parallel stages - bucket ids, the FP64
-// fallback list, head detection and the mean divisions - spread over the
-// block's KD_TILE_WARPS warps.  Results are identical to warp_compress.
+// values as warp_compress, every stage spread over the block's KD_TILE_WARPS
+// warps (the tile in the chunk slot layout).
 // ---------------------------------------------------------------------------
 #define KD_TILE_WARPS 4
 struct BlockScr {
   double totb;          // tile total (int64 bits in the integral path)
   double totd;
   KFilterTile ft;
-  int nneed, ndiv, nout, stop;
+  int nneed, ndiv, nout, stop, maxlen;
+  unsigned nz;          // rounds of 32 that hold a head
+  long long wsum[KD_TILE_WARPS];
   int rc[32];           // heads per round of 32 elements (then their offsets)
   unsigned hb[32];      // head ballot per round
 };
@@ -472,46 +534,96 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
   typedef TileAcc<kInt> A;
   typedef typename A::T T;
   constexpr int NT = KD_TILE_WARPS * 32;
+  constexpr int PER = KD_TILE / NT;  // positions per thread
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int E = tile_chunk(n);
-  const int SE = E | 1;
-  const unsigned inv = tile_inv(E);
+  const SlotMap slot(n);
   const unsigned lt_mask = (1u << lane) - 1u;
+  const int rounds = (n + 31) >> 5;
+  bool uniform = false;  // non-integral tile with all weights equal
 
-  // 1-2. In-chunk prefix (serial per lane) and Kogge-Stone over chunk totals.
-  if (warp == 0) {
-    const int lo = lane * E;
-    const int cnt = max(0, min(E, n - lo));
-    const int sb = lane * SE;
-    T acc = 0;
-    for (int j = 0; j < cnt; ++j) {
-      const T wv = A::from_w(t.w[sb + j]);
-      acc = j == 0 ? wv : A::add(acc, wv);
-      t.L[sb + j] = A::store(acc);
-    }
-    T I = cnt > 0 ? acc : (T)0;
+  // 1-2. Inclusive prefix of the weights in L and the tile total.
+  if (kInt) {
+    // exact int64 sums: each warp scans a contiguous range of rounds, then
+    // adds the totals of the warps before it
+    const int per = (rounds + KD_TILE_WARPS - 1) / KD_TILE_WARPS;
+    const int rb = warp * per, re = min(rounds, rb + per);
+    T carry = 0;
+    for (int r = rb; r < re; ++r) {
+      const int p = r * 32 + lane;
+      T v = p < n ? A::from_w(t.w[slot(p)]) : (T)0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const T v = A::shfl_up(I, o);
-      if (lane >= o) I = A::add(I, v);
+      for (int o = 1; o < 32; o <<= 1) {
+        const T u = A::shfl_up(v, o);
+        if (lane >= o) v = A::add(v, u);
+      }
+      v = A::add(v, carry);
+      if (p < n) t.L[slot(p)] = A::store(v);
+      carry = A::shfl(v, 31);
     }
-    t.P[lane] = A::store(A::shfl_up(I, 1));
-    const int cl = (n - 1) / E;
-    T last_cum = 0;
-    if (cnt > 0) last_cum = lane == 0 ? acc : A::add(A::load(t.P[lane]), acc);
-    T tot = A::shfl(last_cum, cl);
+    if (lane == 0) bs.wsum[warp] = (long long)carry;
+    __syncthreads();
+    T off = 0, all = 0;
+#pragma unroll
+    for (int w2 = 0; w2 < KD_TILE_WARPS; ++w2) {
+      const T s2 = (T)bs.wsum[w2];
+      if (w2 < warp) off = A::add(off, s2);
+      all = A::add(all, s2);
+    }
+    if (off != 0)
+      for (int r = rb; r < re; ++r) {
+        const int p = r * 32 + lane;
+        if (p < n) t.L[slot(p)] = A::store(A::add(A::load(t.L[slot(p)]), off));
+      }
+    if (tid == 0) bs.totb = A::store(all);
+  } else {
+    const double w0 = t.w[slot(0)];
+    bool same = true;
+    for (int p = tid; p < n; p += NT) same = same && __double_as_longlong(t.w[slot(p)]) == __double_as_longlong(w0);
+    uniform = __syncthreads_and(same);
+  }
+  if (!kInt && uniform) {
+    const double w0 = t.w[slot(0)];
+    const double lo = hs_uniform(w0, lane);  // p & 31 == lane for p = tid + k * NT
+    for (int p = tid; p < n; p += NT) t.L[slot(p)] = hs_uniform_hi(w0, lo, p >> 5);
+    if (tid == 0) bs.totb = hs_uniform_total(w0, n);
+  } else if (!kInt) {
+    // the Hillis-Steele rounds, staged through registers: all reads of a
+    // round complete before its writes
+    for (int p = tid; p < n; p += NT) t.L[slot(p)] = t.w[slot(p)];
+    TotalAcc tot;
+    if (tid == 0 && (n & 1)) tot.push(t.w[slot(n - 1)]);
+    __syncthreads();
+    int k = 1;
+    for (int d = 1; d < n; d <<= 1, ++k) {
+      double nv[PER];
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const int p = tid + i * NT;
+        nv[i] = (p < n && p >= d) ? KD_ADD(t.L[slot(p)], t.L[slot(p - d)]) : 0.0;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const int p = tid + i * NT;
+        if (p < n && p >= d) t.L[slot(p)] = nv[i];
+      }
+      __syncthreads();
+      if (tid == 0 && ((n >> k) & 1)) tot.push(t.L[slot(block_end(n, k))]);
+    }
+    if (tid == 0) bs.totb = tot.v;
+  }
+  if (tid == 0) {
+    T tot = A::load(bs.totb);
     double totd = A::to_d(tot);
     if (!(totd > 0.0)) {  // add_batch.mojo:98-100
       totd = 1.0;
       tot = (T)1;
     }
-    if (lane == 0) {
-      bs.totb = A::store(tot);
-      bs.totd = totd;
-      bs.ft = kfilter_tile(scale, compression, kInt ? A::to_f(tot) : kd_d2f_trunc(totd));
-      bs.nneed = 0;
-      bs.ndiv = 0;
-    }
+    bs.totb = A::store(tot);
+    bs.totd = totd;
+    bs.ft = kfilter_tile(scale, compression, kInt ? A::to_f(tot) : kd_d2f_trunc(totd));
+    bs.nneed = 0;
+    bs.ndiv = 0;
   }
   __syncthreads();
   const T tot = A::load(bs.totb);
@@ -525,10 +637,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
     const int p = r0 + lane;
     bool need = false;
     if (p < n) {
-      const int c = (int)(((unsigned)p * inv) >> 16);
-      const int slot = c * SE + (p - c * E);
-      const T Lp = A::load(t.L[slot]);
-      const T cum = c == 0 ? Lp : A::add(A::load(t.P[c]), Lp);
+      const T cum = A::load(t.L[slot(p)]);
       int32_t id = 0;
       bool ok = false;
       if (!force_exact) {
@@ -562,26 +671,21 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
     const double nrm64 = kd_normalizer(scale, compression, totd);
     for (int k = tid; k < nneed; k += NT) {
       const int p = plist[k];
-      const int c = (int)(((unsigned)p * inv) >> 16);
-      const int slot = c * SE + (p - c * E);
-      const T Lp = A::load(t.L[slot]);
-      const T cum = c == 0 ? Lp : A::add(A::load(t.P[c]), Lp);
-      ids[p] = kd_bucket(scale, A::to_d(cum), totd, nrm64);
+      ids[p] = kd_bucket(scale, A::to_d(A::load(t.L[slot(p)])), totd, nrm64);
     }
   }
   __syncthreads();
   // 3c. Heads: flags per round, offsets by a scan over the rounds, then the
   //     positions (the ids are all read before any position is written).
-  const int rounds = (n + 31) >> 5;
   for (int r = warp; r < rounds; r += KD_TILE_WARPS) {
     const int p = r * 32 + lane;
     const bool act = p < n;
     const int32_t id = act ? ids[p] : 0;
     const int32_t prev = (act && p > 0) ? ids[p - 1] : 0;
-    const unsigned hb = __ballot_sync(0xffffffffu, act && (p == 0 || id != prev));
+    const unsigned hbits = __ballot_sync(0xffffffffu, act && (p == 0 || id != prev));
     if (lane == 0) {
-      bs.hb[r] = hb;
-      bs.rc[r] = __popc(hb);
+      bs.hb[r] = hbits;
+      bs.rc[r] = __popc(hbits);
     }
   }
   __syncthreads();
@@ -594,48 +698,94 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
       if (lane >= o) incl += u;
     }
     bs.rc[lane] = incl - v;
+    const unsigned nz = __ballot_sync(0xffffffffu, lane < rounds && bs.hb[lane] != 0u);
     if (lane == 31) bs.nout = incl;
+    if (lane == 0) {
+      bs.nz = nz;
+      bs.maxlen = 1;
+    }
   }
   __syncthreads();
   for (int r = warp; r < rounds; r += KD_TILE_WARPS) {
-    const unsigned hb = bs.hb[r];
-    if ((hb >> lane) & 1u) t.headpos[bs.rc[r] + __popc(hb & lt_mask)] = (unsigned short)(r * 32 + lane);
+    const unsigned hbits = bs.hb[r];
+    if ((hbits >> lane) & 1u) t.headpos[bs.rc[r] + __popc(hbits & lt_mask)] = (unsigned short)(r * 32 + lane);
   }
   __syncthreads();
   const int total_out = bs.nout;
 
-  // 4. Segment sums, parked at each segment's end element.
+  // 4. Segment sums, parked at each segment's end element, with the
+  //    association of warp_compress: sum(w) exact (integral weights) or by the
+  //    up-sweep of the reference's tree, block-wide; sum(w * x) serial per
+  //    lane chunk, carried across chunks by a segmented Kogge-Stone scan
+  //    (one chunk, n <= KD_SERIAL_TILE_MAX: serial per segment).
+  if (!kInt && uniform) {
+    const double w0 = t.w[slot(0)];
+    for (int sI = tid; sI < total_out; sI += NT) {
+      const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
+      t.L[slot(e)] = hs_uniform(w0, e - (int)t.headpos[sI]);
+    }
+  } else if (!kInt) {
+    unsigned short* const send = t.poslist();
+    const unsigned nz = bs.nz;
+    for (int p = tid; p < n; p += NT) {
+      send[p] = (unsigned short)seg_end(bs.hb, nz, p, n);
+      t.L[slot(p)] = t.w[slot(p)];
+    }
+    int ml = 1;
+    for (int sI = tid; sI < total_out; sI += NT) {
+      const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
+      ml = max(ml, e - (int)t.headpos[sI] + 1);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ml = max(ml, __shfl_xor_sync(0xffffffffu, ml, o));
+    if (lane == 0 && ml > 1) atomicMax(&bs.maxlen, ml);
+    __syncthreads();
+    const int maxlen = bs.maxlen;
+    for (int r = 0; (1 << r) < maxlen; ++r) {
+      const int step = 1 << r;
+      const unsigned mask = (2u << r) - 1u;
+      for (int p = tid; p < n; p += NT) {
+        const int e = send[p];
+        if (((unsigned)(e - p) & mask) == 0 && p >= step && send[p - step] == e) {
+          const int sp = slot(p);
+          t.L[sp] = KD_ADD(t.L[sp], t.L[slot(p - step)]);
+        }
+      }
+      __syncthreads();
+    }
+  }
   if (n <= KD_SERIAL_TILE_MAX) {
     for (int sI = tid; sI < total_out; sI += NT) {  // one chunk: serial, thread per segment
       const int h = t.headpos[sI];
       const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
       t.endpos[sI] = (unsigned short)e;
       if (h == e) {
-        t.L[e] = A::store(A::from_w(t.w[e]));
+        if (kInt) t.L[e] = A::store(A::from_w(t.w[e]));
         continue;
       }
       T aw = A::from_w(t.w[h]);
       double awx = KD_MUL(t.w[h], t.x[h]);
       for (int i = h + 1; i <= e; ++i) {
         const double wi = t.w[i];
-        aw = A::add(aw, A::from_w(wi));
+        if (kInt) aw = A::add(aw, A::from_w(wi));
         awx = KD_ADD(awx, KD_MUL(wi, t.x[i]));
       }
-      t.L[e] = A::store(aw);
+      if (kInt) t.L[e] = A::store(aw);
       t.w[e] = awx;
     }
   } else {
+    const int E = slot.E, SE = slot.SE;
     for (int q = tid; q < n; q += NT) {
-      const int sl = tile_slot(q, E, SE, inv);
+      const int sl = slot(q);
       t.hf[sl] = 0;
       t.ef[sl] = 0;
     }
     __syncthreads();
     for (int sI = tid; sI < total_out; sI += NT) {
       const int h = t.headpos[sI];
-      t.hf[tile_slot(h, E, SE, inv)] = 1;
+      t.hf[slot(h)] = 1;
       const int e = sI + 1 < total_out ? (int)t.headpos[sI + 1] - 1 : n - 1;
-      t.ef[tile_slot(e, E, SE, inv)] = 1;
+      t.ef[slot(e)] = 1;
       t.endpos[sI] = (unsigned short)e;
     }
     __syncthreads();
@@ -653,19 +803,18 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
       for (int j = 0; j < cnt; ++j) {
         const double wi = t.w[sb + j], xi = t.x[sb + j];
         const double wx = KD_MUL(wi, xi);
-        const T wv = A::from_w(wi);
         const bool hd = t.hf[sb + j];
         if (hd || j == 0) {
-          aw = wv;
+          if (kInt) aw = A::from_w(wi);
           awx = wx;
         } else {
-          aw = A::add(aw, wv);
+          if (kInt) aw = A::add(aw, A::from_w(wi));
           awx = KD_ADD(awx, wx);
         }
         if (hd) head_seen = true;
         if (t.ef[sb + j]) {
           if (head_seen) {
-            t.L[sb + j] = A::store(aw);
+            if (kInt) t.L[sb + j] = A::store(aw);
             t.w[sb + j] = awx;
           } else {
             pend = true;
@@ -685,7 +834,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
         const int tf = __shfl_up_sync(0xffffffffu, F, o);
         if (lane >= o) {
           if (!F) {
-            Vw = A::add(Vw, tw);
+            if (kInt) Vw = A::add(Vw, tw);
             Vwx = KD_ADD(Vwx, twx);
           }
           F |= tf;
@@ -694,7 +843,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
       const T cw = A::shfl_up(Vw, 1);
       const double cwx = shfl_up_d(Vwx, 1);
       if (pend) {
-        t.L[pend_se] = A::store(A::add(cw, pend_w));
+        if (kInt) t.L[pend_se] = A::store(A::add(cw, pend_w));
         t.w[pend_se] = KD_ADD(cwx, pend_wx);
       }
     }
@@ -710,7 +859,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
     if (sI < total_out) {
       const int e = t.endpos[sI];
       const int h = t.headpos[sI];
-      const int se = tile_slot(e, E, SE, inv), sh = tile_slot(h, E, SE, inv);
+      const int se = slot(e), sh = slot(h);
       const double sw = A::to_d(A::load(t.L[se]));
       const double lo_v = t.x[sh], hi_v = t.x[se];
       ow[sI] = sw;
@@ -737,7 +886,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
     const int sI = dlist[k];
     const int e = t.endpos[sI];
     const int h = t.headpos[sI];
-    const int se = tile_slot(e, E, SE, inv), sh = tile_slot(h, E, SE, inv);
+    const int se = slot(e), sh = slot(h);
     const double sw = A::to_d(A::load(t.L[se]));
     const double lo_v = t.x[sh], hi_v = t.x[se];
     double mean = KD_DIV(t.w[se], sw);
@@ -953,7 +1102,12 @@ __global__ void k_repair(long long n, int kb, int shift, const uint64_t* __restr
 __global__ void k_prepare(PrepareArgs a) {
   const int U = a.totals[0].x;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= U || kd_err_get(a.err)) return;
+  if (j >= U) return;
+  if (kd_err_get(a.err)) {  // a failed step: the planner below sees empty keys
+    a.tm[j] = 0;
+    a.tprior[j] = 0;
+    return;
+  }
   const uint32_t key = a.tkey[j];
   const int start = a.tstart[j];
   const int end = j + 1 < U ? a.tstart[j + 1] : (int)a.n;
@@ -1251,12 +1405,12 @@ __device__ __forceinline__ TileOut tile_out(const TileArgs& a, int ai, int lt, i
   return o;
 }
 
-// One warp per tile: coalesced load into the slot layout of the tile's chunk
-// length, then the tile compress.  CAP = KD_TILE serves the large work list
-// (tiles above KD_SERIAL_TILE_MAX elements), CAP = KD_SERIAL_TILE_MAX the small
-// one; both lists are consumed by their own launch.
+// One warp per tile of the small work list (tiles of at most
+// KD_SERIAL_TILE_MAX elements, 4 warps per block): coalesced load, then the
+// warp tile compress.  The large work list has its own kernel (k_tiles_blk).
 template <int CAP>
 __global__ void __launch_bounds__(32 * (CAP == KD_TILE ? 1 : 4)) k_tiles(TileArgs a) {
+  static_assert(CAP == KD_SERIAL_TILE_MAX, "the warp tile compress serves small tiles only");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int WPB = CAP == KD_TILE ? 1 : 4;
   WarpTileT<CAP>& t = reinterpret_cast<WarpTileT<CAP>*>(smem_raw)[threadIdx.x >> 5];
@@ -1348,9 +1502,9 @@ __global__ void __launch_bounds__(32 * (CAP == KD_TILE ? 1 : 4)) k_tiles(TileArg
     __syncwarp();
     const TileOut o = tile_out(a, ai, lt, j, m);
     const int c = integral
-                      ? warp_compress<true, CAP>(t, n, s.scale, s.compression, a.force_exact,
+                      ? warp_compress<true>(t, n, s.scale, s.compression, a.force_exact,
                                                  a.id_last, o.m, o.w)
-                      : warp_compress<false, CAP>(t, n, s.scale, s.compression, a.force_exact,
+                      : warp_compress<false>(t, n, s.scale, s.compression, a.force_exact,
                                                   a.id_last, o.m, o.w);
     if (lane == 0) *o.count = c;
   }
@@ -1909,6 +2063,7 @@ static const char* err_text(int code) {
     case KD_EINVAL: return "invalid input (key out of range, non-finite value or non-positive weight)";
     case KD_EEMPTY: return "query of an empty digest";
     case KD_ECONVERGE: return "P-path hierarchy did not converge (a pass could not shrink a key's centroids)";
+    case KD_ETIMEOUT: return "a bounded device wait gave up (sort look-back); nothing was committed";
     default: return "error";
   }
 }
@@ -1959,10 +2114,15 @@ static void stage_mark(KdSession* s, int i) {
     cudaEventRecord(s->stats.ev[i], s->stream);
 }
 
-static KdSortBufs sort_bufs(KdWorkspace& w) {
-  return KdSortBufs{{w.k64[0], w.k64[1]}, {w.key[0], w.key[1]}, {w.idx[0], w.idx[1]}, w.ghist,
-                    w.rs_state, w.rs_ticket, w.rs_epoch_base, &w.rs_epochs_used, w.cap_rs_tiles,
-                    &reinterpret_cast<KdErr*>(w.err)->code};
+static KdSortBufs sort_bufs(const KdSession* s, KdWorkspace& w) {
+  KdSortBufs b{{w.k64[0], w.k64[1]}, {w.key[0], w.key[1]}, {w.idx[0], w.idx[1]}, w.ghist,
+               w.rs_state, w.rs_ticket, w.rs_epoch_base, &w.rs_epochs_used, w.cap_rs_tiles,
+               &reinterpret_cast<KdErr*>(w.err)->code};
+  if (s->wait_test > 0) {
+    b.spin_limit = s->wait_test;
+    b.stall_first = 1;
+  }
+  return b;
 }
 
 static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, const KdLevelDev& lv,
@@ -2088,7 +2248,7 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
       v.launches += 1;
     }
     stage_mark(s, 1);
-    KdSortBufs sb = sort_bufs(w);
+    KdSortBufs sb = sort_bufs(s, w);
     int rs = kd_radix_sort(sb, n, sort_bits, with_idx, s->num_sms, str, first_digit);
     v.launches += kd_radix_sort_launches(n, sort_bits, first_digit);
     if (!full_sort) {  // also for n == 1: the key is still packed
@@ -2186,7 +2346,8 @@ static KdGraphKey step_key(const KdSession* s, const KdStoreDev& sd, const KdWor
   key.scale = sd.scale;
   key.compression = sd.compression;
   key.generation = w.generation;
-  key.tuning = s->small_cap | (s->large_bps << 8) | (s->small_bps << 16) | (s->concurrent_tiles << 24);
+  key.tuning = s->small_cap | (s->large_bps << 8) | (s->small_bps << 16) | (s->concurrent_tiles << 24) |
+               ((s->wait_test != 0) << 25);
   return key;
 }
 
@@ -2217,7 +2378,7 @@ int kd_pipeline_attempt(KdSession* s, KdStore* st, KdWorkspace& w, const uint32_
   c.carry = carry;
   c.carry_mm = d_carry_mm;
   c.err = KdErrHost{0, 0, 0x7fffffffffffffffLL};
-  KdSortBufs sb = sort_bufs(w);
+  KdSortBufs sb = sort_bufs(s, w);
   kd_rs_epoch_reserve(sb, str);
   int L = std::max(1, std::min(st->levels_hint, s->max_levels));
 
@@ -2585,7 +2746,7 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
       c.timestamp = timestamps ? timestamps[i] : 0.0;
       c.err = KdErrHost{0, 0, 0x7fffffffffffffffLL};
       if (i >= base + KD_PIPE_WS) v.note(cudaStreamWaitEvent(A, ev_free[k], 0));
-      KdSortBufs sb = sort_bufs(w);
+      KdSortBufs sb = sort_bufs(s, w);
       kd_rs_epoch_reserve(sb, A);
       // capture only a batch size that comes again in this call (a new
       // size for every batch would pay a capture per batch)

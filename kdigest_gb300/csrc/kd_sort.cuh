@@ -12,8 +12,9 @@
 // warp __match_any_sync, publishes its per-digit counts, obtains the counts of
 // all preceding tiles by decoupled look-back, stages the tile in shared memory
 // in digit order and writes it out in coalesced runs.  Look-back waits are
-// bounded: a block that gives up poisons its entry, raises KD_ETIMEOUT and the
-// batch is not committed.
+// bounded: a block that gives up publishes what it has (its scatter stays
+// inside [0, n), since a partial prefix is never larger than the true one),
+// raises KD_ETIMEOUT, and the batch is not committed.
 #pragma once
 
 #include "kd_scan.cuh"
@@ -88,6 +89,8 @@ struct KdRsPass {
   const unsigned* epoch_base;  // device epoch base of this sort
   int pass;                    // epoch = *epoch_base + pass
   int* err_code;  // device status word (KdErr.code)
+  long long spin_limit;  // polls of a look-back wait before it gives up
+  int stall_first;       // tests only: tile 0 never publishes (its successor's wait runs out)
 };
 
 #ifndef KD_LB_WINDOW
@@ -172,7 +175,7 @@ __global__ void __launch_bounds__(KD_RS_THREADS, KD_RS_MIN_BLOCKS) kd_rs_oneswee
     volatile unsigned long long* st = a.state;
     unsigned long long excl = 0;
     if (b == 0) {
-      st[d] = lb_pack(epoch, KD_LB_INC, cnt_d);
+      if (!a.stall_first) st[d] = lb_pack(epoch, KD_LB_INC, cnt_d);
     } else {
       st[(size_t)b * 256 + d] = lb_pack(epoch, KD_LB_AGG, cnt_d);
       long long hi = b - 1;  // next predecessor to account for
@@ -197,7 +200,7 @@ __global__ void __launch_bounds__(KD_RS_THREADS, KD_RS_MIN_BLOCKS) kd_rs_oneswee
         }
         if (done) break;
         hi -= k;
-        if (k == 0 && ++spins > KD_RS_SPIN_LIMIT) {
+        if (k == 0 && ++spins > a.spin_limit) {
           timed_out = true;
           break;
         }
@@ -248,6 +251,8 @@ struct KdSortBufs {
   unsigned long long* epochs_used;  // host: epochs consumed since the last clear
   long long state_tiles;          // tiles the look-back array holds
   int* err_code;
+  long long spin_limit = KD_RS_SPIN_LIMIT;
+  int stall_first = 0;            // tests only (KdRsPass::stall_first)
 };
 
 static inline int kd_rs_blocks(long long n) { return (int)((n + KD_RS_TILE - 1) / KD_RS_TILE); }
@@ -283,7 +288,7 @@ static inline int kd_radix_sort(KdSortBufs& b, long long n, int key_bits, bool w
     const int dst = src ^ 1;
     KdRsPass a{b.k64[src], b.key[src], b.idx[src], b.k64[dst], b.key[dst], b.idx[dst], n, shift,
                from_key, b.ghist + pidx * 256, b.state, b.ticket, ticket_base, b.epoch_base, pidx,
-               b.err_code};
+               b.err_code, b.spin_limit, b.stall_first};
     if (with_idx)
       kd_rs_onesweep<true><<<nb, KD_RS_THREADS, kd_rs_smem(true), st>>>(a);
     else

@@ -26,171 +26,309 @@
 static double canon(double v) { return v == 0.0 ? 0.0 : v; } /* -0.0 -> +0.0 */
 
 /* ------------------------------------------------------------------------- */
-/* Canonical tile compress.                                                   */
-/*                                                                            */
-/* Restates _compress_block_kernel (gpu/add_batch.mojo:45-222) step by step:  */
-/*   1. inclusive prefix of weights, 2. id = floor(k(cum / total)),           */
-/*   3. heads where the id changes, 4. segmented sums of (w, w*x),            */
-/*   5. compaction of segment ends, mean = sum(wx)/sum(w) clamped to the       */
-/*      segment's [first, last] value, zero-weight segment -> mean 0.          */
-/* The reference sums with Hillis-Steele scans in FP32.  In FP64 the build    */
-/* fixes one association order that a single warp evaluates directly:        */
-/*   - the tile is cut into 32 lane chunks of E = ceil(n/32) consecutive      */
-/*     elements; each chunk is summed serially left to right;                 */
-/*   - chunk totals are combined by a Kogge-Stone scan over the 32 lanes      */
-/*     (rounds 1,2,4,8,16), cum = exclusive lane prefix + in-chunk prefix;    */
-/*   - the tile total is the cum of its last element;                         */
-/*   - segment sums: serial within a chunk, carried across chunks by a        */
-/*     segmented Kogge-Stone scan of each lane's trailing piece.              */
-/* Tiles of at most KD_SERIAL_TILE_MAX elements (one GPU lane each) sum       */
-/* serially, left to right, instead.                                          */
-/* For integral weights every one of these sums is exact, so the result is    */
-/* independent of the order and equals any other exact evaluation.            */
+/* Scale arithmetic.  Default: the FP64 functions of kd_math.h (the kernels   */
+/* compute the same bits).  KDO_MATH_LIBM evaluates the same formulas         */
+/* (scale.mojo:78-192) with the C library's log / asin instead, which is what */
+/* the reference's std.math calls lower to on its CPU; tests use it to        */
+/* measure how many bucket ids depend on the transcendental implementation.   */
 /* ------------------------------------------------------------------------- */
-static int tile_compress_serial(int scale, double compression, const double* x, const double* w,
-                                int n, double* out_m, double* out_w, int32_t* ids_out) {
-  double cum[KD_SERIAL_TILE_MAX];
-  int32_t id[KD_SERIAL_TILE_MAX];
-  double acc = w[0];
-  cum[0] = acc;
-  for (int i = 1; i < n; ++i) {
-    acc = acc + w[i];
-    cum[i] = acc;
+static int g_math = KDO_MATH_SHARED;
+
+void kdo_set_math(int mode) { g_math = mode == KDO_MATH_LIBM ? KDO_MATH_LIBM : KDO_MATH_SHARED; }
+int kdo_get_math(void) { return g_math; }
+
+static double libm_normalizer(int scale, double compression, double n) {
+  switch (scale) {
+    case KD_SCALE_K0: return compression / 2.0;
+    case KD_SCALE_K1: return compression / (2.0 * 3.141592653589793);
+    case KD_SCALE_K2: return compression / (4.0 * log(n / compression) + 24.0);
+    default: return compression / (4.0 * log(n / compression) + 21.0);
   }
-  double tot = cum[n - 1];
-  if (!(tot > 0.0)) tot = 1.0;
-  double nrm = kd_normalizer(scale, compression, tot);
-  for (int i = 0; i < n; ++i) id[i] = kd_bucket(scale, cum[i], tot, nrm);
-  if (ids_out)
-    for (int i = 0; i < n; ++i) ids_out[i] = id[i];
-  int cnt = 0, head = 0;
-  double sw = 0.0, swx = 0.0;
-  for (int i = 0; i < n; ++i) {
-    double wx = w[i] * x[i];
-    if (i == 0 || id[i] != id[i - 1]) {
-      head = i;
-      sw = w[i];
-      swx = wx;
-    } else {
-      sw = sw + w[i];
-      swx = swx + wx;
+}
+static double libm_k(int scale, double q, double nrm) {
+  switch (scale) {
+    case KD_SCALE_K0: return nrm * q;
+    case KD_SCALE_K1: return nrm * asin(2.0 * q - 1.0);
+    case KD_SCALE_K2: {
+      double qc = kd_clamp_q(q);
+      return nrm * log(qc / (1.0 - qc));
     }
-    if (i == n - 1 || id[i] != id[i + 1]) {
-      double mean = sw > 0.0 ? swx / sw : 0.0;
-      double lo_v = x[head], hi_v = x[i];
-      mean = mean < lo_v ? lo_v : mean;
-      mean = mean > hi_v ? hi_v : mean;
-      out_m[cnt] = mean;
-      out_w[cnt] = sw;
-      ++cnt;
+    default: {
+      double qc = kd_clamp_q(q);
+      if (qc <= 0.5) return nrm * log(2.0 * qc);
+      return -nrm * log(2.0 * (1.0 - qc));
     }
   }
-  return cnt;
+}
+static double o_normalizer(int scale, double compression, double n) {
+  return g_math == KDO_MATH_LIBM ? libm_normalizer(scale, compression, n)
+                                 : kd_normalizer(scale, compression, n);
+}
+static double o_k(int scale, double q, double nrm) {
+  return g_math == KDO_MATH_LIBM ? libm_k(scale, q, nrm) : kd_k(scale, q, nrm);
+}
+static int32_t o_bucket(int scale, double cum, double tot, double nrm) {
+  return kd_floor_i32(o_k(scale, cum / tot, nrm));
+}
+
+/* ------------------------------------------------------------------------- */
+/* P-path tile compress.                                                      */
+/*                                                                            */
+/* _compress_block_kernel (gpu/add_batch.mojo:45-222) and the grouped kernel  */
+/* (gpu/grouped.mojo:128-276) compress a sorted tile of n <= 1024 pairs on    */
+/* BLOCK_CAP = 1024 lanes (weights and means of lanes >= n are 0):            */
+/*   1. cum = Hillis-Steele inclusive scan of w (:79-95), offsets 1,2,..,512  */
+/*      (cum[i] += cum[i - off] for i >= off);                                */
+/*   2. total = cum[1023] (:97-100; <= 0 -> 1), id = floor(k(cum[i]/total))   */
+/*      (:102-112);                                                           */
+/*   3. heads where the id changes (:114-121);                               */
+/*   4. segmented Hillis-Steele scans of w and w*x (:123-160);              */
+/*   5. segment ends emit mean = sum(wx)/sum(w) (0 for zero weight) clamped  */
+/*      to the segment's [first, last] value, and sum(w) (:162-218).         */
+/* kdo_tile_compress_literal below runs exactly those lane loops.            */
+/* kdo_tile_compress computes the same prefix, total, ids and weights with   */
+/* less work:                                                                 */
+/*   - cum[i] is the Hillis-Steele value itself (all offsets, in place in    */
+/*     descending index order, which reads only values of the previous       */
+/*     round); with integral weights every partial sum is exact and a plain  */
+/*     running sum gives the same bits;                                       */
+/*   - total is the scan's lane 1023: a balanced pairwise tree over lanes     */
+/*     [0, 1024), i.e. over [0, 2^ceil(log2 n)) since adding a zero lane is   */
+/*     exact;                                                                 */
+/*   - a segment's scan value at its end element e (head h) is the sum of     */
+/*     x[h..e] in the right-aligned pairwise tree: level-1 pairs (e, e-1),    */
+/*     (e-2, e-3), ..., each level pairing the previous level's nodes from   */
+/*     the e side, a node without partner carried up unchanged (the scan      */
+/*     stops adding once its window reaches the head), plus the zero the     */
+/*     scan adds in its later rounds.  That is the reference scan's value at */
+/*     e with e - h additions instead of ~10 per lane.                        */
+/* Segment sums of w*x come in two associations (kdo_set_sums):              */
+/*   - KDO_SUMS_REFERENCE: the reference's tree above;                        */
+/*   - KDO_SUMS_BUILD (default): the order the kernels use, which keeps their */
+/*     FP64 pipe busy: tiles of at most KD_SERIAL_TILE_MAX elements sum each  */
+/*     segment serially, left to right; larger tiles cut the tile into 32     */
+/*     lane chunks of E = ceil(n/32) consecutive elements, sum each piece of  */
+/*     a segment inside a chunk serially and carry the trailing pieces across */
+/*     chunks with a segmented Kogge-Stone scan over the 32 chunks.           */
+/* The two differ by rounding in the means only: no prefix, id or weight     */
+/* depends on sum(w*x).  The tests check the reference form against the lane */
+/* loops bit for bit and the build form against the reference form.          */
+/* ------------------------------------------------------------------------- */
+static int g_sums = KDO_SUMS_BUILD;
+
+void kdo_set_sums(int mode) { g_sums = mode == KDO_SUMS_REFERENCE ? KDO_SUMS_REFERENCE : KDO_SUMS_BUILD; }
+int kdo_get_sums(void) { return g_sums; }
+
+static int small_int(double w) { /* an integral weight in [1, 2^42), as the kernels test it */
+  if (!(w >= 1.0 && w < 4398046511104.0)) return 0;
+  return floor(w) == w;
+}
+
+/* Sum of v[0..len) in the right-aligned pairwise tree, v[len-1] being the
+ * segment's end element.  tmp holds at least (len + 1) / 2 entries. */
+static double rapt_sum(const double* v, int len, double* tmp) {
+  if (len == 1) return v[0];
+  int m = 0;
+  for (int u = 0; u < len; u += 2) { /* u: distance from the end */
+    const double a = v[len - 1 - u];
+    tmp[m++] = u + 1 < len ? a + v[len - 2 - u] : a;
+  }
+  while (m > 1) {
+    int k = 0;
+    for (int u = 0; u < m; u += 2) tmp[k++] = u + 1 < m ? tmp[u] + tmp[u + 1] : tmp[u];
+    m = k;
+  }
+  return tmp[0];
+}
+
+/* Total of the tile: the balanced tree over lanes [0, 2^ceil(log2 n)). */
+static double tree_total(const double* w, int n, double* tmp) {
+  if (n == 1) return w[0];
+  int m = 0;
+  for (int i = 0; i < n; i += 2) tmp[m++] = i + 1 < n ? w[i] + w[i + 1] : w[i];
+  while (m > 1) {
+    int k = 0;
+    for (int i = 0; i < m; i += 2) tmp[k++] = i + 1 < m ? tmp[i] + tmp[i + 1] : tmp[i];
+    m = k;
+  }
+  return tmp[0];
+}
+
+static int emit_segment(const double* x, int h, int e, double sw, double swx, double* out_m,
+                        double* out_w, int cnt) {
+  double mean = sw > 0.0 ? swx / sw : 0.0;
+  double lo_v = x[h], hi_v = x[e];
+  mean = mean < lo_v ? lo_v : mean;
+  mean = mean > hi_v ? hi_v : mean;
+  out_m[cnt] = mean;
+  out_w[cnt] = sw;
+  return cnt + 1;
+}
+
+/* sum(w*x) of every segment in the kernels' order (KDO_SUMS_BUILD), written
+ * at each segment end e into swx[e]. */
+static void build_order_wx(const double* wx, const int32_t* id, int n, double* swx) {
+  if (n <= KD_SERIAL_TILE_MAX) {
+    double a = 0.0;
+    for (int i = 0; i < n; ++i) {
+      a = (i == 0 || id[i] != id[i - 1]) ? wx[i] : a + wx[i];
+      if (i == n - 1 || id[i] != id[i + 1]) swx[i] = a;
+    }
+    return;
+  }
+  const int E = (n + 31) / 32;
+  double V[32];
+  int F[32];
+  int pend[32];
+  double pendv[32];
+  for (int c = 0; c < 32; ++c) {
+    V[c] = 0.0;
+    F[c] = 0;
+    pend[c] = -1;
+    int lo = c * E, hi = lo + E < n ? lo + E : n;
+    if (lo >= n) continue;
+    double a = 0.0;
+    for (int i = lo; i < hi; ++i) {
+      const int head = (i == 0) || id[i] != id[i - 1];
+      a = (head || i == lo) ? wx[i] : a + wx[i];
+      if (head) F[c] = 1;
+      if (i == n - 1 || id[i] != id[i + 1]) {
+        if (F[c]) swx[i] = a;
+        else { pend[c] = i; pendv[c] = a; } /* segment started in an earlier chunk */
+      }
+    }
+    V[c] = a;
+  }
+  for (int o = 1; o < 32; o <<= 1) { /* segmented inclusive Kogge-Stone over the chunks */
+    double tv[32];
+    int tf[32];
+    for (int c = 0; c < 32; ++c) { tv[c] = V[c]; tf[c] = F[c]; }
+    for (int c = o; c < 32; ++c) {
+      if (!tf[c]) V[c] = tv[c] + tv[c - o];
+      F[c] = tf[c] | tf[c - o];
+    }
+  }
+  for (int c = 1; c < 32; ++c)
+    if (pend[c] >= 0) swx[pend[c]] = V[c - 1] + pendv[c];
 }
 
 int kdo_tile_compress(int scale, double compression, const double* x, const double* w,
                       int n, double* out_m, double* out_w, int32_t* ids_out) {
   if (n <= 0) return 0;
-  if (n <= KD_SERIAL_TILE_MAX)
-    return tile_compress_serial(scale, compression, x, w, n, out_m, out_w, ids_out);
-  const int E = (n + 31) / 32;
-  double L[KDO_BLOCK_CAP], cum[KDO_BLOCK_CAP];
+  if (n > KDO_BLOCK_CAP) return -1;
+  double cum[KDO_BLOCK_CAP], wx[KDO_BLOCK_CAP], seg[KDO_BLOCK_CAP], tmp[KDO_BLOCK_CAP];
+  double swxb[KDO_BLOCK_CAP];
   int32_t id[KDO_BLOCK_CAP];
-  double S[32], I[32], tmp[32];
-  for (int c = 0; c < 32; ++c) S[c] = 0.0;
-  for (int c = 0; c < 32; ++c) {
-    int lo = c * E, hi = lo + E < n ? lo + E : n;
-    if (lo >= n) break;
-    double acc = w[lo];
-    L[lo] = acc;
-    for (int i = lo + 1; i < hi; ++i) {
+  int integral = 1;
+  for (int i = 0; i < n; ++i) integral &= small_int(w[i]);
+  double tot;
+  if (integral) { /* exact: any order gives these bits */
+    double acc = w[0];
+    cum[0] = acc;
+    for (int i = 1; i < n; ++i) {
       acc = acc + w[i];
-      L[i] = acc;
+      cum[i] = acc;
     }
-    S[c] = acc;
+    tot = cum[n - 1];
+  } else {
+    for (int i = 0; i < n; ++i) cum[i] = w[i];
+    for (int off = 1; off < n; off <<= 1)
+      for (int i = n - 1; i >= off; --i) cum[i] = cum[i] + cum[i - off];
+    tot = tree_total(w, n, tmp);
   }
-  for (int c = 0; c < 32; ++c) I[c] = S[c];
-  for (int o = 1; o < 32; o <<= 1) {
-    for (int c = 0; c < 32; ++c) tmp[c] = I[c];
-    for (int c = o; c < 32; ++c) I[c] = tmp[c] + tmp[c - o];
-  }
-  for (int i = 0; i < n; ++i) {
-    int c = i / E;
-    cum[i] = c == 0 ? L[i] : I[c - 1] + L[i];
-  }
-  double tot = cum[n - 1];
   if (!(tot > 0.0)) tot = 1.0; /* add_batch.mojo:98-100 */
-  double nrm = kd_normalizer(scale, compression, tot);
-  for (int i = 0; i < n; ++i) id[i] = kd_bucket(scale, cum[i], tot, nrm);
+  double nrm = o_normalizer(scale, compression, tot);
+  for (int i = 0; i < n; ++i) id[i] = o_bucket(scale, cum[i], tot, nrm);
   if (ids_out)
     for (int i = 0; i < n; ++i) ids_out[i] = id[i];
-
-  /* Segment sums.  For each lane: pieces are maximal runs inside the chunk
-   * belonging to one segment; piece sums are serial.  Record, per segment end,
-   * its piece sum and whether its head lies in the same chunk. */
-  double pw[KDO_BLOCK_CAP], pwx[KDO_BLOCK_CAP];
-  unsigned char local_head[KDO_BLOCK_CAP];
-  double Vw[32], Vwx[32];
-  int F[32];
-  for (int c = 0; c < 32; ++c) { Vw[c] = 0.0; Vwx[c] = 0.0; F[c] = 0; }
-  for (int c = 0; c < 32; ++c) {
-    int lo = c * E, hi = lo + E < n ? lo + E : n;
-    if (lo >= n) break;
-    double aw = 0.0, awx = 0.0;
-    int head_seen = 0;
-    for (int i = lo; i < hi; ++i) {
-      int head = (i == 0) || id[i] != id[i - 1];
-      double wx = w[i] * x[i];
-      if (head || i == lo) {
-        aw = w[i];
-        awx = wx;
-      } else {
-        aw = aw + w[i];
-        awx = awx + wx;
-      }
-      if (head) head_seen = 1;
-      int end = (i == n - 1) || id[i] != id[i + 1];
-      if (end) {
-        pw[i] = aw;
-        pwx[i] = awx;
-        local_head[i] = (unsigned char)head_seen;
-      }
+  for (int i = 0; i < n; ++i) wx[i] = w[i] * x[i];
+  if (g_sums == KDO_SUMS_BUILD) build_order_wx(wx, id, n, swxb);
+  int cnt = 0;
+  for (int h = 0; h < n;) {
+    int e = h;
+    while (e + 1 < n && id[e + 1] == id[h]) ++e;
+    const int len = e - h + 1;
+    double sw;
+    if (integral) {
+      sw = w[h];
+      for (int i = h + 1; i <= e; ++i) sw = sw + w[i];
+    } else {
+      for (int i = 0; i < len; ++i) seg[i] = w[h + i];
+      sw = rapt_sum(seg, len, tmp);
     }
-    Vw[c] = aw;
-    Vwx[c] = awx;
-    F[c] = head_seen;
+    const double swx = g_sums == KDO_SUMS_BUILD ? swxb[e] : rapt_sum(wx + h, len, tmp) + 0.0;
+    cnt = emit_segment(x, h, e, sw, swx, out_m, out_w, cnt);
+    h = e + 1;
   }
-  /* Segmented inclusive Kogge-Stone over the lanes' trailing pieces. */
-  for (int o = 1; o < 32; o <<= 1) {
-    double tw[32], twx[32];
-    int tf[32];
-    for (int c = 0; c < 32; ++c) { tw[c] = Vw[c]; twx[c] = Vwx[c]; tf[c] = F[c]; }
-    for (int c = o; c < 32; ++c) {
-      if (!tf[c]) {
-        Vw[c] = tw[c] + tw[c - o];
-        Vwx[c] = twx[c] + twx[c - o];
+  return cnt;
+}
+
+/* The reference's lane loops, literally (FP64; test use only). */
+int kdo_tile_compress_literal(int scale, double compression, const double* x, const double* w,
+                              int n, double* out_m, double* out_w, int32_t* ids_out) {
+  enum { B = KDO_BLOCK_CAP };
+  if (n <= 0) return 0;
+  if (n > B) return -1;
+  static _Thread_local double lw[B], cum[B], tmp[B], sw[B], smw[B], nw[B], nmw[B], seg_lo[B];
+  static _Thread_local int32_t cid[B], fl[B], nfl[B], is_end[B], pos[B], npos[B];
+  for (int t = 0; t < B; ++t) lw[t] = t < n ? w[t] : 0.0;
+  for (int t = 0; t < B; ++t) cum[t] = lw[t];
+  for (int off = 1; off < B; off *= 2) {
+    for (int t = 0; t < B; ++t) tmp[t] = t >= off ? cum[t] + cum[t - off] : cum[t];
+    for (int t = 0; t < B; ++t) cum[t] = tmp[t];
+  }
+  double total = cum[B - 1];
+  if (total <= 0.0) total = 1.0;
+  const double nrm = o_normalizer(scale, compression, total);
+  for (int t = 0; t < B; ++t)
+    cid[t] = t < n ? kd_floor_i32(o_k(scale, cum[t] / total, nrm)) : 2147483647;
+  if (ids_out)
+    for (int t = 0; t < n; ++t) ids_out[t] = cid[t];
+  for (int t = 0; t < B; ++t) fl[t] = t == 0 ? 1 : (cid[t] != cid[t - 1] ? 1 : 0);
+  for (int t = 0; t < B; ++t) {
+    sw[t] = lw[t];
+    smw[t] = lw[t] * (t < n ? x[t] : 0.0);
+  }
+  for (int voff = 1; voff < B; voff *= 2) {
+    for (int t = 0; t < B; ++t) {
+      double add_w = 0.0, add_mw = 0.0;
+      if (t >= voff && fl[t] == 0) {
+        add_w = sw[t - voff];
+        add_mw = smw[t - voff];
       }
-      F[c] = tf[c] | tf[c - o];
+      nfl[t] = t >= voff ? ((fl[t] != 0 || fl[t - voff] != 0) ? 1 : 0) : fl[t];
+      nw[t] = sw[t] + add_w;
+      nmw[t] = smw[t] + add_mw;
     }
+    for (int t = 0; t < B; ++t) {
+      sw[t] = nw[t];
+      smw[t] = nmw[t];
+      fl[t] = nfl[t];
+    }
+  }
+  for (int t = 0; t < B; ++t) {
+    is_end[t] = 0;
+    if (t < n) is_end[t] = (t == n - 1 || cid[t] != cid[t + 1]) ? 1 : 0;
+  }
+  for (int t = 0; t < B; ++t) pos[t] = is_end[t];
+  for (int poff = 1; poff < B; poff *= 2) {
+    for (int t = 0; t < B; ++t) npos[t] = t >= poff ? pos[t] + pos[t - poff] : pos[t];
+    for (int t = 0; t < B; ++t) pos[t] = npos[t];
+  }
+  for (int t = 0; t < n; ++t) {
+    const int is_head = t == 0 || cid[t] != cid[t - 1];
+    if (is_head) seg_lo[t == 0 ? 0 : pos[t - 1]] = x[t];
   }
   int cnt = 0;
-  int head_idx = 0;
-  for (int i = 0; i < n; ++i) {
-    if (i == 0 || id[i] != id[i - 1]) head_idx = i;
-    int end = (i == n - 1) || id[i] != id[i + 1];
-    if (!end) continue;
-    int c = i / E;
-    double sw = pw[i], swx = pwx[i];
-    if (!local_head[i]) { /* segment started in an earlier chunk */
-      sw = Vw[c - 1] + sw;
-      swx = Vwx[c - 1] + swx;
-    }
-    double mean = sw > 0.0 ? swx / sw : 0.0;
-    double lo_v = x[head_idx], hi_v = x[i];
+  for (int t = 0; t < n; ++t) {
+    if (!is_end[t]) continue;
+    const int slot = pos[t] - 1;
+    double mean = sw[t] > 0.0 ? smw[t] / sw[t] : 0.0;
+    const double lo_v = seg_lo[slot], hi_v = x[t];
     mean = mean < lo_v ? lo_v : mean;
     mean = mean > hi_v ? hi_v : mean;
-    out_m[cnt] = mean;
-    out_w[cnt] = sw;
+    out_m[slot] = mean;
+    out_w[slot] = sw[t];
     ++cnt;
   }
   return cnt;
@@ -416,7 +554,7 @@ void kdo_merge(kdo_digest* d) {
   }
   double effective_n = effective_count(d);
   double stored_n = d->stored_total;
-  double nrm = kd_normalizer(d->scale, d->compression, effective_n);
+  double nrm = o_normalizer(d->scale, d->compression, effective_n);
   reserve_c(d, n);
   int64_t k = 0;
   double cur_m = m[0], cur_w = w[0];
@@ -424,7 +562,7 @@ void kdo_merge(kdo_digest* d) {
   for (int64_t i = 1; i < n; ++i) {
     double q_left = wsf / stored_n;
     double q_right = (wsf + cur_w + w[i]) / stored_n;
-    double k_span = kd_k(d->scale, q_right, nrm) - kd_k(d->scale, q_left, nrm);
+    double k_span = o_k(d->scale, q_right, nrm) - o_k(d->scale, q_left, nrm);
     if (m[i] == cur_m || k_span <= 1.0) {
       /* Centroid.add_sample — centroid.mojo:279-290 */
       double new_w = cur_w + w[i];

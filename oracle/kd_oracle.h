@@ -11,8 +11,9 @@
  *   src/kdigest/scale.mojo, decay.mojo, centroid.mojo, tdigest.mojo,
  *   grouped.mojo, gpu/add_batch.mojo, gpu/grouped.mojo, gpu/query.mojo,
  *   gpu/sort.mojo, gpu/primitives.mojo
- * in FP64 (the reference's GPU path is FP32; see the design doc for the precision
- * and summation-order choices this restatement pins).
+ * in FP64 (the reference's GPU path is FP32).  Sums keep the reference's own
+ * association order: the Hillis-Steele scans of the P-path tile kernels and
+ * the serial loops of the host code.
  */
 #ifndef KD_ORACLE_H
 #define KD_ORACLE_H
@@ -31,11 +32,30 @@ extern "C" {
 
 #define KDO_BLOCK_CAP 1024
 
-/* One P-path tile: the canonical tile compress of n <= 1024 mean-sorted pairs.
+/* Transcendentals of the scale functions: the FP64 functions shared with the
+ * kernels (default), or the C library's log / asin. */
+#define KDO_MATH_SHARED 0
+#define KDO_MATH_LIBM 1
+void kdo_set_math(int mode);
+int kdo_get_math(void);
+
+/* Association of the segment sums of w*x: the kernels' order (default) or
+ * the reference's segmented Hillis-Steele tree.  Prefix sums, tile totals and
+ * segment weights always take the reference's association. */
+#define KDO_SUMS_BUILD 0
+#define KDO_SUMS_REFERENCE 1
+void kdo_set_sums(int mode);
+int kdo_get_sums(void);
+
+/* One P-path tile (gpu/add_batch.mojo:45-222) of n <= 1024 mean-sorted pairs.
  * Returns the number of centroids written; ids_out (optional, n entries)
  * receives each element's bucket id. */
 int kdo_tile_compress(int scale, double compression, const double* x, const double* w,
                       int n, double* out_m, double* out_w, int32_t* ids_out);
+/* The same tile through the reference kernel's 1024-lane loops run literally
+ * (ten scan rounds per sum, segment flags, zero-padded lanes). */
+int kdo_tile_compress_literal(int scale, double compression, const double* x, const double* w,
+                              int n, double* out_m, double* out_w, int32_t* ids_out);
 
 /* P-path compress of an arbitrary (mean, weight) set: stable sort by mean, then
  * the 1024-tile hierarchy.  out_* need capacity n.  perm_out (optional, n

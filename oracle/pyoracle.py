@@ -43,6 +43,12 @@ def lib():
         L = ctypes.CDLL(_LIB_PATH)
         L.kdo_tile_compress.restype = ctypes.c_int
         L.kdo_tile_compress.argtypes = [ctypes.c_int, _D, _P, _P, ctypes.c_int, _P, _P, _P]
+        L.kdo_tile_compress_literal.restype = ctypes.c_int
+        L.kdo_tile_compress_literal.argtypes = [ctypes.c_int, _D, _P, _P, ctypes.c_int, _P, _P, _P]
+        L.kdo_set_math.argtypes = [ctypes.c_int]
+        L.kdo_get_math.restype = ctypes.c_int
+        L.kdo_set_sums.argtypes = [ctypes.c_int]
+        L.kdo_get_sums.restype = ctypes.c_int
         L.kdo_ppath_compress.restype = _I64
         L.kdo_ppath_compress.argtypes = [ctypes.c_int, _D, _P, _P, _I64, _P, _P, _P]
         L.kdo_digest_new.restype = _P
@@ -97,13 +103,65 @@ class OracleError(RuntimeError):
         self.code = code
 
 
-def tile_compress(scale: int, compression: float, x, w):
+MATH_SHARED, MATH_LIBM = 0, 1
+
+
+class math_mode:
+    """Context manager: evaluate the scale functions with the shared FP64
+    functions (MATH_SHARED, what the kernels compute) or with the C library's
+    log / asin (MATH_LIBM) inside the block."""
+
+    def __init__(self, mode: int):
+        self.mode = mode
+
+    def __enter__(self):
+        self.prev = lib().kdo_get_math()
+        lib().kdo_set_math(self.mode)
+        return self
+
+    def __exit__(self, *exc):
+        lib().kdo_set_math(self.prev)
+        return False
+
+
+SUMS_BUILD, SUMS_REFERENCE = 0, 1
+
+
+class sums_mode:
+    """Context manager: segment sums of w*x in the kernels' association
+    (SUMS_BUILD) or in the reference's Hillis-Steele tree (SUMS_REFERENCE)
+    inside the block.  Prefix sums, totals and weights never change."""
+
+    def __init__(self, mode: int):
+        self.mode = mode
+
+    def __enter__(self):
+        self.prev = lib().kdo_get_sums()
+        lib().kdo_set_sums(self.mode)
+        return self
+
+    def __exit__(self, *exc):
+        lib().kdo_set_sums(self.prev)
+        return False
+
+
+def _tile(fn, scale, compression, x, w):
     x = np.ascontiguousarray(x, dtype=np.float64)
     w = np.ascontiguousarray(w, dtype=np.float64)
     n = len(x)
     om = np.empty(max(n, 1)); ow = np.empty(max(n, 1)); ids = np.empty(max(n, 1), np.int32)
-    c = lib().kdo_tile_compress(scale, compression, _ptr(x), _ptr(w), n, _ptr(om), _ptr(ow), _ptr(ids))
+    c = fn(scale, compression, _ptr(x), _ptr(w), n, _ptr(om), _ptr(ow), _ptr(ids))
     return om[:c].copy(), ow[:c].copy(), ids[:n].copy()
+
+
+def tile_compress(scale: int, compression: float, x, w):
+    """One P-path tile in the reference's Hillis-Steele association."""
+    return _tile(lib().kdo_tile_compress, scale, compression, x, w)
+
+
+def tile_compress_literal(scale: int, compression: float, x, w):
+    """The same tile through the reference kernel's 1024-lane loops."""
+    return _tile(lib().kdo_tile_compress_literal, scale, compression, x, w)
 
 
 def ppath_compress(scale: int, compression: float, means, weights, want_perm: bool = False):

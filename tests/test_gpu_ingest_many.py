@@ -227,3 +227,44 @@ def test_eager_and_one_front_stream(kd, graphs, fronts):
     for k, v in batches:
         b.add_batch(k, v)
     _same(a, b, nk)
+
+
+def _min_budget(kd, nk, batch):
+    """The smallest session budget (to 1 MiB) that holds a store of nk keys
+    and one ingest of `batch`."""
+    from kdigest_gb300 import _native as N
+
+    lo, hi = 1 << 20, 8 << 30
+    while hi - lo > (1 << 20):
+        mid = (lo + hi) // 2
+        try:
+            g = kd.GroupedTDigest(nk, 100.0, scale=kd.K3, session=kd.GpuSession(mem_budget=mid))
+            g.add_batch(*batch)
+            hi = mid
+        except (N.KdError, MemoryError):
+            lo = mid
+        finally:
+            g = None
+    return hi
+
+
+def test_budget_without_room_for_the_pipeline(kd):
+    """A session budget that fits the store and one ingest workspace but not
+    the pipeline's two extra workspaces and staging buffers: add_batches falls
+    back to one call per batch (device tensors, and host arrays) and ends
+    exactly where one add_batch per batch ends."""
+    import torch
+
+    nk = 500
+    batches = _batches(nk, [120000] * 4, 77)
+    budget = _min_budget(kd, nk, batches[0]) + (2 << 20)
+    b = kd.GroupedTDigest(nk, 100.0, scale=kd.K3, session=kd.GpuSession())
+    for k, v in batches:
+        b.add_batch(k, v)
+    a = kd.GroupedTDigest(nk, 100.0, scale=kd.K3, session=kd.GpuSession(mem_budget=budget))
+    dev = [(torch.from_numpy(k).cuda(), torch.from_numpy(v).cuda()) for k, v in batches]
+    a.add_batches(dev)
+    _same(a, b, nk, keys=range(nk))
+    c = kd.GroupedTDigest(nk, 100.0, scale=kd.K3, session=kd.GpuSession(mem_budget=budget))
+    c.add_batches(batches)
+    _same(c, b, nk, keys=range(nk))

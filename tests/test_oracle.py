@@ -307,7 +307,7 @@ def test_ppath_hierarchy_restated():
 
 def _hillis_steele_ids(scale, compression, w):
     """Literal FP64 restatement of the reference's 1024-wide Hillis-Steele
-    inclusive scan + bucket ids (add_batch.mojo:79-112)."""
+    inclusive scan + bucket ids (add_batch.mojo:79-112), in numpy."""
     n = len(w)
     cum = np.zeros(1024)
     cum[:n] = w
@@ -324,17 +324,86 @@ def _hillis_steele_ids(scale, compression, w):
     return [o.bucket(scale, float(cum[i]), float(total), nrm) for i in range(n)]
 
 
+def _tile_cases(rng, count):
+    """Sorted tiles of every size class with integral, fractional, equal
+    decayed and mixed prior/new weights, with and without ties."""
+    for i in range(count):
+        n = int(rng.integers(1, 1025)) if i % 5 else int(rng.choice([1, 2, 3, 31, 32, 33, 127, 128, 129, 1023, 1024]))
+        x = np.sort(rng.standard_normal(n))
+        kind = i % 4
+        if kind == 0:
+            w = rng.integers(1, 50, n).astype(np.float64)
+        elif kind == 1:
+            w = rng.random(n) + 0.5
+        elif kind == 2:  # one batch's samples at a decay factor e^{log_scale}
+            w = np.full(n, np.exp(rng.uniform(0, 40)))
+        else:  # prior centroids (fractional weights) merged with new samples, ties
+            w = np.full(n, 1.37)
+            k = int(rng.integers(0, n))
+            w[:k] = rng.random(k) * 100
+            x = np.sort(np.round(x * 3) / 3)
+        yield int(rng.integers(0, 4)), float(rng.choice([50.0, 100.0, 200.0])), x, w
+
+
+def test_tile_compress_equals_reference_lane_loops():
+    """In the reference association, the oracle's tile (Hillis-Steele prefix,
+    balanced-tree total, right-aligned segment trees) equals the reference
+    kernel's 1024-lane loops run literally, bit for bit: ids, centroid means
+    and weights."""
+    rng = np.random.default_rng(2024)
+    with o.sums_mode(o.SUMS_REFERENCE):
+        for scale, comp, x, w in _tile_cases(rng, 600):
+            a = o.tile_compress(scale, comp, x, w)
+            b = o.tile_compress_literal(scale, comp, x, w)
+            for u, v in zip(a, b):
+                assert np.array_equal(u, v), (scale, comp, len(x))
+
+
+def test_build_sums_differ_from_reference_in_means_only():
+    """The kernels' association of sum(w*x) changes the means by rounding only:
+    bucket ids, centroid counts and weights are identical to the reference's,
+    and every mean agrees within 1e-12 relative (the benchmark spec's bound for
+    summation order)."""
+    rng = np.random.default_rng(77)
+    worst = 0.0
+    for scale, comp, x, w in _tile_cases(rng, 600):
+        x = x * 10.0 ** rng.uniform(-3, 3) + rng.uniform(-50, 50)
+        a = o.tile_compress(scale, comp, x, w)
+        with o.sums_mode(o.SUMS_REFERENCE):
+            b = o.tile_compress(scale, comp, x, w)
+        assert np.array_equal(a[2], b[2]) and np.array_equal(a[1], b[1])
+        scale_m = np.maximum(np.abs(b[0]), np.max(np.abs(x)))  # relative to the tile's magnitude
+        worst = max(worst, float(np.max(np.abs(a[0] - b[0]) / scale_m)))
+    assert worst < 1e-12, worst
+
+
 @pytest.mark.parametrize("scale", [0, 1, 2, 3])
-def test_canonical_order_equals_reference_order_for_integral_weights(scale):
-    """With integral weights every partial sum is exact, so the canonical
-    lane-chunk order and the reference's Hillis-Steele order give identical
-    bucket ids (and therefore identical centroids)."""
+def test_tile_ids_equal_numpy_hillis_steele(scale):
+    """The C lane loops and an independent numpy statement of the reference's
+    scan give the same bucket ids, for integral and fractional weights."""
     rng = np.random.default_rng(9 + scale)
     for n in (1, 5, 32, 33, 100, 777, 1024):
-        w = rng.integers(1, 50, n).astype(np.float64)
+        for w in (rng.integers(1, 50, n).astype(np.float64), rng.random(n) * 3 + 0.01):
+            x = np.sort(rng.standard_normal(n))
+            _, _, ids = o.tile_compress(scale, 100.0, x, w)
+            assert list(ids) == _hillis_steele_ids(scale, 100.0, w)
+
+
+def test_k1_prefix_above_total_maps_to_id_zero():
+    """A fractional tile whose last prefix sum rounds above the balanced-tree
+    total: K1 evaluates asin slightly above 1 (scale.mojo:114-118 does not
+    clamp q), gets NaN and int32 id 0, as the reference's platform converts."""
+    rng = np.random.default_rng(5)
+    hits = 0
+    for _ in range(4000):
+        n = int(rng.integers(3, 40))
+        w = rng.random(n) + 0.1
         x = np.sort(rng.standard_normal(n))
-        _, _, ids = o.tile_compress(scale, 100.0, x, w)
-        assert list(ids) == _hillis_steele_ids(scale, 100.0, w)
+        _, _, ids = o.tile_compress(o.K1, 100.0, x, w)
+        lit = o.tile_compress_literal(o.K1, 100.0, x, w)[2]
+        assert list(ids) == list(lit)
+        hits += int(ids[-1] == 0)
+    assert hits > 0
 
 
 def test_grouped_equals_per_key_single_digest():
