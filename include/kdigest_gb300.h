@@ -103,6 +103,52 @@ KD_API int kd_compress(kd_session* s, int scale, double compression, const doubl
                        const double* weights, int64_t n, int flags, double* out_means,
                        double* out_weights, int64_t cap, int64_t* out_n);
 
+/* Stateless entry points over caller-held digests: the reference's host state
+ * keeps its digests on the host and passes their centroid arrays per call.
+ * Digests and groups are CSR: digest d is entries [offsets[d], offsets[d+1]) of
+ * the means / weights arrays (offsets[0] = 0, non-decreasing).
+ *
+ * gpu_grouped_compress_weighted (gpu/grouped.mojo:415-427, called from
+ * grouped.mojo:144-157): for every key k < num_keys, the P-path compress of its
+ * prior centroids (prior CSR, NULL prior_offsets: none) followed by its new
+ * samples in batch order, each of weight new_weights[k] (NULL: 1).  A key with
+ * neither gets no centroids.  The result is the output CSR over keys:
+ * out_offsets (num_keys + 1, always filled), out_means / out_weights of cap
+ * entries (KD_ERANGE with *out_n = the needed total when cap is too small).
+ * out_min / out_max (num_keys, may be NULL): the range of each key's new
+ * samples (0 without).  Everything is validated before any work (KD_EINVAL:
+ * key out of range, non-finite value, weight <= 0).  Host pointers. */
+KD_API int kd_grouped_compress(kd_session* s, int scale, double compression, int64_t num_keys,
+                               const uint32_t* keys, const double* values, int64_t n,
+                               const double* new_weights, const int64_t* prior_offsets,
+                               const double* prior_means, const double* prior_weights,
+                               int64_t* out_offsets, double* out_means, double* out_weights,
+                               int64_t cap, int64_t* out_n, double* out_min, double* out_max);
+/* gpu_quantile / gpu_cdf (gpu/query.mojo:320-342) for many digests at once:
+ * query i reads digest ids[i] (ids NULL: digest 0) of the caller's CSR, with
+ * that digest's min_v / max_v.  As the reference kernels: the walk's total is
+ * the digest's weights summed in order (<= 0 -> 1), a tail centroid of raw
+ * weight <= 1 + 1e-6 is a singleton, q <= 0 / q >= 1 give min / max (no range
+ * error).  An empty digest gives KD_EEMPTY, one above 1024 centroids KD_ERANGE,
+ * an id out of range KD_EINVAL (NaN for those queries; the first status is
+ * returned).  Host pointers, or device pointers with KD_PTR_DEVICE. */
+KD_API int kd_quantile(kd_session* s, const int64_t* offsets, int64_t ndigests, const double* means,
+                       const double* weights, const double* min_v, const double* max_v,
+                       const uint32_t* ids, const double* qs, int64_t nq, double* out, int flags);
+KD_API int kd_cdf(kd_session* s, const int64_t* offsets, int64_t ndigests, const double* means,
+                  const double* weights, const double* min_v, const double* max_v,
+                  const uint32_t* ids, const double* xs, int64_t nx, double* out, int flags);
+/* gpu_merge_digests (gpu/query.mojo:348-369), batched: group g is the P-path
+ * compress of the centroids of parts part_ids[group_offsets[g] ..
+ * group_offsets[g+1]) (part_ids NULL: parts group_offsets[g] .. in order),
+ * concatenated in that order.  Parts are a CSR (part_offsets, nparts + 1).
+ * Output CSR over groups as kd_grouped_compress.  Host pointers. */
+KD_API int kd_merge(kd_session* s, int scale, double compression, const int64_t* part_offsets,
+                    int64_t nparts, const double* means, const double* weights,
+                    const int64_t* group_offsets, int64_t ngroups, const uint32_t* part_ids,
+                    int64_t* out_offsets, double* out_means, double* out_weights, int64_t cap,
+                    int64_t* out_n);
+
 /* Resident per-key digests (GroupedTDigest, grouped.mojo:30-58; one key is a
  * TDigest, tdigest.mojo:135-151): num_keys dense ids, shared scale, compression
  * and decay rate (Decay.rate / half_life, decay.mojo:24-47; 0 = none). */
@@ -156,6 +202,15 @@ KD_API int kd_store_quantile(kd_store* st, const uint32_t* keys, const double* q
                              double* out, int flags);
 KD_API int kd_store_cdf(kd_store* st, const uint32_t* keys, const double* xs, int64_t nx,
                         double* out, int flags);
+/* kd_store_quantile and kd_store_cdf of one call in one kernel launch: nq
+ * (qkeys, qs) quantile queries into qout and nc (ckeys, xs) cdf queries into
+ * cout (keys NULL: all key 0).  With device pointers, a call with the same
+ * arguments as the call before it is captured as a CUDA graph and replayed
+ * from then on.  Errors fill NaN and return the first failing status.  Same
+ * arithmetic as the two calls (tdigest.mojo:485-587). */
+KD_API int kd_store_query_batch(kd_store* st, const uint32_t* qkeys, const double* qs, int64_t nq,
+                                double* qout, const uint32_t* ckeys, const double* xs, int64_t nc,
+                                double* cout, int flags);
 
 /* gpu_merge_digests (gpu/query.mojo:348-369) with merge_into's rebasing
  * (tdigest.mojo:589-623), batched: dst key g becomes the P-path compress of the

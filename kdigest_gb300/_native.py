@@ -37,6 +37,7 @@ EXPORTED = (
     "kd_store_export", "kd_store_import",
     "kd_keymap_create", "kd_keymap_map", "kd_keymap_lookup", "kd_keymap_size", "kd_keymap_destroy",
     "kd_store_add", "kd_store_flush", "kd_store_merge_into", "kd_store_ingest_many",
+    "kd_store_query_batch", "kd_grouped_compress", "kd_quantile", "kd_cdf", "kd_merge",
 )
 KD_REQ_INGEST, KD_REQ_QUANTILE, KD_REQ_CDF = 0, 1, 2
 
@@ -89,6 +90,13 @@ def load(path: str = LIB_PATH):
                                        ctypes.POINTER(_I64)]
     L.kd_store_quantile.argtypes = [_P, _P, _P, _I64, _P, ctypes.c_int]
     L.kd_store_cdf.argtypes = [_P, _P, _P, _I64, _P, ctypes.c_int]
+    L.kd_store_query_batch.argtypes = [_P, _P, _P, _I64, _P, _P, _P, _I64, _P, ctypes.c_int]
+    L.kd_grouped_compress.argtypes = [_P, ctypes.c_int, _D, _I64, _P, _P, _I64, _P, _P, _P, _P,
+                                      _P, _P, _P, _I64, ctypes.POINTER(_I64), _P, _P]
+    L.kd_quantile.argtypes = [_P, _P, _I64, _P, _P, _P, _P, _P, _P, _I64, _P, ctypes.c_int]
+    L.kd_cdf.argtypes = [_P, _P, _I64, _P, _P, _P, _P, _P, _P, _I64, _P, ctypes.c_int]
+    L.kd_merge.argtypes = [_P, ctypes.c_int, _D, _P, _I64, _P, _P, _P, _I64, _P, _P, _P, _P, _I64,
+                           ctypes.POINTER(_I64)]
     L.kd_store_merge.argtypes = [_P, _P, _P, _P, _I64]
     L.kd_store_get_digest.argtypes = [_P, ctypes.c_uint32, _P, _P, _P, _I64, ctypes.POINTER(_I64)]
     L.kd_store_set_digest.argtypes = [_P, ctypes.c_uint32, _P, _P, _P, _I64]

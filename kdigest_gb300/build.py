@@ -19,8 +19,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libkdigest_gb300.so")
 
 SOURCES = ["kd_pipeline.cu", "kd_capi.cu", "kd_noalloc.cu", "kd_server.cu", "kd_serde.cu",
-           "kd_keymap.cu", "kd_spath.cu"]
-HEADERS = ["kd_math.h", "kd_internal.cuh", "kd_scan.cuh", "kd_sort.cuh", "kd_engine.h"]
+           "kd_keymap.cu", "kd_spath.cu", "kd_stateless.cu"]
+HEADERS = ["kd_math.h", "kd_internal.cuh", "kd_scan.cuh", "kd_sort.cuh", "kd_engine.h", "kd_query.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -55,6 +55,8 @@ static void dfree(KdSession* s, void* p, size_t bytes) {
   if (bytes == 0) bytes = 16;
   s->mem_used -= std::min(s->mem_used, bytes);
 }
+int kd_dalloc(KdSession* s, void** p, size_t bytes) { return dalloc(s, p, bytes); }
+void kd_dfree(KdSession* s, void* p, size_t bytes) { dfree(s, p, bytes); }
 
 void kd_ws_free(KdWorkspace& w) {
   void* ptrs[] = {w.k64[0], w.k64[1], w.key[0], w.key[1], w.idx[0], w.idx[1], w.ghist,
@@ -306,6 +308,10 @@ void kd_store_drop_graphs(KdStore* st) {
       g = KdGraphEntry();
     }
   st->last_eager = KdGraphKey();
+  if (st->q_graph) cudaGraphExecDestroy(st->q_graph);
+  st->q_graph = nullptr;
+  st->q_graph_args = KdQueryArgs();
+  st->q_last = KdQueryArgs();
 }
 
 void kd_store_free(KdStore* st) {
@@ -420,6 +426,12 @@ KD_API void kd_session_destroy(kd_session* h) {
     kd_store_free(s->scratch_store);
     delete s->scratch_store;
   }
+  if (s->scratch_many) {
+    kd_store_free(s->scratch_many);
+    delete s->scratch_many;
+  }
+  if (s->sl_buf) cudaFree(s->sl_buf);
+  s->sl_buf = nullptr;
   if (s->ws.d_in) cudaFree(s->ws.d_in);
   s->ws.d_in = nullptr;
   kd_ws_free(s->ws);
@@ -699,6 +711,49 @@ KD_API int kd_store_quantile(kd_store* h, const uint32_t* keys, const double* qs
 KD_API int kd_store_cdf(kd_store* h, const uint32_t* keys, const double* xs, int64_t nx,
                         double* out, int flags) {
   return query_common(h, keys, xs, nx, out, flags, 1);
+}
+
+KD_API int kd_store_query_batch(kd_store* h, const uint32_t* qkeys, const double* qs, int64_t nq,
+                                double* qout, const uint32_t* ckeys, const double* xs, int64_t nc,
+                                double* cout, int flags) {
+  if (!h) return KD_EINVAL;
+  KdStore* st = &h->st;
+  KdSession* s = st->sess;
+  if (!s) return KD_EINVAL;  // the store's session was destroyed
+  if (nq < 0 || nc < 0 || (nq > 0 && (!qs || !qout)) || (nc > 0 && (!xs || !cout)))
+    return fail(s, KD_EINVAL, "null query arrays");
+  if (nq + nc == 0) return KD_OK;
+  cudaSetDevice(s->device);
+  int frc = kd_spath_flush(s, st);  // quantile / cdf run merge() first (tdigest.mojo:493,542)
+  if (frc) return frc;
+  if (flags & KD_PTR_DEVICE) return kd_pipeline_query2(s, st, qkeys, qs, nq, qout, ckeys, xs, nc, cout);
+  const size_t kq = qkeys ? ((size_t)nq * 4 + 15) / 16 * 16 : 0;
+  const size_t kc = ckeys ? ((size_t)nc * 4 + 15) / 16 * 16 : 0;
+  int rc = stage_in(s, kq + kc + (size_t)(nq + nc) * 16);
+  if (rc) return rc;
+  char* base = (char*)s->ws.d_in;
+  const uint32_t* dqk = nullptr;
+  const uint32_t* dck = nullptr;
+  if (qkeys) {
+    KD_CK(cudaMemcpyAsync(base, qkeys, (size_t)nq * 4, cudaMemcpyHostToDevice, s->stream));
+    dqk = (const uint32_t*)base;
+  }
+  if (ckeys) {
+    KD_CK(cudaMemcpyAsync(base + kq, ckeys, (size_t)nc * 4, cudaMemcpyHostToDevice, s->stream));
+    dck = (const uint32_t*)(base + kq);
+  }
+  double* dq = (double*)(base + kq + kc);
+  double* dx = dq + nq;
+  double* dqo = dx + nc;
+  double* dco = dqo + nq;
+  if (nq) KD_CK(cudaMemcpyAsync(dq, qs, (size_t)nq * 8, cudaMemcpyHostToDevice, s->stream));
+  if (nc) KD_CK(cudaMemcpyAsync(dx, xs, (size_t)nc * 8, cudaMemcpyHostToDevice, s->stream));
+  int qrc = kd_pipeline_query2(s, st, dqk, dq, nq, dqo, dck, dx, nc, dco);
+  if (qrc == KD_ECUDA) return qrc;
+  if (nq) KD_CK(cudaMemcpyAsync(qout, dqo, (size_t)nq * 8, cudaMemcpyDeviceToHost, s->stream));
+  if (nc) KD_CK(cudaMemcpyAsync(cout, dco, (size_t)nc * 8, cudaMemcpyDeviceToHost, s->stream));
+  KD_CK(cudaStreamSynchronize(s->stream));
+  return qrc;
 }
 
 KD_API int kd_store_merge(kd_store* dst, kd_store* src, const int64_t* group_offsets,

@@ -217,6 +217,9 @@ struct KdSession {
   long long cap_many = 0;
   KdStageStats stats;
   struct KdStore* scratch_store = nullptr;  // 1-key store for stateless compress
+  struct KdStore* scratch_many = nullptr;   // K-key store for the stateless grouped calls
+  void* sl_buf = nullptr;                   // device working memory of the stateless calls
+  size_t sl_bytes = 0;
   std::vector<struct KdStore*> stores;         // live stores of this session
   std::vector<struct kd_server*> servers;      // live serving loops over them
   std::vector<struct kd_keymap*> keymaps;      // live key dictionaries
@@ -256,6 +259,18 @@ struct KdGraphEntry {
 };
 #define KD_GRAPH_CACHE 4
 
+// Arguments of a batched quantile + cdf call; the same arguments twice in a row
+// capture the call (one kernel and its status copies) as a CUDA graph.
+struct KdQueryArgs {
+  const void* p[6] = {};
+  long long nq = -1, nc = -1;
+  bool operator==(const KdQueryArgs& o) const {
+    for (int i = 0; i < 6; ++i)
+      if (p[i] != o.p[i]) return false;
+    return nq == o.nq && nc == o.nc;
+  }
+};
+
 struct KdStore {
   KdSession* sess = nullptr;
   KdStoreDev d{};
@@ -278,6 +293,8 @@ struct KdStore {
   bool carry = false;
   void* sp_scratch = nullptr;  // working memory of the pass when shared memory is too small
   size_t sp_scratch_bytes = 0;
+  KdQueryArgs q_last, q_graph_args;
+  cudaGraphExec_t q_graph = nullptr;
 };
 
 // The opaque handles of the C-ABI.
@@ -307,6 +324,14 @@ int kd_spath_carry_ingest(KdSession* s, KdStore* st, const double* d_vals, long 
 void kd_spath_free(KdSession* s, KdStore* st);
 int kd_pipeline_quantile(KdSession* s, KdStore* st, const uint32_t* d_keys, const double* d_q,
                          long long nq, double* d_out, int is_cdf);
+// Quantiles (qk/qs/qout, nq) and cdfs (ck/xs/cout, nc) of a store in one
+// kernel launch, device pointers; captured as a graph when the same arguments
+// recur.
+int kd_pipeline_query2(KdSession* s, KdStore* st, const uint32_t* qk, const double* qs, long long nq,
+                       double* qout, const uint32_t* ck, const double* xs, long long nc, double* cout);
+// Session device memory with budget accounting (kd_capi.cu).
+int kd_dalloc(KdSession* s, void** p, size_t bytes);
+void kd_dfree(KdSession* s, void* p, size_t bytes);
 int kd_pipeline_merge(KdSession* s, KdStore* dst, KdStore* src, const long long* h_group_off,
                       const uint32_t* h_parts, long long ngroups);
 int kd_store_alloc(KdSession* s, KdStore* st);

@@ -27,6 +27,7 @@
 
 #include "kd_engine.h"
 #include "kd_internal.cuh"
+#include "kd_query.cuh"
 #include "kd_scan.cuh"
 #include "kd_sort.cuh"
 
@@ -1839,123 +1840,57 @@ __global__ void __launch_bounds__(256) k_commit_warp(CommitArgs a) {
 // Queries: TDigest.quantile / cdf (tdigest.mojo:485-587) with binary searches
 // over the committed prefix (bit-identical to the reference's serial walk).
 // ---------------------------------------------------------------------------
+// One (key, q | x) query against a resident digest; NaN and the error word on
+// failure (key out of range, q outside [0, 1], empty digest).
+__device__ __forceinline__ double store_query(const KdStoreDev& s, uint32_t key, double q, bool is_cdf,
+                                              KdErrHost* err, long long i) {
+  const double nan = kd_from_bits(0x7ff8000000000000ULL);
+  if ((long long)key >= s.K || (!is_cdf && !(q >= 0.0 && q <= 1.0))) {
+    kd_err_set(err, KD_EINVAL, i);
+    return nan;
+  }
+  const int nc = s.count[key];
+  if (nc == 0) {
+    kd_err_set(err, KD_EEMPTY, i);
+    return nan;
+  }
+  const int b = s.cur[key];
+  KdQueryDigest d;
+  d.m = s.slot_m + slot_base(s.K, b, key);
+  d.w = s.slot_w + slot_base(s.K, b, key);
+  d.P = s.prefix + (size_t)key * KD_TILE;
+  d.nc = nc;
+  d.n = s.total[key];
+  d.mn = s.min_v[key];
+  d.mx = s.max_v[key];
+  d.scaled = s.lambda > 0.0;
+  d.dfac = s.dfac[key];
+  d.single = 1.0 + 1e-9;  // tdigest.mojo:481-483 (effective weight)
+  return is_cdf ? kd_cdf_one(d, q) : kd_quantile_one(d, q);
+}
+
 __global__ void k_query(KdStoreDev s, const uint32_t* __restrict__ keys, const double* __restrict__ qx,
                         long long nq, double* __restrict__ out, int is_cdf, KdErrHost* err) {
-  const double nan = kd_from_bits(0x7ff8000000000000ULL);
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nq;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = store_query(s, keys ? keys[i] : 0u, qx[i], is_cdf != 0, err, i);
+}
+
+// Quantile and cdf queries of one call in one launch: indices [0, nq) are the
+// quantiles, [nq, nq + nc) the cdfs.
+__global__ void k_query2(KdStoreDev s, const uint32_t* __restrict__ qk, const double* __restrict__ qs,
+                         long long nq, double* __restrict__ qout, const uint32_t* __restrict__ ck,
+                         const double* __restrict__ xs, long long nc, double* __restrict__ cout,
+                         KdErrHost* err) {
+  const long long tot = nq + nc;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot;
        i += (long long)gridDim.x * blockDim.x) {
-    const uint32_t key = keys ? keys[i] : 0u;
-    const double q = qx[i];
-    if ((long long)key >= s.K) {
-      kd_err_set(err, KD_EINVAL, i);
-      out[i] = nan;
-      continue;
-    }
-    if (!is_cdf && !(q >= 0.0 && q <= 1.0)) {
-      kd_err_set(err, KD_EINVAL, i);
-      out[i] = nan;
-      continue;
-    }
-    const int nc = s.count[key];
-    if (nc == 0) {
-      kd_err_set(err, KD_EEMPTY, i);
-      out[i] = nan;
-      continue;
-    }
-    const int b = s.cur[key];
-    const double* m = s.slot_m + slot_base(s.K, b, key);
-    const double* w = s.slot_w + slot_base(s.K, b, key);
-    const double* P = s.prefix + (size_t)key * KD_TILE;
-    const double n = s.total[key];
-    const double mn = s.min_v[key], mx = s.max_v[key];
-    const bool decay = s.lambda > 0.0;
-    const double dfac = s.dfac[key];
-    double r;
-    if (!is_cdf) {
-      if (nc == 1) {
-        r = m[0];
-      } else if (q <= 0.0) {
-        r = mn;
-      } else if (q >= 1.0) {
-        r = mx;
-      } else {
-        const double target = KD_MUL(q, n);
-        const double w0 = w[0];
-        const double first_half = KD_MUL(w0, 0.5);
-        const double wl = w[nc - 1], ml = m[nc - 1];
-        const double last_half = KD_MUL(wl, 0.5);
-        if (target < first_half) {
-          const double eff = decay ? KD_MUL(w0, dfac) : w0;
-          r = eff <= 1.0 + 1e-9 ? mn : KD_ADD(mn, KD_MUL(KD_SUB(m[0], mn), KD_DIV(target, first_half)));
-        } else if (target > KD_SUB(n, last_half)) {
-          const double eff = decay ? KD_MUL(wl, dfac) : wl;
-          if (eff <= 1.0 + 1e-9) {
-            r = mx;
-          } else {
-            const double frac = KD_DIV(KD_SUB(target, KD_SUB(n, last_half)), last_half);
-            r = KD_ADD(ml, KD_MUL(KD_SUB(mx, ml), frac));
-          }
-        } else {
-          int lo = 1, hi = nc;  // first p in [1, nc-1] with P[p] >= target
-          while (lo < hi) {
-            int mid = (lo + hi) >> 1;
-            if (P[mid] >= target) hi = mid;
-            else lo = mid + 1;
-          }
-          if (lo >= nc) {
-            r = ml;
-          } else {
-            const int k = lo - 1;
-            const double dw = KD_MUL(KD_ADD(w[k], w[k + 1]), 0.5);
-            const double frac = KD_DIV(KD_SUB(target, P[k]), dw);
-            r = KD_ADD(m[k], KD_MUL(KD_SUB(m[k + 1], m[k]), frac));
-          }
-        }
-      }
+    if (i < nq) {
+      qout[i] = store_query(s, qk ? qk[i] : 0u, qs[i], false, err, i);
     } else {
-      const double x = q;
-      if (x < mn) {
-        r = 0.0;
-      } else if (x > mx) {
-        r = 1.0;
-      } else if (nc == 1) {
-        r = x < m[0] ? 0.0 : (x > m[0] ? 1.0 : 0.5);
-      } else if (x < m[0]) {
-        if (mn == m[0]) r = 0.0;
-        else {
-          const double frac = KD_DIV(KD_SUB(x, mn), KD_SUB(m[0], mn));
-          r = KD_DIV(KD_MUL(KD_MUL(w[0], 0.5), frac), n);
-        }
-      } else if (x > m[nc - 1]) {
-        const double ml = m[nc - 1], wl = w[nc - 1];
-        if (mx == ml) r = 1.0;
-        else {
-          const double frac = KD_DIV(KD_SUB(x, ml), KD_SUB(mx, ml));
-          const double hl = KD_MUL(wl, 0.5);
-          r = KD_DIV(KD_ADD(KD_SUB(n, hl), KD_MUL(hl, frac)), n);
-        }
-      } else {
-        int lo = 1, hi = nc;  // first p in [1, nc-1] with x <= m[p]
-        while (lo < hi) {
-          int mid = (lo + hi) >> 1;
-          if (x <= m[mid]) hi = mid;
-          else lo = mid + 1;
-        }
-        if (lo >= nc) {
-          r = 1.0;
-        } else {
-          const int k = lo - 1;
-          const double dw = KD_MUL(KD_ADD(w[k], w[k + 1]), 0.5);
-          if (m[k + 1] == m[k]) {
-            r = KD_DIV(KD_ADD(P[k], KD_MUL(dw, 0.5)), n);
-          } else {
-            const double frac = KD_DIV(KD_SUB(x, m[k]), KD_SUB(m[k + 1], m[k]));
-            r = KD_DIV(KD_ADD(P[k], KD_MUL(dw, frac)), n);
-          }
-        }
-      }
+      const long long j = i - nq;
+      cout[j] = store_query(s, ck ? ck[j] : 0u, xs[j], true, err, i);
     }
-    out[i] = r;
   }
 }
 
@@ -2809,6 +2744,65 @@ int kd_pipeline_quantile(KdSession* s, KdStore* st, const uint32_t* d_keys, cons
   k_query<<<grid, 256, 0, str>>>(st->d, d_keys, d_q, nq, d_out, is_cdf, w.err);
   KD_CK(cudaGetLastError());
   KD_CK(cudaMemcpyAsync(w.h_err, w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, str));
+  KD_CK(cudaStreamSynchronize(str));
+  if (w.h_err->code) {
+    char buf[256];
+    snprintf(buf, sizeof buf, "%s (query %lld)", err_text(w.h_err->code), w.h_err->index);
+    kd_set_msg(s, buf);
+    return w.h_err->code;
+  }
+  return KD_OK;
+}
+
+int kd_pipeline_query2(KdSession* s, KdStore* st, const uint32_t* qk, const double* qs, long long nq,
+                       double* qout, const uint32_t* ck, const double* xs, long long nc, double* cout) {
+  if (nq + nc <= 0) return KD_OK;
+  int rc = s->ws.err ? KD_OK : kd_ws_reserve(s, 1, 1, 64, 64, 64, 1);
+  if (rc) return rc;
+  KdWorkspace& w = s->ws;
+  cudaStream_t str = s->stream;
+  *w.h_err = KdErrHost{0, 0, -1};
+  const int grid = (int)std::min<long long>((nq + nc + 255) / 256, (long long)s->num_sms * 32);
+  // the status reset, the one kernel, the status read-back
+  auto enqueue = [&]() {
+    cudaMemcpyAsync(w.err, w.h_err, sizeof(KdErrHost), cudaMemcpyHostToDevice, str);
+    k_query2<<<grid, 256, 0, str>>>(st->d, qk, qs, nq, qout, ck, xs, nc, cout, w.err);
+    cudaMemcpyAsync(w.h_err, w.err, sizeof(KdErrHost), cudaMemcpyDeviceToHost, str);
+  };
+  KdQueryArgs args;
+  const void* ps[6] = {qk, qs, qout, ck, xs, cout};
+  for (int i = 0; i < 6; ++i) args.p[i] = ps[i];
+  args.nq = nq;
+  args.nc = nc;
+  bool ran = false;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (s->use_graphs && cudaStreamIsCapturing(str, &cs) == cudaSuccess &&
+      cs == cudaStreamCaptureStatusNone) {
+    if (!(st->q_graph && st->q_graph_args == args) && args == st->q_last) {
+      if (st->q_graph) cudaGraphExecDestroy(st->q_graph);
+      st->q_graph = nullptr;
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(str, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        enqueue();
+        if (cudaStreamEndCapture(str, &g) == cudaSuccess && g) {
+          cudaGraphExec_t ex = nullptr;
+          if (cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
+            st->q_graph = ex;
+            st->q_graph_args = args;
+          }
+        }
+        if (g) cudaGraphDestroy(g);
+      }
+      cudaGetLastError();  // a failed capture leaves the eager path below
+    }
+    if (st->q_graph && st->q_graph_args == args) {
+      KD_CK(cudaGraphLaunch(st->q_graph, str));
+      ran = true;
+    }
+  }
+  if (!ran) enqueue();
+  st->q_last = args;
+  KD_CK(cudaGetLastError());
   KD_CK(cudaStreamSynchronize(str));
   if (w.h_err->code) {
     char buf[256];

@@ -505,6 +505,113 @@ def merge_digests(dst: TDigest, parts) -> None:
     dst._store.merge_from(tmp, [0, len(parts)], np.arange(len(parts), dtype=np.uint32))
 
 
+# ---------------------------------------------------------------------------
+# Stateless calls over caller-held centroid arrays (the reference's GPU entry
+# points, which its host-side digests call with their centroids)
+# ---------------------------------------------------------------------------
+def _csr(parts):
+    offs = np.zeros(len(parts) + 1, np.int64)
+    offs[1:] = np.cumsum([len(p) for p in parts])
+    cat = np.concatenate([np.asarray(p, np.float64) for p in parts]) if offs[-1] else np.zeros(1)
+    return offs, np.ascontiguousarray(cat)
+
+
+def _split(offs, m, w):
+    return ([m[offs[k]:offs[k + 1]].copy() for k in range(len(offs) - 1)],
+            [w[offs[k]:offs[k + 1]].copy() for k in range(len(offs) - 1)])
+
+
+def gpu_grouped_compress_weighted(keys, values, new_weights, prior_means, prior_weights,
+                                  num_keys: int, compression: float, scale: int = K2,
+                                  session: GpuSession | None = None):
+    """gpu_grouped_compress_weighted (gpu/grouped.mojo:415-643): per key, the
+    P-path compress of its prior centroids followed by its new samples (weight
+    new_weights[k]).  Returns (means per key, weights per key, mins, maxs), the
+    ranges over each key's new samples only, like GroupedResult."""
+    s = session or default_session()
+    k = np.ascontiguousarray(keys, dtype=np.uint32)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    nw = None if new_weights is None else np.ascontiguousarray(new_weights, dtype=np.float64)
+    po, pm = _csr(prior_means)
+    _, pw = _csr(prior_weights)
+    out_off = np.zeros(num_keys + 1, np.int64)
+    mins = np.zeros(num_keys)
+    maxs = np.zeros(num_keys)
+    cap = int(po[-1] + len(v))
+    om = np.empty(max(cap, 1))
+    ow = np.empty(max(cap, 1))
+    out_n = ctypes.c_int64(0)
+    rc = N.load().kd_grouped_compress(s.handle, scale, compression, num_keys, N.ptr(k), N.ptr(v),
+                                      len(v), N.ptr(nw) if nw is not None else None, N.ptr(po),
+                                      N.ptr(pm), N.ptr(pw), N.ptr(out_off), N.ptr(om), N.ptr(ow),
+                                      cap, ctypes.byref(out_n), N.ptr(mins), N.ptr(maxs))
+    _check(s.handle, rc)
+    means, weights = _split(out_off, om, ow)
+    return means, weights, mins, maxs
+
+
+def _digest_query(fn, means, weights, mins, maxs, ids, xs, session):
+    s = session or default_session()
+    offs, m = _csr(means)
+    _, w = _csr(weights)
+    mn = np.ascontiguousarray(mins, dtype=np.float64)
+    mx = np.ascontiguousarray(maxs, dtype=np.float64)
+    x = np.ascontiguousarray(xs, dtype=np.float64)
+    k = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint32)
+    out = np.empty(len(x))
+    rc = fn(s.handle, N.ptr(offs), len(means), N.ptr(m), N.ptr(w), N.ptr(mn), N.ptr(mx),
+            N.ptr(k) if k is not None else None, N.ptr(x), len(x), N.ptr(out), 0)
+    _check(s.handle, rc)
+    return out
+
+
+def gpu_quantile(means, weights, qs, min_v: float, max_v: float,
+                 session: GpuSession | None = None) -> np.ndarray:
+    """gpu_quantile (gpu/query.mojo:320-330): every q against one digest."""
+    return _digest_query(N.load().kd_quantile, [means], [weights], [min_v], [max_v], None, qs, session)
+
+
+def gpu_cdf(means, weights, xs, min_v: float, max_v: float,
+            session: GpuSession | None = None) -> np.ndarray:
+    """gpu_cdf (gpu/query.mojo:333-342): every x against one digest."""
+    return _digest_query(N.load().kd_cdf, [means], [weights], [min_v], [max_v], None, xs, session)
+
+
+def gpu_quantile_many(means, weights, mins, maxs, ids, qs, session: GpuSession | None = None):
+    """gpu_quantile for many caller-held digests in one call: query i against
+    digest ids[i]."""
+    return _digest_query(N.load().kd_quantile, means, weights, mins, maxs, ids, qs, session)
+
+
+def gpu_cdf_many(means, weights, mins, maxs, ids, xs, session: GpuSession | None = None):
+    return _digest_query(N.load().kd_cdf, means, weights, mins, maxs, ids, xs, session)
+
+
+def gpu_merge_digests(part_means, part_weights, compression: float, scale: int = K2,
+                      group_offsets=None, session: GpuSession | None = None):
+    """gpu_merge_digests (gpu/query.mojo:348-369): the parts' centroids
+    concatenated in order and compressed once.  With group_offsets, each group
+    of consecutive parts is merged on its own and a list per group returned."""
+    s = session or default_session()
+    po, m = _csr(part_means)
+    _, w = _csr(part_weights)
+    go = np.array([0, len(part_means)] if group_offsets is None else group_offsets, np.int64)
+    ng = len(go) - 1
+    out_off = np.zeros(ng + 1, np.int64)
+    cap = max(int(po[-1]), 1)
+    om = np.empty(cap)
+    ow = np.empty(cap)
+    out_n = ctypes.c_int64(0)
+    rc = N.load().kd_merge(s.handle, scale, compression, N.ptr(po), len(part_means), N.ptr(m),
+                           N.ptr(w), N.ptr(go), ng, None, N.ptr(out_off), N.ptr(om), N.ptr(ow),
+                           cap, ctypes.byref(out_n))
+    _check(s.handle, rc)
+    means, weights = _split(out_off, om, ow)
+    if group_offsets is None:
+        return means[0], weights[0]
+    return means, weights
+
+
 class GroupedTDigest:
     """num_keys independent digests updated together (grouped.mojo:30-190)."""
 
@@ -610,6 +717,36 @@ class GroupedTDigest:
 
     def cdfs(self, keys, xs) -> np.ndarray:
         return self._store.query(self._check_keys(keys), xs, True)
+
+    def query_batch(self, qkeys, qs, ckeys, xs):
+        """quantiles(qkeys, qs) and cdfs(ckeys, xs) in one kernel launch.
+        Host arrays return numpy arrays; CUDA tensors (uint32 / int32 keys,
+        float64 values) are read and written in place, returning two CUDA
+        tensors, and a repeated call with the same tensors replays a captured
+        CUDA graph."""
+        L = N.load()
+        h = self._store._h
+        if getattr(qs, "is_cuda", False):
+            import torch
+
+            qo = torch.empty_like(qs)
+            co = torch.empty_like(xs)
+            torch.cuda.current_stream(qs.device).synchronize()
+            rc = L.kd_store_query_batch(h, qkeys.data_ptr(), qs.data_ptr(), qs.numel(), qo.data_ptr(),
+                                        ckeys.data_ptr(), xs.data_ptr(), xs.numel(), co.data_ptr(),
+                                        N.KD_PTR_DEVICE)
+            _check(self.session.handle, rc)
+            return qo, co
+        qk = self._check_keys(qkeys)
+        ck = self._check_keys(ckeys)
+        q = np.ascontiguousarray(qs, dtype=np.float64)
+        x = np.ascontiguousarray(xs, dtype=np.float64)
+        qo = np.empty(len(q))
+        co = np.empty(len(x))
+        rc = L.kd_store_query_batch(h, N.ptr(qk), N.ptr(q), len(q), N.ptr(qo), N.ptr(ck), N.ptr(x),
+                                    len(x), N.ptr(co), 0)
+        _check(self.session.handle, rc)
+        return qo, co
 
     def to_bytes(self, key: int) -> bytes:
         return self._store.to_bytes(self._key(key))
