@@ -280,6 +280,11 @@ C1_X = (-3.0, -1.0, 0.0, 1.0, 3.0)
 
 
 def run_config1(args) -> int:
+    print(json.dumps(config1_line(args)), flush=True)
+    return 0
+
+
+def config1_line(args) -> dict:
     import torch
 
     import kdigest_gb300 as kd
@@ -320,7 +325,11 @@ def run_config1(args) -> int:
                 reps.append(e0.elapsed_time(e1))
         return statistics.median(reps), d
 
+    sampler = ClockSampler(0)
+    sampler.start()
     ms, d = stream(True)
+    clocks = sampler.stop()
+    clocks["region"] = "the timed whole-stream passes of the single-sample path"
     ms_p, dp = stream(False)
     # the same stream with count decay (half-life 10^5 samples): non-integral
     # weights take the speculate-and-verify sweep and the per-sample clock chain
@@ -365,6 +374,10 @@ def run_config1(args) -> int:
         cpu = {"value": C1_TOTAL / dt, "unit": "samples/s", "cores": 1, "kind": "port",
                "sample": f"the whole stream through the oracle's sequential add loop in C "
                          f"({dt:.2f} s)"}
+    peaks = measured_peaks()
+    # compulsory bytes: every sample read once (8 B); the digest (about 60
+    # centroids and a 500-sample buffer) stays on chip across a call
+    c1_gbs = 8 * C1_TOTAL / (ms / 1e3) / 1e9
     line = {
         "metric": "single-digest ingest samples/s (K1 d100, batches of 4096)",
         "value": C1_TOTAL / (ms / 1e3), "unit": "samples/s", "n_gpus": 1, "steps": 3,
@@ -375,10 +388,20 @@ def run_config1(args) -> int:
                                "reference's path for this batch size, the add loop",
                    "batch": C1_BATCH},
         "bit_exact_vs_reference_loop": parity,
+        "parity_vs_oracle": parity,
+        "roofline": {"bound": "hbm", "kernel": "k_spath (one launch per call)",
+                     "achieved": round(c1_gbs, 3), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(c1_gbs / peaks["hbm_gbs"], 6), "traffic": None,
+                     "algorithmic_bytes_per_sample": 8,
+                     "note": "a sequential sweep per merge pass (latency of dependent FP64 "
+                             "operations), far from any bandwidth limit"},
+        "plain_form": {"value": C1_TOTAL / (ms / 1e3), "unit": "samples/s",
+                       "sample": "the same: one digest, one launch per call of 4096 samples, no graph"},
+        "gpu_launches": (C1_TOTAL + C1_BATCH - 1) // C1_BATCH,
+        "clocks": clocks,
         "accuracy": out, "cpu_baseline": cpu,
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 # ----------------------------------------------------------------------------
@@ -466,6 +489,11 @@ def c2_queries(seed: int = SEED + 2):
 
 
 def run_config2(args) -> int:
+    print(json.dumps(config2_line(args)), flush=True)
+    return 0
+
+
+def config2_line(args) -> dict:
     import torch
 
     import kdigest_gb300 as kd
@@ -545,6 +573,32 @@ def run_config2(args) -> int:
     del dp
     value = steps * C2_BATCH / (pipe_ms / 1e3)
 
+    # plain form: one digest per call with graphs off, on the first batches
+    plain = None
+    if not args.no_plain:
+        sess_p = kd.GpuSession()
+        sess_p.set_option(N.KD_OPT_GRAPHS, 0)
+        d0 = kd.TDigest(200.0, kd.K2, decay=kd.Decay.half_life(1e6), session=sess_p)
+        h0 = d0._store._h
+        extp = torch.cuda.ExternalStream(sess_p.stream, device=dev)
+        pt = []
+        for b in range(min(nb, args.warmup + 16)):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(extp)
+            rc = L.kd_store_ingest(h0, None, vals.data_ptr() + b * C2_BATCH * 8, C2_BATCH,
+                                   N.KD_CLOCK_COUNT, 0.0, N.KD_PTR_DEVICE)
+            e1.record(extp)
+            e1.synchronize()
+            if rc:
+                raise kd.KdError(rc, L.kd_last_error(sess_p.handle).decode())
+            if b >= args.warmup:
+                pt.append(e0.elapsed_time(e1))
+        plain = {"value": len(pt) * C2_BATCH / (sum(pt) / 1e3), "unit": "samples/s",
+                 "sample": f"batches {args.warmup}..{args.warmup + len(pt) - 1}, one kd_store_ingest "
+                           "per batch, CUDA graphs off"}
+        del d0, sess_p
+
     qs = c2_queries()
     dq = torch.from_numpy(qs).to(dev)
     dout = torch.empty_like(dq)
@@ -599,6 +653,14 @@ def run_config2(args) -> int:
             gm, gw = d.centroids()
             cpu["centroids_bit_identical"] = bool(np.array_equal(om, gm) and np.array_equal(ow, gw))
 
+    peaks = measured_peaks()
+    # compulsory bytes per batch: every new value read once (8 B), the digest's
+    # prior and new centroids once each (16 B) and its header twice
+    c2_bytes = 8 * C2_BATCH + 16 * 2 * len(d) + 96
+    c2_gbs = c2_bytes / (pipe_ms / steps / 1e3) / 1e9
+    parity = None
+    if cpu is not None and "quantiles_bit_identical" in cpu:
+        parity = bool(cpu["quantiles_bit_identical"] and cpu["centroids_bit_identical"])
     line = {
         "metric": "single-digest ingest samples/s (K2 d200, 1e6-sample half-life)",
         "value": value, "unit": "samples/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
@@ -622,9 +684,16 @@ def run_config2(args) -> int:
                        "queries_4096_max_ppm": round(float(err_all.max()), 1),
                        "reference": "exact sort of all 2^26 samples with their decay weights"},
         "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks,
+        "parity_vs_oracle": parity,
+        "plain_form": plain,
+        "roofline": {"bound": "hbm", "kernel": "whole ingest step", "achieved": round(c2_gbs, 2),
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(c2_gbs / peaks["hbm_gbs"], 5), "traffic": None,
+                     "compulsory_bytes_per_step": c2_bytes,
+                     "note": "one digest per batch: about 30 dependent launches over 1024 tiles, "
+                             "bound by launch latency and FP64 arithmetic, not by HBM"},
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 # ----------------------------------------------------------------------------
@@ -640,6 +709,11 @@ C4_QUERIES = 1 << 24
 
 
 def run_config4(args) -> int:
+    print(json.dumps(config4_line(args)), flush=True)
+    return 0
+
+
+def config4_line(args) -> dict:
     import torch
 
     import kdigest_gb300 as kd
@@ -706,10 +780,38 @@ def run_config4(args) -> int:
     out_c = torch.empty_like(dx)
     ext = torch.cuda.ExternalStream(sess.stream, device=dev)
     h2 = lvl2._store._h
-    tq, tc = [], []
-    for rep in range(6):
-        for fn, k, x, o, acc in ((L.kd_store_quantile, dk, dq, out_q, tq),
-                                 (L.kd_store_cdf, dck, dx, out_c, tc)):
+    # all 2^24 quantile and 2^24 cdf queries in one kd_store_query_batch call:
+    # one kernel launch, captured as a CUDA graph on the second call and
+    # replayed from then on (the timed calls are replays)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    sess.reset_stats()
+    tqc = []
+    sampler = ClockSampler(0)
+    sampler.start()
+    for rep in range(3 + 5):
+        flush.fill_(rep & 0xFF)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        rc = L.kd_store_query_batch(h2, dk.data_ptr(), dq.data_ptr(), C4_QUERIES, out_q.data_ptr(),
+                                    dck.data_ptr(), dx.data_ptr(), C4_QUERIES, out_c.data_ptr(),
+                                    N.KD_PTR_DEVICE)
+        e1.record(ext)
+        e1.synchronize()
+        if rc:
+            raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+        if rep >= 3:
+            tqc.append(e0.elapsed_time(e1))
+    clocks = sampler.stop()
+    clocks["region"] = "the timed query calls"
+    ms_qc = statistics.median(tqc)
+    qps = 2 * C4_QUERIES / (ms_qc / 1e3)
+    # the same queries through the two separate calls, for the split and a check
+    sep = []
+    for fn, k, x, o in ((L.kd_store_quantile, dk, dq, out_q), (L.kd_store_cdf, dck, dx, out_c)):
+        ts = []
+        for rep in range(4):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(ext)
@@ -718,10 +820,18 @@ def run_config4(args) -> int:
             e1.synchronize()
             if rc:
                 raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
-            if rep >= 3:
-                acc.append(e0.elapsed_time(e1))
-    ms_q, ms_c = statistics.median(tq), statistics.median(tc)
-    qps = 2 * C4_QUERIES / ((ms_q + ms_c) / 1e3)
+            if rep >= 1:
+                ts.append(e0.elapsed_time(e1))
+        sep.append(statistics.median(ts))
+    ms_q, ms_c = sep
+    sep_q, sep_c = out_q.clone(), out_c.clone()
+    rc = L.kd_store_query_batch(h2, dk.data_ptr(), dq.data_ptr(), C4_QUERIES, out_q.data_ptr(),
+                                dck.data_ptr(), dx.data_ptr(), C4_QUERIES, out_c.data_ptr(),
+                                N.KD_PTR_DEVICE)
+    if rc:
+        raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+    one_launch_same = bool(torch.equal(sep_q, out_q) and torch.equal(sep_c, out_c))
+    del sep_q, sep_c, flush
     # plain form: one call per group digest (host arrays), on 64 groups
     plain = None
     if not args.no_plain:
@@ -755,12 +865,12 @@ def run_config4(args) -> int:
                "sample": f"the first 2^22 quantile and 2^22 cdf queries ({dt:.2f} s, C oracle, "
                          f"queries split over {threads} threads)"}
     peaks = measured_peaks()
-    qbytes = 20 * C4_QUERIES  # key 4 B + q 8 B + result 8 B per query
-    achieved = qbytes / (ms_q / 1e3) / 1e9
+    qbytes = 2 * 20 * C4_QUERIES  # per query: key 4 B + q or x 8 B + result 8 B
+    achieved = qbytes / (ms_qc / 1e3) / 1e9
     line = {
         "metric": "batched queries/s after a 2^20-digest 32-way merge (K2)",
-        "value": qps, "unit": "queries/s", "n_gpus": 1, "steps": 3, "warmup": 3,
-        "ms_per_step": ms_q + ms_c, "higher_is_better": True, "scaling": "weak",
+        "value": qps, "unit": "queries/s", "n_gpus": 1, "steps": 5, "warmup": 3,
+        "ms_per_step": ms_qc, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (torch device RNG for samples, seeded numpy for shapes and queries)",
         "config": {"workload": "config 4: 2^20 K2 d50 digests of U{64..4096} normal samples, "
@@ -771,18 +881,22 @@ def run_config4(args) -> int:
         "merge": {"level1_s": round(m1, 4), "level2_s": round(m2, 4),
                   "digests_per_s": (C4_DIGESTS + C4_DIGESTS // 32) / (m1 + m2),
                   "centroids_in_level1": cent_in},
-        "queries": {"quantile_ms": round(ms_q, 4), "cdf_ms": round(ms_c, 4),
-                    "launches": "one kernel per call"},
-        "roofline": {"bound": "hbm", "kernel": "k_query (quantile)", "achieved": round(achieved, 1),
+        "queries": {"both_ms": round(ms_qc, 4), "launches": "one kernel (k_query2) per step, "
+                    "replayed from a captured CUDA graph",
+                    "separate_calls_ms": {"quantile": round(ms_q, 4), "cdf": round(ms_c, 4)}},
+        "gpu_launches": 5,
+        "one_launch_equals_two_calls": one_launch_same,
+        "clocks": clocks,
+        "roofline": {"bound": "hbm", "kernel": "k_query2", "achieved": round(achieved, 1),
                      "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
                      "algorithmic_bytes": qbytes},
         "cpu_baseline": cpu,
         "queries_bit_identical_to_oracle": parity,
+        "parity_vs_oracle": parity,
         "plain_form": plain,
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 # ----------------------------------------------------------------------------
@@ -797,14 +911,30 @@ SERVE_RATE = 20_000.0
 SERVE_POOL = 1 << 25
 
 
+_SERVE_ZIPF = {}
+
+
+def _serve_zipf(num_keys: int, seed: int = SEED + 5):
+    """Zipf(1.2) key-rank CDF and the seeded rank -> id permutation of the
+    serving keys."""
+    if num_keys not in _SERVE_ZIPF:
+        rng = np.random.default_rng(seed)
+        p = 1.0 / np.arange(1, num_keys + 1, dtype=np.float64) ** 1.2
+        cdf = np.cumsum(p)
+        cdf /= cdf[-1]
+        _SERVE_ZIPF[num_keys] = (cdf, rng.permutation(num_keys).astype(np.uint32))
+    return _SERVE_ZIPF[num_keys]
+
+
+def serve_zipf_keys(rng, n: int, num_keys: int = SERVE_KEYS) -> np.ndarray:
+    cdf, perm = _serve_zipf(num_keys)
+    return perm[np.minimum(np.searchsorted(cdf, rng.random(n), side="right"), num_keys - 1)]
+
+
 def make_serve_pool(seed: int = SEED + 5, num_keys: int = SERVE_KEYS, size: int = SERVE_POOL):
     """Pairs that ingest requests take slices of (keys Zipf(1.2) over a seeded
     rank->id permutation, values lognormal(0, 2))."""
-    rng = np.random.default_rng(seed)
-    p = 1.0 / np.arange(1, num_keys + 1, dtype=np.float64) ** 1.2
-    cdf = np.cumsum(p)
-    cdf /= cdf[-1]
-    perm = rng.permutation(num_keys).astype(np.uint32)
+    cdf, perm = _serve_zipf(num_keys, seed)
     keys = np.empty(size, np.uint32)
     vals = np.empty(size, np.float64)
     parts = max(1, min(32, size >> 20))
@@ -839,9 +969,23 @@ def make_serve_trace(seconds: float, rate: float = SERVE_RATE, seed: int = SEED 
         rng.lognormal(np.log(4096.0), 1.0, m)))), rng.integers(1, 1025, m)).astype(np.int64)
     offs = (rng.random(m) * (pool - sizes)).astype(np.int64)
     nq = int(sizes[~ingest].sum())
-    qkeys = rng.integers(0, num_keys, nq).astype(np.uint32)
+    # Query requests alternate between two key populations: keys uniform over
+    # all 10^6 (most never ingested: such a pair completes with KD_EEMPTY and
+    # NaN) and keys drawn like the ingest keys, Zipf(1.2), which exist.
+    qpop = np.zeros(m, np.int8)
+    qidx = np.flatnonzero(~ingest)
+    qpop[qidx[1::2]] = 1
+    qkeys = np.empty(nq, np.uint32)
+    qo = 0
+    for i in qidx:
+        n = int(sizes[i])
+        if qpop[i]:
+            qkeys[qo:qo + n] = serve_zipf_keys(rng, n, num_keys)
+        else:
+            qkeys[qo:qo + n] = rng.integers(0, num_keys, n)
+        qo += n
     qvals = rng.random(nq)
-    return arr, ingest, sizes, offs, qkeys, qvals
+    return arr, ingest, sizes, offs, qkeys, qvals, qpop
 
 
 def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
@@ -854,7 +998,7 @@ def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
                               session=sess)
     srv = kd.Server(store, window=window, budget_bytes=100 << 30)
     pk, pv = make_serve_pool()
-    arr, ingest, sizes, offs, qkeys, qvals = make_serve_trace(seconds, rate)
+    arr, ingest, sizes, offs, qkeys, qvals, qpop = make_serve_trace(seconds, rate)
     tickets = []
     lag = 0.0
     qo = 0
@@ -878,11 +1022,28 @@ def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
     srv.flush()
     t_all = time.perf_counter() - t0
     st = srv.stats()
+    mem = srv.memory()
     statuses = {}
-    for tk in tickets:
+    lat = np.empty(len(tickets))
+    for i, tk in enumerate(tickets):
+        lat[i] = srv.latency(tk)
         s, _ = srv.wait(tk, 60.0)
         statuses[s] = statuses.get(s, 0) + 1
     srv.close()
+
+    def pct(sel):
+        x = np.sort(lat[sel])
+        if len(x) == 0:
+            return None
+
+        def r(p):
+            return float(x[min(len(x) - 1, max(0, int(math.ceil(p * len(x))) - 1))]) * 1e3
+
+        return {"requests": int(len(x)), "p50_ms": round(r(0.5), 3), "p99_ms": round(r(0.99), 3),
+                "p999_ms": round(r(0.999), 3)}
+
+    populations = {"ingest": pct(ingest), "query_uniform_keys": pct(~ingest & (qpop == 0)),
+                   "query_ingested_keys": pct(~ingest & (qpop == 1))}
     ing_pairs = int(sizes[ingest].sum())
     q_pairs = int(sizes[~ingest].sum())
     return {
@@ -895,6 +1056,8 @@ def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
         "windows": st["windows"], "gpu_worker_busy_frac": round(st["busy_s"] / t_all, 3),
         "client_max_lag_ms": round(lag * 1e3, 3), "submit_seconds": round(t_sub, 3),
         "status_counts": {str(k): v for k, v in sorted(statuses.items())},
+        "latency_by_population": populations,
+        "device_memory": {"budget_bytes": mem["budget_bytes"], "peak_counted_bytes": mem["peak_bytes"]},
     }
 
 
@@ -1088,13 +1251,13 @@ def run_gpu(args):
     # Dominant stage (kernel group) from the stage events on the launching stream.
     stage_ms = {k: v / max(1, st["ingests"]) for k, v in st["stage_ms"].items()}
     dom = max(stage_ms, key=stage_ms.get)
-    # (16-bit key, value bits) packed into 64 bits; the sort orders the key and
-    # the top 40 value bits in 8-bit digits (7 passes), the unpack repairs the rest
-    passes = 7
+    # Algorithmic bytes of a stage: what any implementation of it must move.
+    # Sorting the batch's (u32 key, f64 value) pairs reads and writes every
+    # 12-byte pair once; level 0 reads every sample and every touched key's
+    # prior centroids and writes its new centroids; prep reads the batch and
+    # writes its sort keys.
     alg = {
-        # one histogram read of the 8 B packed keys for all passes, per pass a read
-        # and a write of every pair, then the unpack (read + write)
-        "sort": (8 + passes * 24 + 24) * BATCH,
+        "sort": 24 * BATCH,
         "level0": 8 * BATCH + touched_avg * 16 * 2 * prior_avg,
         "prep": 12 * BATCH + 12 * BATCH,
     }
@@ -1170,25 +1333,33 @@ def run_gpu(args):
         bounds = np.flatnonzero(np.diff(ks)) + 1
         starts = np.concatenate([[0], bounds])
         ends = np.concatenate([bounds, [len(ks)]])
+        # The reference's per-digest GPU form: gpu_compress_batch of one digest's
+        # input per call (gpu/add_batch.mojo:629-663), here kd_compress with the
+        # key's samples of batch 0 (no prior centroids yet), graphs off.
         d_vs = torch.from_numpy(vs).to(dev)
-        d_ks = torch.from_numpy(np.ascontiguousarray(ks)).to(dev)
-        store3 = kd.GroupedTDigest(NUM_KEYS, COMPRESSION, scale=kd.K3, session=sess)
-        h3 = store3._store._h
+        d_ws = torch.ones_like(d_vs)
+        om = torch.empty(1024, dtype=torch.float64, device=dev)
+        ow = torch.empty(1024, dtype=torch.float64, device=dev)
+        sess_p = kd.GpuSession(local_rank)
+        sess_p.set_option(N.KD_OPT_GRAPHS, 0)
+        out_n = ctypes.c_int64(0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         done = 0
         for s_, e_ in zip(starts, ends):
-            rc = L.kd_store_ingest(h3, d_ks.data_ptr() + int(s_) * 4, d_vs.data_ptr() + int(s_) * 8,
-                                   int(e_ - s_), N.KD_CLOCK_COUNT, 0.0, N.KD_PTR_DEVICE)
+            rc = L.kd_compress(sess_p.handle, kd.K3, COMPRESSION, d_vs.data_ptr() + int(s_) * 8,
+                               d_ws.data_ptr() + int(s_) * 8, int(e_ - s_), N.KD_PTR_DEVICE,
+                               om.data_ptr(), ow.data_ptr(), 1024, ctypes.byref(out_n))
             if rc:
-                raise kd.KdError(rc, L.kd_last_error(sess.handle).decode())
+                raise kd.KdError(rc, L.kd_last_error(sess_p.handle).decode())
             done += int(e_ - s_)
             if time.perf_counter() - t0 > args.plain_seconds:
                 break
         dt = time.perf_counter() - t0
         plain = {"value": done / dt, "unit": "samples/s", "digests": int(np.searchsorted(ends, done, side="right")),
-                 "sample": f"batch 0, one key per call in key order, {done} samples in {dt:.1f} s"}
-        del store3
+                 "sample": f"batch 0, one kd_compress (one digest) per call in key order, CUDA graphs "
+                           f"off, {done} samples in {dt:.1f} s"}
+        del sess_p
 
     cpu = None
     parity = None
@@ -1217,7 +1388,21 @@ def run_gpu(args):
 
     serving = None
     if not args.no_serve and rank == 0 and world == 1:
-        serving = run_serve(args.serve_seconds or 3.0, args.serve_window, args.serve_rate)
+        serving = run_serve(args.serve_seconds or 10.0, args.serve_window, args.serve_rate)
+
+    # The other configs, each measured here with its own baselines and parity
+    # check, as sub-objects of the one line.
+    others = {}
+    if rank == 0 and world == 1 and not args.no_configs:
+        del store
+        torch.cuda.synchronize()
+        for name, fn in (("config1", config1_line), ("config2", config2_line), ("config4", config4_line)):
+            try:
+                others[name] = fn(args)
+            except Exception as e:  # a failing sub-config must not hide the headline
+                others[name] = {"error": f"{type(e).__name__}: {e}"}
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
 
     line = {
         "metric": METRIC, "value": pipe_value, "unit": "samples/s", "n_gpus": world,
@@ -1250,6 +1435,7 @@ def run_gpu(args):
         "clocks": clocks,
         "rank_error": accuracy,
         "serving": serving,
+        **others,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -1276,6 +1462,8 @@ def main():
     ap.add_argument("--serve-window", type=float, default=1e-3)
     ap.add_argument("--serve-rate", type=float, default=SERVE_RATE)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="headline (config 3) only: skip the config 1, 2 and 4 sub-objects")
     ap.add_argument("--keymap", action="store_true",
                     help="run only the key-dictionary benchmark and print its line")
     ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4],

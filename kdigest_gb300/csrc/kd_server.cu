@@ -14,9 +14,11 @@
 // advances the clock past its end, or on flush — never on a wall-clock timer,
 // so the batches, and therefore every result, depend only on the request
 // stream.  Requests that arrive while earlier windows are on the GPU are
-// admitted (against the byte budget) into the open window; the next closed
-// window's host->device copy runs on a copy stream while the current window
-// computes.
+// admitted into the open window while the device memory in use (the session's
+// store and workspaces, the server's staging buffers) plus the device
+// footprint of the requests already buffered stays within the budget; the
+// next closed window's host->device copy runs on a copy stream while the
+// current window computes.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -53,7 +55,7 @@ struct Req {
   std::vector<uint32_t> keys;
   std::vector<double> vals;  // values, q or x
   double* out = nullptr;     // caller's output (queries)
-  size_t bytes = 0;
+  size_t dev_bytes = 0;      // device footprint until completion (staging, workspace share)
   int status = -1;  // -1 while pending
   double t_submit = 0.0, t_done = 0.0;
 };
@@ -85,6 +87,17 @@ void free_buf(Buf& b) {
     if (p) cudaFreeHost(p);
   if (b.copied) cudaEventDestroy(b.copied);
   b = Buf();
+}
+
+// Device bytes of a buffer set: ingest keys and values, query keys, values
+// and results.
+size_t buf_dev_bytes(const Buf& b) { return b.cap_i * 12 + b.cap_q * 20; }
+
+// Device footprint of one request while it is buffered and served: its
+// staging, and for ingest pairs the share of the ingest workspace they need
+// (sort buffers, dense level inputs: about 100 bytes per sample).
+size_t req_dev_bytes(int kind, long long n) {
+  return (size_t)n * (kind == KD_REQ_INGEST ? 12 + 100 : 20) + 64;
 }
 
 bool grow_buf(Buf& b, size_t ni, size_t nq) {
@@ -137,8 +150,10 @@ struct kd_server {
   double clock_ts = -std::numeric_limits<double>::infinity();
   long long newest_window = std::numeric_limits<long long>::min();
   bool flushing = false, stop = false;
-  size_t buffered = 0;
   std::vector<double> latencies;
+  size_t buffered_dev = 0;   // device footprint of submitted, not yet completed requests
+  size_t dev_in_use = 0;     // session device memory + staging, as of the last window
+  size_t dev_peak = 0;       // the largest dev_in_use + buffered_dev seen
   long long completed = 0, windows_done = 0;
   double busy_s = 0.0;
   int fatal = 0;
@@ -184,6 +199,10 @@ std::unique_ptr<Staged> take_window(kd_server* v, int bi) {
 int stage_copy(kd_server* v, Staged& sg) {
   Buf& b = v->buf[sg.buf];
   if (!grow_buf(b, (size_t)sg.n_ing, (size_t)(sg.n_qq + sg.n_qc))) return KD_ENOMEM;
+  {
+    std::lock_guard<std::mutex> lk(v->mu);
+    v->dev_in_use = v->s->mem_used + buf_dev_bytes(v->buf[0]) + buf_dev_bytes(v->buf[1]);
+  }
   long long oi = 0, oq = 0, oc = sg.n_qq;  // quantile pairs first, then cdf pairs
   for (auto& r : sg.reqs) {
     const size_t n = r->vals.size();
@@ -262,9 +281,10 @@ void run_window(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>*
     std::vector<uint32_t>().swap(r->keys);  // the data is consumed: release it now
     std::vector<double>().swap(r->vals);
     v->latencies.push_back(t1 - r->t_submit);
-    v->buffered -= std::min(v->buffered, r->bytes);
+    v->buffered_dev -= std::min(v->buffered_dev, r->dev_bytes);
     ++v->completed;
   }
+  v->dev_in_use = v->s->mem_used + buf_dev_bytes(v->buf[0]) + buf_dev_bytes(v->buf[1]);
   ++v->windows_done;
   v->busy_s += t1 - t0;
   v->cv.notify_all();
@@ -317,6 +337,7 @@ KD_API int kd_server_create(kd_store* store, double window_s, size_t budget_byte
   v->s = s;
   v->window_s = window_s;
   v->budget = budget_bytes ? budget_bytes : ((size_t)1 << 40);
+  v->dev_in_use = s->mem_used;
   cudaSetDevice(s->device);
   int rc = kd_pipeline_prepare_device(s);
   // Samples a one-key store buffered on the single-sample path are merged
@@ -357,21 +378,24 @@ KD_API int kd_server_submit(kd_server* v, int kind, double timestamp, const uint
   if (keys && n) memcpy(r->keys.data(), keys, (size_t)n * 4);
   if (n) r->vals.assign(vals, vals + n);
   r->out = out;
-  r->bytes = (size_t)n * (kind == KD_REQ_INGEST ? 12 : 20) + 64;
-  if (r->bytes > v->budget) return KD_ENOMEM;
+  r->dev_bytes = req_dev_bytes(kind, n);
   std::unique_lock<std::mutex> lk(v->mu);
   if (v->stop) return KD_EINVAL;
   if (timestamp < v->last_ts) return KD_EINVAL;  // timestamps must not decrease
   if (r->window < v->newest_window || (double)(r->window + 1) * v->window_s <= v->clock_ts)
     return KD_EINVAL;  // its window is already closed
-  // admission: wait until the buffered requests leave room for this one
-  v->cv.wait(lk, [&] { return v->buffered + r->bytes <= v->budget || v->stop; });
+  // a request that could not fit even with nothing else buffered
+  if (v->dev_in_use + r->dev_bytes > v->budget) return KD_ENOMEM;
+  // admission: wait until the device memory in use and the buffered requests'
+  // footprint leave room for this one
+  v->cv.wait(lk, [&] { return v->dev_in_use + v->buffered_dev + r->dev_bytes <= v->budget || v->stop; });
   if (v->stop) return KD_EINVAL;
   r->id = v->next_id++;
   r->t_submit = now_s();
   v->last_ts = timestamp;
   v->newest_window = std::max(v->newest_window, r->window);
-  v->buffered += r->bytes;
+  v->buffered_dev += r->dev_bytes;
+  v->dev_peak = std::max(v->dev_peak, v->dev_in_use + v->buffered_dev);
   v->live[r->id] = r;
   v->pending.push_back(r);
   *ticket = r->id;
@@ -404,12 +428,30 @@ KD_API int kd_server_wait(kd_server* v, int64_t ticket, double timeout_s, int* s
   return KD_OK;
 }
 
+KD_API int kd_server_latency(kd_server* v, int64_t ticket, double* seconds) {
+  if (!v || !seconds) return KD_EINVAL;
+  std::lock_guard<std::mutex> lk(v->mu);
+  auto it = v->live.find(ticket);
+  if (it == v->live.end()) return KD_EINVAL;
+  *seconds = it->second->status >= 0 ? it->second->t_done - it->second->t_submit : -1.0;
+  return KD_OK;
+}
+
+KD_API int kd_server_memory(kd_server* v, size_t* in_use, size_t* peak, size_t* budget) {
+  if (!v) return KD_EINVAL;
+  std::lock_guard<std::mutex> lk(v->mu);
+  if (in_use) *in_use = v->dev_in_use + v->buffered_dev;
+  if (peak) *peak = v->dev_peak;
+  if (budget) *budget = v->budget;
+  return KD_OK;
+}
+
 KD_API int kd_server_flush(kd_server* v) {
   if (!v) return KD_EINVAL;
   std::unique_lock<std::mutex> lk(v->mu);
   v->flushing = true;
   v->cv.notify_all();
-  v->cv.wait(lk, [&] { return v->pending.empty() && v->buffered == 0; });
+  v->cv.wait(lk, [&] { return v->pending.empty() && v->buffered_dev == 0; });
   v->flushing = false;
   // later requests open new windows after the flushed ones
   v->clock_ts = std::max(v->clock_ts, (double)(v->newest_window + 1) * v->window_s);

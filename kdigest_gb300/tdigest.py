@@ -954,6 +954,21 @@ class Server:
     def flush(self):
         N.load().kd_server_flush(self._h)
 
+    def latency(self, ticket: int) -> float:
+        """Submit-to-completion seconds of a completed request not yet waited
+        for (-1 while pending)."""
+        sec = ctypes.c_double(0.0)
+        rc = N.load().kd_server_latency(self._h, int(ticket), ctypes.byref(sec))
+        if rc:
+            raise KdError(rc, "unknown ticket")
+        return sec.value
+
+    def memory(self) -> dict:
+        """Device bytes counted against the admission budget: now, peak, budget."""
+        a, b, c = ctypes.c_size_t(0), ctypes.c_size_t(0), ctypes.c_size_t(0)
+        N.load().kd_server_memory(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return {"in_use_bytes": a.value, "peak_bytes": b.value, "budget_bytes": c.value}
+
     def stats(self) -> dict:
         lat = np.zeros(3)
         done = ctypes.c_int64(0)

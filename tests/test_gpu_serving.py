@@ -49,8 +49,21 @@ def _store(kd):
                              session=kd.GpuSession())
 
 
+def _device_budget(kd, g, extra):
+    """A budget of `extra` bytes above the device memory the store's session
+    holds once its ingest workspace exists (warmed on another store)."""
+    warm = kd.GroupedTDigest(8, 200.0, scale=kd.K2, session=g.session)
+    warm.add_batch(np.zeros(5000, np.uint32), np.ones(5000))
+    probe = kd.Server(g, window=1e-3)
+    used = probe.memory()["in_use_bytes"]
+    probe.close()
+    return used + extra
+
+
 def _serve(kd, reqs, window, budget=0):
     g = _store(kd)
+    if budget:
+        budget = _device_budget(kd, g, budget)
     srv = kd.Server(g, window=window, budget_bytes=budget)
     tickets = []
     for kind, t, k, v in reqs:
@@ -139,7 +152,7 @@ def test_one_request_per_window_is_request_by_request(kd):
 def test_budget_backpressure_keeps_results(kd):
     reqs = _trace(13, 300, 2e-4)
     window = 1e-3
-    ga, ra, _ = _serve(kd, reqs, window, budget=80_000)  # a few requests at a time
+    ga, ra, _ = _serve(kd, reqs, window, budget=120_000)  # a few requests' device footprint at a time
     gb, rb = _alone(kd, reqs, window)
     _compare(kd, ga, ra, gb, rb)
 
@@ -177,7 +190,7 @@ def test_rejections_and_empty_digest(kd):
     from kdigest_gb300 import KdError
 
     g = _store(kd)
-    srv = kd.Server(g, window=1e-3, budget_bytes=10_000)
+    srv = kd.Server(g, window=1e-3, budget_bytes=_device_budget(kd, g, 10_000))
     k = np.array([1, 2], dtype=np.uint32)
     with pytest.raises(KdError):
         srv.submit_ingest(0.5, np.array([NK], dtype=np.uint32), [1.0])  # key out of range
@@ -186,7 +199,7 @@ def test_rejections_and_empty_digest(kd):
     with pytest.raises(KdError):
         srv.submit_quantiles(0.5, k, [0.5, 1.5])
     with pytest.raises(KdError):
-        srv.submit_ingest(0.5, np.zeros(2000, np.uint32), np.ones(2000))  # over budget
+        srv.submit_ingest(0.5, np.zeros(2000, np.uint32), np.ones(2000))  # could not fit alone
     t0 = srv.submit_quantiles(0.5, k, [0.5, 0.5])  # empty digests
     t1 = srv.submit_ingest(0.6, k, [3.0, 4.0])
     with pytest.raises(KdError):
