@@ -1057,7 +1057,8 @@ def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
         "client_max_lag_ms": round(lag * 1e3, 3), "submit_seconds": round(t_sub, 3),
         "status_counts": {str(k): v for k, v in sorted(statuses.items())},
         "latency_by_population": populations,
-        "device_memory": {"budget_bytes": mem["budget_bytes"], "peak_counted_bytes": mem["peak_bytes"]},
+        "device_memory": {"budget_bytes": mem["budget_bytes"], "peak_counted_bytes": mem["peak_bytes"],
+                          "measured_after_last_window_bytes": mem["measured_bytes"]},
     }
 
 

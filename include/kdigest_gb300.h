@@ -263,9 +263,9 @@ KD_API int kd_store_import(kd_store* st, const uint32_t* keys, int64_t nkeys, co
  * every result depends only on the request stream.  Requests are validated at
  * submit (KD_EINVAL: key out of range, non-finite value, q outside [0,1],
  * decreasing timestamp or a closed window) and admitted against a device-memory
- * budget (budget_bytes, 0 = 1 TiB): the device memory in use (the session's
- * store and workspaces, the server's staging buffers) plus the device footprint
- * of every buffered request (its staging, and about 100 bytes of ingest
+ * budget (budget_bytes, 0 = 1 TiB): the session's device memory when the server
+ * started (its stores and workspaces) plus the device footprint of every
+ * buffered or in-flight request (its staging, and about 100 bytes of ingest
  * workspace per ingest pair) must stay within it; submit blocks until there is
  * room, and returns KD_ENOMEM for a request that could not fit alone.  The store's session belongs to the server until it is
  * destroyed.  Query outputs are written to `out` (n doubles, kept valid until
@@ -286,9 +286,12 @@ KD_API int kd_server_wait(kd_server* srv, int64_t ticket, double timeout_s, int*
 /* Submit-to-completion latency of a completed request not yet waited for
  * (-1 while it is pending); KD_EINVAL for an unknown ticket. */
 KD_API int kd_server_latency(kd_server* srv, int64_t ticket, double* seconds);
-/* Device bytes counted against the budget now (in use plus buffered
- * requests), their peak so far, and the budget. */
-KD_API int kd_server_memory(kd_server* srv, size_t* in_use, size_t* peak, size_t* budget);
+/* Device bytes counted against the budget now (the baseline plus buffered
+ * requests), their peak so far, the budget, and the session's device memory
+ * plus the server's staging buffers measured after the last window.  Any
+ * pointer may be NULL. */
+KD_API int kd_server_memory(kd_server* srv, size_t* in_use, size_t* peak, size_t* budget,
+                            size_t* measured);
 /* Closes every open window and waits until all submitted requests completed. */
 KD_API int kd_server_flush(kd_server* srv);
 /* Submit-to-completion latency percentiles in seconds (p50, p99, p999), requests

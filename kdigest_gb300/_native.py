@@ -116,7 +116,7 @@ def load(path: str = LIB_PATH):
     L.kd_server_destroy.argtypes = [_P]
     L.kd_server_latency.argtypes = [_P, _I64, ctypes.POINTER(_D)]
     L.kd_server_memory.argtypes = [_P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t),
-                                   ctypes.POINTER(ctypes.c_size_t)]
+                                   ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
     L.kd_compress_noalloc.argtypes = [ctypes.c_int, _D, _P, _P, _I64, ctypes.c_int, _P, _P, _I64,
                                       ctypes.POINTER(_I64), _P, ctypes.c_char_p, ctypes.c_int]
     L.kd_store_stats.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),

@@ -14,11 +14,12 @@
 // advances the clock past its end, or on flush — never on a wall-clock timer,
 // so the batches, and therefore every result, depend only on the request
 // stream.  Requests that arrive while earlier windows are on the GPU are
-// admitted into the open window while the device memory in use (the session's
-// store and workspaces, the server's staging buffers) plus the device
-// footprint of the requests already buffered stays within the budget; the
-// next closed window's host->device copy runs on a copy stream while the
-// current window computes.
+// admitted into the open window while the session's device memory when the
+// server started (store, workspaces) plus the device footprint of the requests
+// buffered or in flight (staging, and their share of the ingest workspace)
+// stays within the budget; the next closed window's host->device copy runs on
+// a copy stream while the current window computes.  The baseline is fixed, so
+// a request that fits alone is always admitted once the queue drains.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -152,8 +153,9 @@ struct kd_server {
   bool flushing = false, stop = false;
   std::vector<double> latencies;
   size_t buffered_dev = 0;   // device footprint of submitted, not yet completed requests
-  size_t dev_in_use = 0;     // session device memory + staging, as of the last window
-  size_t dev_peak = 0;       // the largest dev_in_use + buffered_dev seen
+  size_t dev_base = 0;       // session device memory when the server started
+  size_t dev_measured = 0;   // session device memory + staging after the last window
+  size_t dev_peak = 0;       // the largest dev_base + buffered_dev seen
   long long completed = 0, windows_done = 0;
   double busy_s = 0.0;
   int fatal = 0;
@@ -199,10 +201,7 @@ std::unique_ptr<Staged> take_window(kd_server* v, int bi) {
 int stage_copy(kd_server* v, Staged& sg) {
   Buf& b = v->buf[sg.buf];
   if (!grow_buf(b, (size_t)sg.n_ing, (size_t)(sg.n_qq + sg.n_qc))) return KD_ENOMEM;
-  {
-    std::lock_guard<std::mutex> lk(v->mu);
-    v->dev_in_use = v->s->mem_used + buf_dev_bytes(v->buf[0]) + buf_dev_bytes(v->buf[1]);
-  }
+
   long long oi = 0, oq = 0, oc = sg.n_qq;  // quantile pairs first, then cdf pairs
   for (auto& r : sg.reqs) {
     const size_t n = r->vals.size();
@@ -284,7 +283,7 @@ void run_window(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>*
     v->buffered_dev -= std::min(v->buffered_dev, r->dev_bytes);
     ++v->completed;
   }
-  v->dev_in_use = v->s->mem_used + buf_dev_bytes(v->buf[0]) + buf_dev_bytes(v->buf[1]);
+  v->dev_measured = v->s->mem_used + buf_dev_bytes(v->buf[0]) + buf_dev_bytes(v->buf[1]);
   ++v->windows_done;
   v->busy_s += t1 - t0;
   v->cv.notify_all();
@@ -337,7 +336,7 @@ KD_API int kd_server_create(kd_store* store, double window_s, size_t budget_byte
   v->s = s;
   v->window_s = window_s;
   v->budget = budget_bytes ? budget_bytes : ((size_t)1 << 40);
-  v->dev_in_use = s->mem_used;
+  v->dev_base = v->dev_measured = s->mem_used;
   cudaSetDevice(s->device);
   int rc = kd_pipeline_prepare_device(s);
   // Samples a one-key store buffered on the single-sample path are merged
@@ -385,17 +384,17 @@ KD_API int kd_server_submit(kd_server* v, int kind, double timestamp, const uint
   if (r->window < v->newest_window || (double)(r->window + 1) * v->window_s <= v->clock_ts)
     return KD_EINVAL;  // its window is already closed
   // a request that could not fit even with nothing else buffered
-  if (v->dev_in_use + r->dev_bytes > v->budget) return KD_ENOMEM;
-  // admission: wait until the device memory in use and the buffered requests'
-  // footprint leave room for this one
-  v->cv.wait(lk, [&] { return v->dev_in_use + v->buffered_dev + r->dev_bytes <= v->budget || v->stop; });
+  if (v->dev_base + r->dev_bytes > v->budget) return KD_ENOMEM;
+  // admission: wait until the baseline and the buffered requests' footprint
+  // leave room for this one
+  v->cv.wait(lk, [&] { return v->dev_base + v->buffered_dev + r->dev_bytes <= v->budget || v->stop; });
   if (v->stop) return KD_EINVAL;
   r->id = v->next_id++;
   r->t_submit = now_s();
   v->last_ts = timestamp;
   v->newest_window = std::max(v->newest_window, r->window);
   v->buffered_dev += r->dev_bytes;
-  v->dev_peak = std::max(v->dev_peak, v->dev_in_use + v->buffered_dev);
+  v->dev_peak = std::max(v->dev_peak, v->dev_base + v->buffered_dev);
   v->live[r->id] = r;
   v->pending.push_back(r);
   *ticket = r->id;
@@ -437,10 +436,12 @@ KD_API int kd_server_latency(kd_server* v, int64_t ticket, double* seconds) {
   return KD_OK;
 }
 
-KD_API int kd_server_memory(kd_server* v, size_t* in_use, size_t* peak, size_t* budget) {
+KD_API int kd_server_memory(kd_server* v, size_t* in_use, size_t* peak, size_t* budget,
+                            size_t* measured) {
   if (!v) return KD_EINVAL;
   std::lock_guard<std::mutex> lk(v->mu);
-  if (in_use) *in_use = v->dev_in_use + v->buffered_dev;
+  if (in_use) *in_use = v->dev_base + v->buffered_dev;
+  if (measured) *measured = v->dev_measured;
   if (peak) *peak = v->dev_peak;
   if (budget) *budget = v->budget;
   return KD_OK;

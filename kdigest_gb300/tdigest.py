@@ -964,10 +964,13 @@ class Server:
         return sec.value
 
     def memory(self) -> dict:
-        """Device bytes counted against the admission budget: now, peak, budget."""
-        a, b, c = ctypes.c_size_t(0), ctypes.c_size_t(0), ctypes.c_size_t(0)
-        N.load().kd_server_memory(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
-        return {"in_use_bytes": a.value, "peak_bytes": b.value, "budget_bytes": c.value}
+        """Device bytes counted against the admission budget (now, peak), the
+        budget, and the device memory measured after the last window."""
+        a, b, c, d = (ctypes.c_size_t(0) for _ in range(4))
+        N.load().kd_server_memory(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                  ctypes.byref(d))
+        return {"in_use_bytes": a.value, "peak_bytes": b.value, "budget_bytes": c.value,
+                "measured_bytes": d.value}
 
     def stats(self) -> dict:
         lat = np.zeros(3)

@@ -51,9 +51,7 @@ def _store(kd):
 
 def _device_budget(kd, g, extra):
     """A budget of `extra` bytes above the device memory the store's session
-    holds once its ingest workspace exists (warmed on another store)."""
-    warm = kd.GroupedTDigest(8, 200.0, scale=kd.K2, session=g.session)
-    warm.add_batch(np.zeros(5000, np.uint32), np.ones(5000))
+    holds when a server starts."""
     probe = kd.Server(g, window=1e-3)
     used = probe.memory()["in_use_bytes"]
     probe.close()

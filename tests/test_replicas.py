@@ -38,7 +38,7 @@ def _rank(rank, world, port, out):
 
 def test_two_gloo_replicas_time_and_value():
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
         r0, r1 = out[0], out[1]
