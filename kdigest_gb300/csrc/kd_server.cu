@@ -30,6 +30,7 @@
 #include <cstring>
 #include <deque>
 #include <limits>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -153,6 +154,8 @@ struct kd_server {
   bool flushing = false, stop = false;
   std::vector<double> latencies;
   size_t buffered_dev = 0;   // device footprint of submitted, not yet completed requests
+  std::map<long long, size_t> win_dev;  // the same, per window
+  unsigned long long next_seq = 0, admit_seq = 0;  // admission in submit order
   size_t dev_base = 0;       // session device memory when the server started
   size_t dev_measured = 0;   // session device memory + staging after the last window
   size_t dev_peak = 0;       // the largest dev_base + buffered_dev seen
@@ -281,6 +284,9 @@ void run_window(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>*
     std::vector<double>().swap(r->vals);
     v->latencies.push_back(t1 - r->t_submit);
     v->buffered_dev -= std::min(v->buffered_dev, r->dev_bytes);
+    auto wi = v->win_dev.find(r->window);
+    if (wi != v->win_dev.end() && (wi->second -= std::min(wi->second, r->dev_bytes)) == 0)
+      v->win_dev.erase(wi);
     ++v->completed;
   }
   v->dev_measured = v->s->mem_used + buf_dev_bytes(v->buf[0]) + buf_dev_bytes(v->buf[1]);
@@ -385,15 +391,34 @@ KD_API int kd_server_submit(kd_server* v, int kind, double timestamp, const uint
     return KD_EINVAL;  // its window is already closed
   // a request that could not fit even with nothing else buffered
   if (v->dev_base + r->dev_bytes > v->budget) return KD_ENOMEM;
-  // admission: wait until the baseline and the buffered requests' footprint
-  // leave room for this one
-  v->cv.wait(lk, [&] { return v->dev_base + v->buffered_dev + r->dev_bytes <= v->budget || v->stop; });
-  if (v->stop) return KD_EINVAL;
-  r->id = v->next_id++;
+  // The request takes its place in the stream now: its timestamp closes every
+  // earlier window, so those drain while it waits for room.  Requests are
+  // admitted in submit order.  Its own window closes only on a later request,
+  // an advance or a flush, so if the earlier windows have all drained and its
+  // window still leaves no room, waiting cannot help: KD_ENOMEM.
   r->t_submit = now_s();
   v->last_ts = timestamp;
   v->newest_window = std::max(v->newest_window, r->window);
+  const unsigned long long seq = v->next_seq++;
+  v->cv.notify_all();
+  auto own = [&]() -> size_t {
+    auto it = v->win_dev.find(r->window);
+    return it == v->win_dev.end() ? 0 : it->second;
+  };
+  auto room = [&] { return v->dev_base + v->buffered_dev + r->dev_bytes <= v->budget; };
+  v->cv.wait(lk, [&] {
+    return v->stop || (v->admit_seq == seq && (room() || v->buffered_dev == own()));
+  });
+  if (v->stop) return KD_EINVAL;
+  if (!room()) {  // only its own window holds the budget
+    ++v->admit_seq;
+    v->cv.notify_all();
+    return KD_ENOMEM;
+  }
+  ++v->admit_seq;
+  r->id = v->next_id++;
   v->buffered_dev += r->dev_bytes;
+  v->win_dev[r->window] += r->dev_bytes;
   v->dev_peak = std::max(v->dev_peak, v->dev_base + v->buffered_dev);
   v->live[r->id] = r;
   v->pending.push_back(r);

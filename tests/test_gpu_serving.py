@@ -150,7 +150,8 @@ def test_one_request_per_window_is_request_by_request(kd):
 def test_budget_backpressure_keeps_results(kd):
     reqs = _trace(13, 300, 2e-4)
     window = 1e-3
-    ga, ra, _ = _serve(kd, reqs, window, budget=120_000)  # a few requests' device footprint at a time
+    # the largest window's footprint is about 0.32 MB: at most two windows at a time
+    ga, ra, _ = _serve(kd, reqs, window, budget=500_000)
     gb, rb = _alone(kd, reqs, window)
     _compare(kd, ga, ra, gb, rb)
 
@@ -213,4 +214,16 @@ def test_rejections_and_empty_digest(kd):
     srv.flush()
     st2, out2 = srv.wait(t2, 30.0)
     assert st2 == 0 and np.array_equal(out2, [3.0, 4.0])
+    # A window whose own requests fill the budget: the next request of that
+    # window is refused (waiting could not help: the window closes only on a
+    # later request); a request of a later window closes it and is admitted
+    # once it drained.
+    big = np.ones(60)
+    t3 = srv.submit_ingest(0.9, np.zeros(60, np.uint32), big)
+    with pytest.raises(KdError) as ei:
+        srv.submit_ingest(0.9, np.ones(60, np.uint32), big)
+    assert ei.value.code == 5  # KD_ENOMEM
+    t4 = srv.submit_ingest(0.95, np.ones(60, np.uint32), big)
+    srv.flush()
+    assert srv.wait(t3, 30.0)[0] == 0 and srv.wait(t4, 30.0)[0] == 0
     srv.close()
