@@ -26,6 +26,8 @@
 #define KD_RS_MIN_BLOCKS 3
 #endif
 #define KD_RS_WARPS (KD_RS_THREADS / 32)
+// One thread per digit in the per-digit stages (scan, look-back, scatter table).
+static_assert(KD_RS_THREADS >= 256 && KD_RS_THREADS % 32 == 0, "a radix block needs a thread per digit");
 #ifndef KD_RS_PER_WARP
 #define KD_RS_PER_WARP 512
 #endif
@@ -93,8 +95,15 @@ struct KdRsPass {
   int stall_first;       // tests only: tile 0 never publishes (its successor's wait runs out)
 };
 
+// Predecessor words read per look-back round trip (GB300: 2 to 8 measure
+// alike, 16 and above cost more L2 traffic than they save round trips).
 #ifndef KD_LB_WINDOW
-#define KD_LB_WINDOW 16
+#define KD_LB_WINDOW 4
+#endif
+// Pause before polling again when no predecessor word was ready (0: none);
+// with the bounded poll count this caps a look-back wait near one second.
+#ifndef KD_LB_BACKOFF_NS
+#define KD_LB_BACKOFF_NS 256
 #endif
 
 template <bool kIdx>
@@ -146,6 +155,7 @@ __global__ void __launch_bounds__(KD_RS_THREADS, KD_RS_MIN_BLOCKS) kd_rs_oneswee
     else rank2[r >> 1] = rk;
   }
   __syncthreads();
+
   // 2. per digit: exclusive prefix over warps, tile count, tile offset
   unsigned cnt_d = 0;
   if (threadIdx.x < 256) {
@@ -164,8 +174,12 @@ __global__ void __launch_bounds__(KD_RS_THREADS, KD_RS_MIN_BLOCKS) kd_rs_oneswee
     const unsigned g = threadIdx.x < 256 ? a.ghist[threadIdx.x] : 0u;
     const int4 inc = block_scan_incl(make_int4((int)cnt_d, (int)g, 0, 0), scan_tmp, &tot);
     if (threadIdx.x < 256) {
-      blk_off[threadIdx.x] = (unsigned)(inc.x - (int)cnt_d);
+      const unsigned off = (unsigned)(inc.x - (int)cnt_d);
+      blk_off[threadIdx.x] = off;
       gbase = (unsigned)(inc.y - (int)g);
+      // the staging position of a warp's digit-d run: tile offset + warp prefix
+#pragma unroll
+      for (int w = 0; w < KD_RS_WARPS; ++w) wcnt[w][threadIdx.x] += off;
     }
   }
   // 3. decoupled look-back, one thread per digit, KD_LB_WINDOW predecessors per
@@ -204,11 +218,15 @@ __global__ void __launch_bounds__(KD_RS_THREADS, KD_RS_MIN_BLOCKS) kd_rs_oneswee
           timed_out = true;
           break;
         }
+#if KD_LB_BACKOFF_NS > 0
+        if (k == 0) __nanosleep(KD_LB_BACKOFF_NS);
+#endif
       }
       if (timed_out) atomicCAS(a.err_code, 0, KD_ETIMEOUT);
       st[(size_t)b * 256 + d] = lb_pack(epoch, KD_LB_INC, excl + cnt_d);
     }
-    gpos[d] = (long long)gbase + (long long)excl;
+    // staged position i of digit d goes to gpos[d] + i
+    gpos[d] = (long long)gbase + (long long)excl - (long long)blk_off[d];
   }
   __syncthreads();
   // 4. stage in digit order (the tile is re-read from L1/L2)
@@ -218,7 +236,7 @@ __global__ void __launch_bounds__(KD_RS_THREADS, KD_RS_MIN_BLOCKS) kd_rs_oneswee
     if (i < a.n) {
       const unsigned d = dig[r];
       const unsigned rk = (rank2[r >> 1] >> ((r & 1) * 16)) & 0xffffu;
-      const unsigned lp = blk_off[d] + wcnt[warp][d] + rk;
+      const unsigned lp = wcnt[warp][d] + rk;
       const uint64_t kvv = a.kin[i];
       const uint32_t kkv = a.keyin[i];
       sk[lp] = kvv;
@@ -233,7 +251,7 @@ __global__ void __launch_bounds__(KD_RS_THREADS, KD_RS_MIN_BLOCKS) kd_rs_oneswee
     const uint64_t v = sk[i];
     const uint32_t k2 = skey[i];
     const unsigned d = a.from_key ? (k2 >> shift) & 255u : (unsigned)(v >> shift) & 255u;
-    const long long pos = gpos[d] + (i - (int)blk_off[d]);
+    const long long pos = gpos[d] + i;
     a.kout[pos] = v;
     a.keyout[pos] = k2;
     if (kIdx) a.idxout[pos] = sidx[i];
