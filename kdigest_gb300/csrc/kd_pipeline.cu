@@ -524,6 +524,9 @@ struct BlockScr {
   int nneed, ndiv, nout, stop, maxlen;
   unsigned nz;          // rounds of 32 that hold a head
   long long wsum[KD_TILE_WARPS];
+  double cwx[KD_TILE_WARPS];  // per warp: segmented sum(w * x) carried out of its last chunk
+  double cw[KD_TILE_WARPS];   // the same for sum(w) (int64 bits, integral path)
+  int cf[KD_TILE_WARPS];      // whether the warp's chunks hold a head
   int rc[32];           // heads per round of 32 elements (then their offsets)
   unsigned hb[32];      // head ballot per round
 };
@@ -717,8 +720,9 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
   // 4. Segment sums, parked at each segment's end element, with the
   //    association of warp_compress: sum(w) exact (integral weights) or by the
   //    up-sweep of the reference's tree, block-wide; sum(w * x) serial per
-  //    lane chunk, carried across chunks by a segmented Kogge-Stone scan
-  //    (one chunk, n <= KD_SERIAL_TILE_MAX: serial per segment).
+  //    chunk of ceil(n / 128) elements (one per thread), carried across each
+  //    warp's chunks by a segmented Kogge-Stone scan and across the warps in
+  //    order (one chunk, n <= KD_SERIAL_TILE_MAX: serial per segment).
   if (!kInt && uniform) {
     const double w0 = t.w[slot(0)];
     for (int sI = tid; sI < total_out; sI += NT) {
@@ -775,7 +779,6 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
       t.w[e] = awx;
     }
   } else {
-    const int E = slot.E, SE = slot.SE;
     for (int q = tid; q < n; q += NT) {
       const int sl = slot(q);
       t.hf[sl] = 0;
@@ -790,10 +793,11 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
       t.endpos[sI] = (unsigned short)e;
     }
     __syncthreads();
-    if (warp == 0) {  // chunk-serial pieces and the segmented carry across lanes
-      const int lo = lane * E;
-      const int cnt = max(0, min(E, n - lo));
-      const int sb = lane * SE;
+    {  // one chunk per thread: serial pieces, a segmented carry across each
+       // warp's 32 chunks, then across the warps in order
+      const int E4 = (n + NT - 1) / NT;
+      const int lo = tid * E4;
+      const int cnt = max(0, min(E4, n - lo));
       T aw = 0;
       double awx = 0.0;
       bool head_seen = false;
@@ -802,9 +806,10 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
       double pend_wx = 0.0;
       int pend_se = 0;
       for (int j = 0; j < cnt; ++j) {
-        const double wi = t.w[sb + j], xi = t.x[sb + j];
+        const int sp = slot(lo + j);
+        const double wi = t.w[sp], xi = t.x[sp];
         const double wx = KD_MUL(wi, xi);
-        const bool hd = t.hf[sb + j];
+        const bool hd = t.hf[sp];
         if (hd || j == 0) {
           if (kInt) aw = A::from_w(wi);
           awx = wx;
@@ -813,15 +818,15 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
           awx = KD_ADD(awx, wx);
         }
         if (hd) head_seen = true;
-        if (t.ef[sb + j]) {
+        if (t.ef[sp]) {
           if (head_seen) {
-            if (kInt) t.L[sb + j] = A::store(aw);
-            t.w[sb + j] = awx;
+            if (kInt) t.L[sp] = A::store(aw);
+            t.w[sp] = awx;
           } else {
             pend = true;
             pend_w = aw;
             pend_wx = awx;
-            pend_se = sb + j;
+            pend_se = sp;
           }
         }
       }
@@ -841,8 +846,38 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
           F |= tf;
         }
       }
-      const T cw = A::shfl_up(Vw, 1);
-      const double cwx = shfl_up_d(Vwx, 1);
+      if (lane == 31) {
+        bs.cwx[warp] = Vwx;
+        bs.cw[warp] = A::store(Vw);
+        bs.cf[warp] = F;
+      }
+      __syncthreads();
+      // the final value of the previous warp's last chunk
+      double cwx_prev = 0.0;
+      T cw_prev = 0;
+      if (warp > 0) {
+        cwx_prev = bs.cwx[0];
+        cw_prev = A::load(bs.cw[0]);
+        for (int g = 1; g < warp; ++g) {
+          if (bs.cf[g]) {
+            cwx_prev = bs.cwx[g];
+            cw_prev = A::load(bs.cw[g]);
+          } else {
+            cwx_prev = KD_ADD(bs.cwx[g], cwx_prev);
+            if (kInt) cw_prev = A::add(A::load(bs.cw[g]), cw_prev);
+          }
+        }
+        if (!F) {
+          Vwx = KD_ADD(Vwx, cwx_prev);
+          if (kInt) Vw = A::add(Vw, cw_prev);
+        }
+      }
+      double cwx = shfl_up_d(Vwx, 1);
+      T cw = A::shfl_up(Vw, 1);
+      if (lane == 0) {
+        cwx = cwx_prev;
+        cw = cw_prev;
+      }
       if (pend) {
         if (kInt) t.L[pend_se] = A::store(A::add(cw, pend_w));
         t.w[pend_se] = KD_ADD(cwx, pend_wx);

@@ -106,10 +106,11 @@ static int32_t o_bucket(int scale, double cum, double tot, double nrm) {
 /*   - KDO_SUMS_REFERENCE: the reference's tree above;                        */
 /*   - KDO_SUMS_BUILD (default): the order the kernels use, which keeps their */
 /*     FP64 pipe busy: tiles of at most KD_SERIAL_TILE_MAX elements sum each  */
-/*     segment serially, left to right; larger tiles cut the tile into 32     */
-/*     lane chunks of E = ceil(n/32) consecutive elements, sum each piece of  */
-/*     a segment inside a chunk serially and carry the trailing pieces across */
-/*     chunks with a segmented Kogge-Stone scan over the 32 chunks.           */
+/*     segment serially, left to right; larger tiles cut the tile into 128    */
+/*     chunks of E = ceil(n/128) consecutive elements (one per thread of a    */
+/*     4-warp block), sum each piece of a segment inside a chunk serially,    */
+/*     carry the trailing pieces across the 32 chunks of each warp with a     */
+/*     segmented Kogge-Stone scan, then across the 4 warps in order.          */
 /* The two differ by rounding in the means only: no prefix, id or weight     */
 /* depends on sum(w*x).  The tests check the reference form against the lane */
 /* loops bit for bit and the build form against the reference form.          */
@@ -176,12 +177,13 @@ static void build_order_wx(const double* wx, const int32_t* id, int n, double* s
     }
     return;
   }
-  const int E = (n + 31) / 32;
-  double V[32];
-  int F[32];
-  int pend[32];
-  double pendv[32];
-  for (int c = 0; c < 32; ++c) {
+  enum { C = 128, G = 32 }; /* chunks, chunks per group (a warp of the block) */
+  const int E = (n + C - 1) / C;
+  double V[C];
+  int F[C];
+  int pend[C];
+  double pendv[C];
+  for (int c = 0; c < C; ++c) {
     V[c] = 0.0;
     F[c] = 0;
     pend[c] = -1;
@@ -199,16 +201,28 @@ static void build_order_wx(const double* wx, const int32_t* id, int n, double* s
     }
     V[c] = a;
   }
-  for (int o = 1; o < 32; o <<= 1) { /* segmented inclusive Kogge-Stone over the chunks */
-    double tv[32];
-    int tf[32];
-    for (int c = 0; c < 32; ++c) { tv[c] = V[c]; tf[c] = F[c]; }
-    for (int c = o; c < 32; ++c) {
-      if (!tf[c]) V[c] = tv[c] + tv[c - o];
-      F[c] = tf[c] | tf[c - o];
+  /* segmented inclusive Kogge-Stone over the chunks of each group */
+  for (int g = 0; g < C / G; ++g) {
+    double* Vg = V + g * G;
+    int* Fg = F + g * G;
+    for (int o = 1; o < G; o <<= 1) {
+      double tv[G];
+      int tf[G];
+      for (int c = 0; c < G; ++c) { tv[c] = Vg[c]; tf[c] = Fg[c]; }
+      for (int c = o; c < G; ++c) {
+        if (!tf[c]) Vg[c] = tv[c] + tv[c - o];
+        Fg[c] = tf[c] | tf[c - o];
+      }
     }
   }
-  for (int c = 1; c < 32; ++c)
+  /* carried across the groups in order: a chunk with no head since its group
+   * began adds the final value of the previous group's last chunk */
+  for (int g = 1; g < C / G; ++g) {
+    const double carry = V[g * G - 1];
+    for (int c = g * G; c < (g + 1) * G; ++c)
+      if (!F[c]) V[c] = V[c] + carry;
+  }
+  for (int c = 1; c < C; ++c)
     if (pend[c] >= 0) swx[pend[c]] = V[c - 1] + pendv[c];
 }
 
