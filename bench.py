@@ -957,7 +957,8 @@ def make_serve_pool(seed: int = SEED + 5, num_keys: int = SERVE_KEYS, size: int 
 
 
 def make_serve_trace(seconds: float, rate: float = SERVE_RATE, seed: int = SEED + 7,
-                     num_keys: int = SERVE_KEYS, pool: int = SERVE_POOL):
+                     num_keys: int = SERVE_KEYS, pool: int = SERVE_POOL, pool_keys=None,
+                     window: float = 1e-3):
     """Arrival times (Poisson), kinds, sizes, pool offsets and query pairs."""
     rng = np.random.default_rng(seed)
     n = int(rate * seconds * 1.1) + 16
@@ -971,16 +972,25 @@ def make_serve_trace(seconds: float, rate: float = SERVE_RATE, seed: int = SEED 
     nq = int(sizes[~ingest].sum())
     # Query requests alternate between two key populations: keys uniform over
     # all 10^6 (most never ingested: such a pair completes with KD_EEMPTY and
-    # NaN) and keys drawn like the ingest keys, Zipf(1.2), which exist.
+    # NaN), and keys of pairs that ingest requests sent at least two windows
+    # earlier (so the window's queries find them in the store; hot keys are
+    # drawn as often as they were ingested).  Queries before any such ingest
+    # join the uniform population.
+    ing_idx = np.flatnonzero(ingest)
+    ing_arr = arr[ing_idx]
+    ing_cum = np.concatenate([[0], np.cumsum(sizes[ing_idx])])
     qpop = np.zeros(m, np.int8)
     qidx = np.flatnonzero(~ingest)
-    qpop[qidx[1::2]] = 1
     qkeys = np.empty(nq, np.uint32)
     qo = 0
-    for i in qidx:
+    for j, i in enumerate(qidx):
         n = int(sizes[i])
-        if qpop[i]:
-            qkeys[qo:qo + n] = serve_zipf_keys(rng, n, num_keys)
+        seen = int(np.searchsorted(ing_arr, arr[i] - 2.0 * window, side="right"))
+        if j % 2 == 1 and seen > 0 and pool_keys is not None:
+            qpop[i] = 1
+            u = rng.integers(0, ing_cum[seen], n)
+            r = np.searchsorted(ing_cum, u, side="right") - 1
+            qkeys[qo:qo + n] = pool_keys[offs[ing_idx[r]] + (u - ing_cum[r])]
         else:
             qkeys[qo:qo + n] = rng.integers(0, num_keys, n)
         qo += n
@@ -988,9 +998,16 @@ def make_serve_trace(seconds: float, rate: float = SERVE_RATE, seed: int = SEED 
     return arr, ingest, sizes, offs, qkeys, qvals, qpop
 
 
+SERVE_WARM_S = 0.5  # leading part of the trace whose requests are not in the percentiles
+
+
 def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
     """Open-loop client at `rate` requests/s against the serving loop; returns
-    latency percentiles (submit -> completion) and throughput."""
+    latency percentiles (submit -> completion) and throughput.  The trace runs
+    SERVE_WARM_S + `seconds`; the percentiles and rates cover the requests
+    arriving after the warm-up (the first windows allocate the workspaces)."""
+    import gc
+
     import kdigest_gb300 as kd
 
     sess = kd.GpuSession()
@@ -998,40 +1015,51 @@ def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
                               session=sess)
     srv = kd.Server(store, window=window, budget_bytes=100 << 30)
     pk, pv = make_serve_pool()
-    arr, ingest, sizes, offs, qkeys, qvals, qpop = make_serve_trace(seconds, rate)
+    arr, ingest, sizes, offs, qkeys, qvals, qpop = make_serve_trace(
+        SERVE_WARM_S + seconds, rate, pool_keys=pk, window=window)
     tickets = []
     lag = 0.0
     qo = 0
-    t0 = time.perf_counter()
-    for i in range(len(arr)):
-        target = t0 + arr[i]
-        now = time.perf_counter()
-        while now < target:
+    gc.collect()
+    gc.disable()  # no collector pauses in the open-loop client
+    try:
+        t0 = time.perf_counter()
+        t_meas = None
+        for i in range(len(arr)):
+            target = t0 + arr[i]
             now = time.perf_counter()
-        lag = max(lag, now - target)
-        n = int(sizes[i])
-        if ingest[i]:
-            o = int(offs[i])
-            tickets.append(srv.submit_ingest(arr[i], pk[o:o + n], pv[o:o + n]))
-        else:
-            tickets.append(srv.submit_quantiles(arr[i], qkeys[qo:qo + n], qvals[qo:qo + n]))
-            qo += n
-        # nothing earlier than the next arrival can come: windows ending by then close
-        srv.advance(arr[i + 1] if i + 1 < len(arr) else arr[i] + window)
-    t_sub = time.perf_counter() - t0
-    srv.flush()
-    t_all = time.perf_counter() - t0
+            while now < target:
+                now = time.perf_counter()
+            if arr[i] >= SERVE_WARM_S:
+                if t_meas is None:
+                    t_meas = now
+                lag = max(lag, now - target)
+            n = int(sizes[i])
+            if ingest[i]:
+                o = int(offs[i])
+                tickets.append(srv.submit_ingest(arr[i], pk[o:o + n], pv[o:o + n]))
+            else:
+                tickets.append(srv.submit_quantiles(arr[i], qkeys[qo:qo + n], qvals[qo:qo + n]))
+                qo += n
+            # nothing earlier than the next arrival can come: windows ending by then close
+            srv.advance(arr[i + 1] if i + 1 < len(arr) else arr[i] + window)
+        t_sub = time.perf_counter() - t_meas
+        srv.flush()
+        t_all = time.perf_counter() - t_meas
+    finally:
+        gc.enable()
     st = srv.stats()
     mem = srv.memory()
-    statuses = {}
     lat = np.empty(len(tickets))
+    status = np.empty(len(tickets), np.int64)
     for i, tk in enumerate(tickets):
         lat[i] = srv.latency(tk)
-        s, _ = srv.wait(tk, 60.0)
-        statuses[s] = statuses.get(s, 0) + 1
+        status[i], _ = srv.wait(tk, 60.0)
     srv.close()
+    meas = arr >= SERVE_WARM_S
 
     def pct(sel):
+        sel = sel & meas
         x = np.sort(lat[sel])
         if len(x) == 0:
             return None
@@ -1040,22 +1068,29 @@ def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
             return float(x[min(len(x) - 1, max(0, int(math.ceil(p * len(x))) - 1))]) * 1e3
 
         return {"requests": int(len(x)), "p50_ms": round(r(0.5), 3), "p99_ms": round(r(0.99), 3),
-                "p999_ms": round(r(0.999), 3)}
+                "p999_ms": round(r(0.999), 3),
+                "empty_digest_requests": int((status[sel] == 2).sum())}
 
+    allp = pct(np.ones(len(arr), bool))
     populations = {"ingest": pct(ingest), "query_uniform_keys": pct(~ingest & (qpop == 0)),
                    "query_ingested_keys": pct(~ingest & (qpop == 1))}
-    ing_pairs = int(sizes[ingest].sum())
-    q_pairs = int(sizes[~ingest].sum())
+    ing_pairs = int(sizes[ingest & meas].sum())
+    q_pairs = int(sizes[~ingest & meas].sum())
+    vals, cnts = np.unique(status[meas], return_counts=True)
     return {
-        "p50_ms": round(st["p50_s"] * 1e3, 3), "p99_ms": round(st["p99_s"] * 1e3, 3),
-        "p999_ms": round(st["p999_s"] * 1e3, 3), "requests": len(arr),
-        "seconds": seconds, "window_ms": window * 1e3, "offered_req_per_s": rate,
-        "achieved_req_per_s": round(len(arr) / t_all, 1),
+        "p50_ms": allp["p50_ms"], "p99_ms": allp["p99_ms"], "p999_ms": allp["p999_ms"],
+        "requests": int(meas.sum()), "seconds": seconds, "warmup_seconds": SERVE_WARM_S,
+        "incl_warmup": {"requests": len(arr), "p50_ms": round(st["p50_s"] * 1e3, 3),
+                        "p99_ms": round(st["p99_s"] * 1e3, 3), "p999_ms": round(st["p999_s"] * 1e3, 3)},
+        "window_ms": window * 1e3, "offered_req_per_s": rate,
+        "achieved_req_per_s": round(int(meas.sum()) / t_all, 1),
         "ingest_pairs_per_s": round(ing_pairs / t_all, 1),
         "query_pairs_per_s": round(q_pairs / t_all, 1),
-        "windows": st["windows"], "gpu_worker_busy_frac": round(st["busy_s"] / t_all, 3),
+        "windows": st["windows"], "window_groups": st["groups"],
+        "windows_in_overlapped_groups": st["windows_grouped"],
+        "gpu_worker_busy_frac": round(st["busy_s"] / (t_all + (t_meas - t0)), 3),
         "client_max_lag_ms": round(lag * 1e3, 3), "submit_seconds": round(t_sub, 3),
-        "status_counts": {str(k): v for k, v in sorted(statuses.items())},
+        "status_counts": {str(int(k)): int(v) for k, v in zip(vals, cnts)},
         "latency_by_population": populations,
         "device_memory": {"budget_bytes": mem["budget_bytes"], "peak_counted_bytes": mem["peak_bytes"],
                           "measured_after_last_window_bytes": mem["measured_bytes"]},

@@ -267,8 +267,8 @@ KD_API int kd_store_import(kd_store* st, const uint32_t* keys, int64_t nkeys, co
  * started (its stores and workspaces) plus the device footprint of every
  * buffered or in-flight request (its staging, and about 100 bytes of ingest
  * workspace per ingest pair) must stay within it; submit blocks until there is
- * room, and returns KD_ENOMEM for a request that could not fit alone.  The store's session belongs to the server until it is
- * destroyed.  Query outputs are written to `out` (n doubles, kept valid until
+ * room, and returns KD_ENOMEM for a request that could not fit alone.  The
+ * store's session belongs to the server until it is destroyed.  Query outputs are written to `out` (n doubles, kept valid until
  * the request is waited for); a query of an empty digest completes with
  * KD_EEMPTY and NaN. */
 #define KD_REQ_INGEST 0
@@ -298,6 +298,12 @@ KD_API int kd_server_flush(kd_server* srv);
  * completed, windows served and seconds the worker spent serving windows. */
 KD_API int kd_server_stats(kd_server* srv, double* lat3, int64_t* completed, int64_t* windows,
                            double* busy_s);
+/* Windows that were closed together when the worker took them run as one
+ * group through the pipelined ingest: one window's prep and sort on the device
+ * beside the previous window's queries, compress and commit.  Groups run so
+ * far, and the windows that ran in groups of two or more.  Either pointer may
+ * be NULL. */
+KD_API int kd_server_groups(kd_server* srv, int64_t* groups, int64_t* windows_grouped);
 KD_API void kd_server_destroy(kd_server* srv);
 
 /* Key dictionary.  No counterpart in the reference: GroupedTDigest.add_batch

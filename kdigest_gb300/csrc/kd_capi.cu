@@ -103,7 +103,14 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
   long long nn = std::max(n, w.cap_n), kk = std::max(keys, w.cap_keys);
   long long ii = std::max(inter, w.cap_inter), ww = std::max(work, w.cap_work);
   long long mm = std::max(merged, w.cap_merged), tt = std::max(tmap, w.cap_tmap);
+  // Growth at least doubles a capacity, so a run of ever larger batches
+  // reallocates a logarithmic number of times (each reallocation frees and
+  // synchronises the device).
   if (nn > w.cap_n && w.cap_n > 0) nn = std::max(nn, std::min<long long>(2 * w.cap_n, (1LL << 31) - 1));
+  if (kk > w.cap_keys && w.cap_keys > 0) kk = std::max(kk, 2 * w.cap_keys);
+  if (ii > w.cap_inter && w.cap_inter > 0) ii = std::max(ii, 2 * w.cap_inter);
+  if (ww > w.cap_work && w.cap_work > 0) ww = std::max(ww, 2 * w.cap_work);
+  if (mm > w.cap_merged && w.cap_merged > 0) mm = std::max(mm, 2 * w.cap_merged);
   nn = std::max<long long>(nn, 4096);
   kk = std::max<long long>(kk, 64);
   ii = std::max<long long>(ii, 64);

@@ -329,6 +329,11 @@ int kd_pipeline_quantile(KdSession* s, KdStore* st, const uint32_t* d_keys, cons
 // recur.
 int kd_pipeline_query2(KdSession* s, KdStore* st, const uint32_t* qk, const double* qs, long long nq,
                        double* qout, const uint32_t* ck, const double* xs, long long nc, double* cout);
+// The same kernel enqueued on `str` with no synchronisation; failures (empty
+// digests) go to the caller's device status word `err`.
+int kd_pipeline_query2_enqueue(KdSession* s, KdStore* st, const uint32_t* qk, const double* qs,
+                               long long nq, double* qout, const uint32_t* ck, const double* xs,
+                               long long nc, double* cout, KdErrHost* err, cudaStream_t str);
 // Session device memory with budget accounting (kd_capi.cu).
 int kd_dalloc(KdSession* s, void** p, size_t bytes);
 void kd_dfree(KdSession* s, void* p, size_t bytes);
@@ -344,9 +349,19 @@ int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, lo
 // and every later one are not.
 // With `host_inputs`, the key and value pointers are host memory (pinned or
 // pageable): each batch is first copied into a device staging buffer.
+// Work a caller interleaves with the batches of a multi-batch ingest: before(i)
+// enqueues on `str` what must see the store after batch i - 1 and before batch
+// i (the serving loop's queries of window i).  It is called for every batch,
+// empty ones included, in batch order; after a retry of batch j the batches
+// from j + 1 on are enqueued, and their before() called, once more.
+struct KdBatchHook {
+  void* ctx = nullptr;
+  void (*before)(void* ctx, long long i, cudaStream_t str) = nullptr;
+};
 int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint32_t* const* d_keys,
                             const double* const* d_vals, const long long* ns, int mode,
-                            const double* timestamps, long long* done, bool host_inputs = false);
+                            const double* timestamps, long long* done, bool host_inputs = false,
+                            const KdBatchHook* hook = nullptr);
 void kd_ws_free(KdWorkspace& ws);
 void kd_store_drop_graphs(KdStore* st);
 int kd_cuda_fail(KdSession* s, cudaError_t e, const char* what);

@@ -2492,9 +2492,13 @@ static int pipe_fail(KdSession* s, cudaError_t e) { return kd_cuda_fail(s, e, "p
 
 int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint32_t* const* d_keys,
                             const double* const* d_vals, const long long* ns, int mode,
-                            const double* timestamps, long long* done, bool host_inputs) {
+                            const double* timestamps, long long* done, bool host_inputs,
+                            const KdBatchHook* hook) {
   *done = 0;
   if (nb <= 0) return KD_OK;
+  auto before = [&](long long i, cudaStream_t str) {
+    if (hook && hook->before) hook->before(hook->ctx, i, str);
+  };
   long long nmax = 0;
   for (long long i = 0; i < nb; ++i) {
     if (ns[i] > (1LL << 31) - 1) {
@@ -2505,6 +2509,7 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
     nmax = std::max(nmax, ns[i]);
   }
   if (nmax == 0) {
+    for (long long i = 0; i < nb; ++i) before(i, s->stream);
     *done = nb;
     return KD_OK;
   }
@@ -2624,7 +2629,8 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
       cm = std::max(cm, wp->cap_merged);
     }
     bool room = true;
-    for (KdWorkspace* wp : ws) {
+    for (long long i = base; i < std::min(nb, base + KD_PIPE_WS); ++i) {  // the workspaces in use
+      KdWorkspace* wp = ws[i % KD_PIPE_WS];
       rc = kd_ws_reserve(s, nmax, keys_max, ci, cw, cm, sd.K, wp);
       if (rc == KD_ENOMEM && wp != &s->ws) {
         room = false;  // no memory for the extra workspaces: one call per batch
@@ -2637,6 +2643,7 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
     }
     if (!room) {
       for (long long t = base; t < nb; ++t) {
+        before(t, M);
         const int r = ns[t] > 0 ? single(t) : KD_OK;
         if (r) {
           *done = t;
@@ -2695,7 +2702,10 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
     v.note(cudaStreamWaitEvent(s->ahead2, ev_start, 0));
     for (long long i = base; i < nb; ++i) {
       s->h_many[i] = KdErrHost{0, 0, 0};
-      if (ns[i] == 0) continue;  // an empty batch changes nothing
+      if (ns[i] == 0) {  // an empty batch changes nothing
+        before(i, M);
+        continue;
+      }
       const int k = (int)(i % KD_PIPE_WS);
       KdWorkspace& w = *ws[k];
       // consecutive fronts on two streams, so that they may overlap each other too
@@ -2724,6 +2734,7 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
       run_part(KD_PART_FRONT, k, w, ns[i], A, nullptr, v, capture);
       v.note(cudaEventRecord(ev_copied[k], A));
       v.note(cudaEventRecord(ev_front[k], A));
+      before(i, M);  // after batch i - 1's back, beside batch i's front
       v.note(cudaStreamWaitEvent(M, ev_front[k], 0));
       KdTailOut out{chain, true};
       run_part(KD_PART_BACK, k, w, ns[i], M, &out, v, capture);
@@ -2846,6 +2857,15 @@ int kd_pipeline_query2(KdSession* s, KdStore* st, const uint32_t* qk, const doub
     return w.h_err->code;
   }
   return KD_OK;
+}
+
+int kd_pipeline_query2_enqueue(KdSession* s, KdStore* st, const uint32_t* qk, const double* qs,
+                               long long nq, double* qout, const uint32_t* ck, const double* xs,
+                               long long nc, double* cout, KdErrHost* err, cudaStream_t str) {
+  if (nq + nc <= 0) return KD_OK;
+  const int grid = (int)std::min<long long>((nq + nc + 255) / 256, (long long)s->num_sms * 32);
+  k_query2<<<grid, 256, 0, str>>>(st->d, qk, qs, nq, qout, ck, xs, nc, cout, err);
+  return cudaGetLastError() == cudaSuccess ? KD_OK : KD_ECUDA;
 }
 
 int kd_pipeline_merge(KdSession* s, KdStore* dst, KdStore* src, const long long* h_goff,

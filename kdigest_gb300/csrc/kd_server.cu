@@ -16,10 +16,16 @@
 // stream.  Requests that arrive while earlier windows are on the GPU are
 // admitted into the open window while the session's device memory when the
 // server started (store, workspaces) plus the device footprint of the requests
-// buffered or in flight (staging, and their share of the ingest workspace)
-// stays within the budget; the next closed window's host->device copy runs on
-// a copy stream while the current window computes.  The baseline is fixed, so
-// a request that fits alone is always admitted once the queue drains.
+// buffered or in flight (staging, and their share of the ingest workspaces)
+// stays within the budget.  The baseline is fixed, so a request that fits
+// alone is always admitted once the queue drains.
+//
+// The worker takes every closed window (up to KD_SRV_GROUP) as one group and
+// runs the group through the pipelined multi-batch ingest, one batch per
+// window: window i + 1's prep and sort run on a side stream beside window i's
+// queries, compress and commit, and each window's queries are enqueued between
+// the commits of the windows before and after it.  The next group's
+// host->device copy runs on a copy stream while the current group computes.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -72,11 +78,23 @@ struct Buf {
   cudaEvent_t copied = nullptr;
 };
 
-struct Staged {
+// Windows a worker takes at once (each is one batch of the pipelined ingest).
+#define KD_SRV_GROUP 4
+
+// One window of a staged group: its requests [r0, r1) of the group's list and
+// its place in the group's buffers.
+struct Win {
   long long window = 0;
-  std::vector<std::shared_ptr<Req>> reqs;
-  long long n_ing = 0, n_qq = 0, n_qc = 0;  // ingest pairs, quantile pairs, cdf pairs
-  double ts = 0.0;                          // last ingest timestamp of the window
+  size_t r0 = 0, r1 = 0;
+  long long oi = 0, n_ing = 0;           // ingest pairs at [oi, oi + n_ing)
+  long long oq = 0, n_qq = 0, n_qc = 0;  // quantile pairs from oq, then the cdf pairs
+  double ts = 0.0;                       // last ingest timestamp of the window
+};
+
+struct Staged {
+  std::vector<std::shared_ptr<Req>> reqs;  // window by window, arrival order within
+  std::vector<Win> wins;
+  long long n_ing = 0, n_q = 0;
   int buf = 0;
 };
 
@@ -160,10 +178,12 @@ struct kd_server {
   size_t dev_measured = 0;   // session device memory + staging after the last window
   size_t dev_peak = 0;       // the largest dev_base + buffered_dev seen
   long long completed = 0, windows_done = 0;
+  long long groups = 0, windows_grouped = 0;  // groups run; windows run in groups of two or more
   double busy_s = 0.0;
   int fatal = 0;
   char fatal_msg[256] = {0};
   cudaStream_t copy_stream = nullptr;
+  KdErrHost* d_qerr = nullptr;  // status word of the query kernels (empty digests read as NaN)
   Buf buf[2];
   std::thread worker;
 
@@ -178,119 +198,179 @@ struct kd_server {
 
 namespace {
 
-// Takes the oldest closed window (caller holds the lock) and packs it into
-// buffer `bi`, then starts its host->device copy on the copy stream.
-std::unique_ptr<Staged> take_window(kd_server* v, int bi) {
+// Takes the closed windows, oldest first, up to KD_SRV_GROUP of them (caller
+// holds the lock, at least one window is closed), for buffer set `bi`.
+std::unique_ptr<Staged> take_group(kd_server* v, int bi) {
   auto sg = std::make_unique<Staged>();
-  sg->window = v->pending.front()->window;
   sg->buf = bi;
-  while (!v->pending.empty() && v->pending.front()->window == sg->window) {
-    auto r = v->pending.front();
-    v->pending.pop_front();
-    const long long n = (long long)r->vals.size();
-    if (r->kind == KD_REQ_INGEST) {
-      sg->n_ing += n;
-      sg->ts = r->ts;
-    } else if (r->kind == KD_REQ_QUANTILE) {
-      sg->n_qq += n;
-    } else {
-      sg->n_qc += n;
+  while (sg->wins.size() < KD_SRV_GROUP && v->front_closed()) {
+    Win w;
+    w.window = v->pending.front()->window;
+    w.r0 = sg->reqs.size();
+    w.oi = sg->n_ing;
+    w.oq = sg->n_q;
+    while (!v->pending.empty() && v->pending.front()->window == w.window) {
+      auto r = v->pending.front();
+      v->pending.pop_front();
+      const long long n = (long long)r->vals.size();
+      if (r->kind == KD_REQ_INGEST) {
+        w.n_ing += n;
+        w.ts = r->ts;
+      } else if (r->kind == KD_REQ_QUANTILE) {
+        w.n_qq += n;
+      } else {
+        w.n_qc += n;
+      }
+      sg->reqs.push_back(std::move(r));
     }
-    sg->reqs.push_back(std::move(r));
+    w.r1 = sg->reqs.size();
+    sg->n_ing += w.n_ing;
+    sg->n_q += w.n_qq + w.n_qc;
+    sg->wins.push_back(w);
   }
   return sg;
 }
 
+// Packs the group into its pinned buffers and starts the host->device copy.
 int stage_copy(kd_server* v, Staged& sg) {
   Buf& b = v->buf[sg.buf];
-  if (!grow_buf(b, (size_t)sg.n_ing, (size_t)(sg.n_qq + sg.n_qc))) return KD_ENOMEM;
-
-  long long oi = 0, oq = 0, oc = sg.n_qq;  // quantile pairs first, then cdf pairs
-  for (auto& r : sg.reqs) {
-    const size_t n = r->vals.size();
-    if (r->kind == KD_REQ_INGEST) {
-      memcpy(b.h_ik + oi, r->keys.data(), n * 4);
-      memcpy(b.h_iv + oi, r->vals.data(), n * 8);
-      oi += (long long)n;
-    } else {
-      long long& o = r->kind == KD_REQ_QUANTILE ? oq : oc;
-      memcpy(b.h_qk + o, r->keys.data(), n * 4);
-      memcpy(b.h_qv + o, r->vals.data(), n * 8);
-      o += (long long)n;
+  if (!grow_buf(b, (size_t)sg.n_ing, (size_t)sg.n_q)) return KD_ENOMEM;
+  for (const Win& w : sg.wins) {
+    long long oi = w.oi, oq = w.oq, oc = w.oq + w.n_qq;
+    for (size_t j = w.r0; j < w.r1; ++j) {
+      const Req& r = *sg.reqs[j];
+      const size_t n = r.vals.size();
+      if (r.kind == KD_REQ_INGEST) {
+        memcpy(b.h_ik + oi, r.keys.data(), n * 4);
+        memcpy(b.h_iv + oi, r.vals.data(), n * 8);
+        oi += (long long)n;
+      } else {
+        long long& o = r.kind == KD_REQ_QUANTILE ? oq : oc;
+        memcpy(b.h_qk + o, r.keys.data(), n * 4);
+        memcpy(b.h_qv + o, r.vals.data(), n * 8);
+        o += (long long)n;
+      }
     }
   }
   cudaStream_t cs = v->copy_stream;
-  const long long nq = sg.n_qq + sg.n_qc;
   if (sg.n_ing) {
     cudaMemcpyAsync(b.d_ik, b.h_ik, (size_t)sg.n_ing * 4, cudaMemcpyHostToDevice, cs);
     cudaMemcpyAsync(b.d_iv, b.h_iv, (size_t)sg.n_ing * 8, cudaMemcpyHostToDevice, cs);
   }
-  if (nq) {
-    cudaMemcpyAsync(b.d_qk, b.h_qk, (size_t)nq * 4, cudaMemcpyHostToDevice, cs);
-    cudaMemcpyAsync(b.d_qv, b.h_qv, (size_t)nq * 8, cudaMemcpyHostToDevice, cs);
+  if (sg.n_q) {
+    cudaMemcpyAsync(b.d_qk, b.h_qk, (size_t)sg.n_q * 4, cudaMemcpyHostToDevice, cs);
+    cudaMemcpyAsync(b.d_qv, b.h_qv, (size_t)sg.n_q * 8, cudaMemcpyHostToDevice, cs);
   }
   cudaEventRecord(b.copied, cs);
   return cudaGetLastError() == cudaSuccess ? KD_OK : KD_ECUDA;
 }
 
-// Queries (against the state before the window's ingests), then the ingest.
-void run_window(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>* next) {
+struct HookCtx {
+  kd_server* v;
+  Staged* sg;
+  Buf* b;
+};
+
+// Window i's queries and their read-back, on the ingest's main stream after
+// the commit of window i - 1 and before that of window i.
+void before_window(void* ctx, long long i, cudaStream_t str) {
+  const HookCtx& h = *(const HookCtx*)ctx;
+  const Win& w = h.sg->wins[(size_t)i];
+  const long long nq = w.n_qq + w.n_qc;
+  if (!nq) return;
+  Buf& b = *h.b;
+  const long long oc = w.oq + w.n_qq;
+  kd_pipeline_query2_enqueue(h.v->s, h.v->st, b.d_qk + w.oq, b.d_qv + w.oq, w.n_qq, b.d_qo + w.oq,
+                             b.d_qk + oc, b.d_qv + oc, w.n_qc, b.d_qo + oc, h.v->d_qerr, str);
+  cudaMemcpyAsync(b.h_qo + w.oq, b.d_qo + w.oq, (size_t)nq * 8, cudaMemcpyDeviceToHost, str);
+}
+
+// Runs a staged group: every window's queries (against the state before the
+// window's ingests) and ingest, through the pipelined multi-batch ingest.
+void run_group(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>* next) {
   KdSession* s = v->s;
   Buf& b = v->buf[sg.buf];
   const double t0 = now_s();
-  int ing_rc = stage_rc;
-  const long long nq = sg.n_qq + sg.n_qc;
-  if (stage_rc == KD_OK) {
-    cudaStreamWaitEvent(s->stream, b.copied, 0);
-    if (sg.n_qq) kd_pipeline_quantile(s, v->st, b.d_qk, b.d_qv, sg.n_qq, b.d_qo, 0);
-    if (sg.n_qc) kd_pipeline_quantile(s, v->st, b.d_qk + sg.n_qq, b.d_qv + sg.n_qq, sg.n_qc, b.d_qo + sg.n_qq, 1);
-    if (nq) cudaMemcpyAsync(b.h_qo, b.d_qo, (size_t)nq * 8, cudaMemcpyDeviceToHost, s->stream);
-  }
-  // While this window's ingest runs, the next closed window is packed and its
-  // copy starts on the copy stream (into the other buffer).
+  const long long nw = (long long)sg.wins.size();
+  if (stage_rc == KD_OK) cudaStreamWaitEvent(s->stream, b.copied, 0);
+  // The next group is packed now and its copy runs while this one computes.
   {
     std::unique_lock<std::mutex> lk(v->mu);
     if (!*next && v->front_closed()) {
-      *next = take_window(v, sg.buf ^ 1);
+      *next = take_group(v, sg.buf ^ 1);
       lk.unlock();
       const int rc = stage_copy(v, **next);
       if (rc) (*next)->buf = -rc - 1;  // remember the failure for its turn
     }
   }
-  if (stage_rc == KD_OK && sg.n_ing)
-    ing_rc = kd_pipeline_ingest(s, v->st, b.d_ik, b.d_iv, nullptr, sg.n_ing, KD_MODE_TIME, sg.ts,
-                                nullptr, nullptr, nullptr);
-  if (stage_rc == KD_OK) cudaStreamSynchronize(s->stream);
+  int rc = stage_rc;
+  long long done = 0;  // windows whose ingest committed
+  if (stage_rc == KD_OK) {
+    std::vector<const uint32_t*> dk((size_t)nw);
+    std::vector<const double*> dv((size_t)nw);
+    std::vector<long long> ns((size_t)nw);
+    std::vector<double> ts((size_t)nw);
+    for (long long i = 0; i < nw; ++i) {
+      const Win& w = sg.wins[(size_t)i];
+      dk[(size_t)i] = b.d_ik + w.oi;
+      dv[(size_t)i] = b.d_iv + w.oi;
+      ns[(size_t)i] = w.n_ing;
+      ts[(size_t)i] = w.ts;
+    }
+    HookCtx hc{v, &sg, &b};
+    if (nw == 1) {  // one window: its queries, then the one-call ingest
+      before_window(&hc, 0, s->stream);
+      if (ns[0]) rc = kd_pipeline_ingest(s, v->st, dk[0], dv[0], nullptr, ns[0], KD_MODE_TIME, ts[0],
+                                         nullptr, nullptr, nullptr);
+    } else {
+      KdBatchHook hook;
+      hook.ctx = &hc;
+      hook.before = before_window;
+      rc = kd_pipeline_ingest_many(s, v->st, nw, dk.data(), dv.data(), ns.data(), KD_MODE_TIME,
+                                   ts.data(), &done, false, &hook);
+    }
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess && rc == KD_OK) rc = KD_ECUDA;
+    if (rc == KD_OK) done = nw;
+  }
   const double t1 = now_s();
   std::lock_guard<std::mutex> lk(v->mu);
-  long long oq = 0, oc = sg.n_qq;
-  for (auto& r : sg.reqs) {
-    const size_t n = r->vals.size();
-    if (r->kind == KD_REQ_INGEST) {
-      r->status = ing_rc;
-    } else {
-      long long& o = r->kind == KD_REQ_QUANTILE ? oq : oc;
-      int stt = stage_rc;
-      if (stage_rc == KD_OK) {
-        for (size_t i = 0; i < n; ++i)
-          if (std::isnan(b.h_qo[o + (long long)i])) stt = KD_EEMPTY;  // inputs were validated
-        if (r->out) memcpy(r->out, b.h_qo + o, n * 8);
+  for (long long i = 0; i < nw; ++i) {
+    const Win& w = sg.wins[(size_t)i];
+    // A failed window fails its requests and every later window's (whose
+    // queries would have seen a store without it).
+    const int wrc = (rc != KD_OK && i >= done) ? rc : KD_OK;
+    long long oq = w.oq, oc = w.oq + w.n_qq;
+    for (size_t j = w.r0; j < w.r1; ++j) {
+      Req& r = *sg.reqs[j];
+      const size_t n = r.vals.size();
+      if (r.kind == KD_REQ_INGEST) {
+        r.status = wrc;
+      } else {
+        long long& o = r.kind == KD_REQ_QUANTILE ? oq : oc;
+        int stt = wrc;
+        if (wrc == KD_OK) {
+          for (size_t k = 0; k < n; ++k)
+            if (std::isnan(b.h_qo[o + (long long)k])) stt = KD_EEMPTY;  // inputs were validated
+          if (r.out) memcpy(r.out, b.h_qo + o, n * 8);
+        }
+        o += (long long)n;
+        r.status = stt;
       }
-      o += (long long)n;
-      r->status = stt;
+      r.t_done = t1;
+      std::vector<uint32_t>().swap(r.keys);  // the data is consumed: release it now
+      std::vector<double>().swap(r.vals);
+      v->latencies.push_back(t1 - r.t_submit);
+      v->buffered_dev -= std::min(v->buffered_dev, r.dev_bytes);
+      auto wi = v->win_dev.find(r.window);
+      if (wi != v->win_dev.end() && (wi->second -= std::min(wi->second, r.dev_bytes)) == 0)
+        v->win_dev.erase(wi);
+      ++v->completed;
     }
-    r->t_done = t1;
-    std::vector<uint32_t>().swap(r->keys);  // the data is consumed: release it now
-    std::vector<double>().swap(r->vals);
-    v->latencies.push_back(t1 - r->t_submit);
-    v->buffered_dev -= std::min(v->buffered_dev, r->dev_bytes);
-    auto wi = v->win_dev.find(r->window);
-    if (wi != v->win_dev.end() && (wi->second -= std::min(wi->second, r->dev_bytes)) == 0)
-      v->win_dev.erase(wi);
-    ++v->completed;
   }
   v->dev_measured = v->s->mem_used + buf_dev_bytes(v->buf[0]) + buf_dev_bytes(v->buf[1]);
-  ++v->windows_done;
+  v->windows_done += nw;
+  ++v->groups;
+  if (nw > 1) v->windows_grouped += nw;
   v->busy_s += t1 - t0;
   v->cv.notify_all();
 }
@@ -304,18 +384,18 @@ void worker_main(kd_server* v) {
       std::unique_lock<std::mutex> lk(v->mu);
       v->cv.wait(lk, [&] { return v->front_closed() || (v->stop && v->pending.empty()); });
       if (v->pending.empty()) return;  // stopping
-      cur = take_window(v, bi);
+      cur = take_group(v, bi);
       lk.unlock();
       const int rc = stage_copy(v, *cur);
       if (rc) cur->buf = -rc - 1;
     }
     int stage_rc = KD_OK;
-    if (cur->buf < 0) {  // staging failed: report it on the window's requests
+    if (cur->buf < 0) {  // staging failed: report it on the group's requests
       stage_rc = -cur->buf - 1;
       cur->buf = bi;
     }
     std::unique_ptr<Staged> next;
-    run_window(v, *cur, stage_rc, &next);
+    run_group(v, *cur, stage_rc, &next);
     bi = cur->buf ^ 1;
     cur = std::move(next);
   }
@@ -350,7 +430,12 @@ KD_API int kd_server_create(kd_store* store, double window_s, size_t budget_byte
   // path with the centroids as their priors.
   if (rc == KD_OK) rc = kd_spath_flush(s, &store->st);
   if (rc == KD_OK && cudaStreamCreateWithFlags(&v->copy_stream, cudaStreamNonBlocking) != cudaSuccess) rc = KD_ECUDA;
+  if (rc == KD_OK && cudaMalloc(&v->d_qerr, sizeof(KdErrHost)) != cudaSuccess) rc = KD_ECUDA;
+  if (rc == KD_OK && cudaMemset(v->d_qerr, 0, sizeof(KdErrHost)) != cudaSuccess) rc = KD_ECUDA;
   if (rc) {
+    cudaGetLastError();
+    if (v->copy_stream) cudaStreamDestroy(v->copy_stream);
+    if (v->d_qerr) cudaFree(v->d_qerr);
     delete v;
     return rc;
   }
@@ -507,6 +592,14 @@ KD_API int kd_server_stats(kd_server* v, double* lat3, int64_t* completed, int64
   return KD_OK;
 }
 
+KD_API int kd_server_groups(kd_server* v, int64_t* groups, int64_t* windows_grouped) {
+  if (!v) return KD_EINVAL;
+  std::lock_guard<std::mutex> lk(v->mu);
+  if (groups) *groups = v->groups;
+  if (windows_grouped) *windows_grouped = v->windows_grouped;
+  return KD_OK;
+}
+
 // Drains and stops the worker, then frees the device resources; the handle
 // stays valid for waits and stats.
 static void server_stop(kd_server* v) {
@@ -522,6 +615,8 @@ static void server_stop(kd_server* v) {
   for (Buf& b : v->buf) free_buf(b);
   if (v->copy_stream) cudaStreamDestroy(v->copy_stream);
   v->copy_stream = nullptr;
+  if (v->d_qerr) cudaFree(v->d_qerr);
+  v->d_qerr = nullptr;
 }
 
 KD_API void kd_server_destroy(kd_server* v) {

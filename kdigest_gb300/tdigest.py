@@ -977,10 +977,15 @@ class Server:
         done = ctypes.c_int64(0)
         wins = ctypes.c_int64(0)
         busy = ctypes.c_double(0.0)
-        N.load().kd_server_stats(self._h, N.ptr(lat), ctypes.byref(done), ctypes.byref(wins),
-                                 ctypes.byref(busy))
+        groups = ctypes.c_int64(0)
+        grouped = ctypes.c_int64(0)
+        L = N.load()
+        L.kd_server_stats(self._h, N.ptr(lat), ctypes.byref(done), ctypes.byref(wins),
+                          ctypes.byref(busy))
+        L.kd_server_groups(self._h, ctypes.byref(groups), ctypes.byref(grouped))
         return {"p50_s": lat[0], "p99_s": lat[1], "p999_s": lat[2], "completed": done.value,
-                "windows": wins.value, "busy_s": busy.value}
+                "windows": wins.value, "busy_s": busy.value, "groups": groups.value,
+                "windows_grouped": grouped.value}
 
     def close(self):
         if getattr(self, "_h", None):
