@@ -149,6 +149,13 @@ KD_API int kd_merge(kd_session* s, int scale, double compression, const int64_t*
                     int64_t* out_offsets, double* out_means, double* out_weights, int64_t cap,
                     int64_t* out_n);
 
+/* Self-test of the integer-pipe FP64 helpers the query kernels use (no
+ * counterpart in the reference): element by element over device arrays,
+ * op 0 writes kd_div(a, b), 1 the FP64 a / b, 2 kd_half(a), 3 the FP64
+ * a * 0.5, 4 the order of the helpers' keys of a and b (1 less, 0.5 equal,
+ * 0 greater), 5 the FP64 order of a and b.  Synchronous; b unused by 2 and 3. */
+KD_API int kd_selftest_fp64(int op, const double* a, const double* b, int64_t n, double* out);
+
 /* Resident per-key digests (GroupedTDigest, grouped.mojo:30-58; one key is a
  * TDigest, tdigest.mojo:135-151): num_keys dense ids, shared scale, compression
  * and decay rate (Decay.rate / half_life, decay.mojo:24-47; 0 = none). */

@@ -20,7 +20,8 @@ LIB = os.path.join(HERE, "libkdigest_gb300.so")
 
 SOURCES = ["kd_pipeline.cu", "kd_capi.cu", "kd_noalloc.cu", "kd_server.cu", "kd_serde.cu",
            "kd_keymap.cu", "kd_spath.cu", "kd_stateless.cu"]
-HEADERS = ["kd_math.h", "kd_internal.cuh", "kd_scan.cuh", "kd_sort.cuh", "kd_engine.h", "kd_query.cuh"]
+HEADERS = ["kd_math.h", "kd_internal.cuh", "kd_scan.cuh", "kd_sort.cuh", "kd_engine.h", "kd_query.cuh",
+           "kd_fp64i.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1896,10 +1896,9 @@ __device__ __forceinline__ double store_query(const KdStoreDev& s, uint32_t key,
   d.P = s.prefix + (size_t)key * KD_TILE;
   d.nc = nc;
   d.n = s.total[key];
-  d.mn = s.min_v[key];
-  d.mx = s.max_v[key];
-  d.scaled = s.lambda > 0.0;
-  d.dfac = s.dfac[key];
+  d.mn = s.min_v + key;
+  d.mx = s.max_v + key;
+  d.dfac = s.lambda > 0.0 ? s.dfac + key : nullptr;
   d.single = 1.0 + 1e-9;  // tdigest.mojo:481-483 (effective weight)
   return is_cdf ? kd_cdf_one(d, q) : kd_quantile_one(d, q);
 }

@@ -117,10 +117,9 @@ __global__ void k_sl_query(const int64_t* off, long long nd, const double* m, co
     q.P = P + b;
     q.nc = (int)nc;
     q.n = total[d];
-    q.mn = mn[d];
-    q.mx = mx[d];
-    q.scaled = false;
-    q.dfac = 1.0;
+    q.mn = mn + d;
+    q.mx = mx + d;
+    q.dfac = nullptr;
     q.single = 1.0 + 1e-6;  // the GPU kernels' test on the raw weight (query.mojo:103,113)
     out[i] = is_cdf ? kd_cdf_one(q, qx[i]) : kd_quantile_one(q, qx[i]);
   }
@@ -468,3 +467,33 @@ KD_API int kd_merge(kd_session* h, int scale, double compression, const int64_t*
 }
 
 }  // extern "C"
+
+// Integer-pipe FP64 helpers next to the FP64 instructions they stand for.
+__global__ void k_fp64i_selftest(int op, const double* __restrict__ a, const double* __restrict__ b,
+                                 long long n, double* __restrict__ out) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double x = a[i], y = b ? b[i] : 0.0;
+    double r;
+    switch (op) {
+      case 0: r = kd_div(x, y); break;
+      case 1: r = KD_DIV(x, y); break;
+      case 2: r = kd_half(x); break;
+      case 3: r = KD_MUL(x, 0.5); break;
+      case 4: r = kd_okey(x) < kd_okey(y) ? 1.0 : (kd_okey(x) == kd_okey(y) ? 0.5 : 0.0); break;
+      default: r = x < y ? 1.0 : (x == y ? 0.5 : 0.0); break;
+    }
+    out[i] = r;
+  }
+}
+
+extern "C" KD_API int kd_selftest_fp64(int op, const double* a, const double* b, int64_t n,
+                                       double* out) {
+  if (op < 0 || op > 5 || n < 0 || (n > 0 && (!a || !out || (op != 2 && op != 3 && !b))))
+    return KD_EINVAL;
+  if (n == 0) return KD_OK;
+  const int grid = (int)std::min<long long>((n + 255) / 256, 4096);
+  k_fp64i_selftest<<<grid, 256>>>(op, a, op == 2 || op == 3 ? nullptr : b, n, out);
+  if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return KD_ECUDA;
+  return KD_OK;
+}
