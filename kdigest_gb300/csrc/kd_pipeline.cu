@@ -26,17 +26,10 @@
 #include <vector>
 
 #include "kd_engine.h"
-#include "kd_fp64i.cuh"
 #include "kd_internal.cuh"
 #include "kd_query.cuh"
 #include "kd_scan.cuh"
 #include "kd_sort.cuh"
-
-// w * x of a segment sum: a unit weight (every new sample of an unweighted
-// batch) leaves x unchanged, exactly, with no FP64 multiply.
-__device__ __forceinline__ double kd_wx(double w, double x) {
-  return kd_dbits(w) == 0x3ff0000000000000ull ? x : KD_MUL(w, x);
-}
 
 #define KD_ERANGE_SCRATCH KD_ERANGE_SCRATCH_INTERNAL  // scratch too small (index = needed)
 #define KD_EMORE_LEVELS 101    // internal: keys still above one tile after the levels run
@@ -461,11 +454,11 @@ __device__ int warp_compress(WarpTileSmall& t, int n, int scale, double compress
       continue;
     }
     T aw = A::from_w(t.w[h]);
-    double awx = kd_wx(t.w[h], t.x[h]);
+    double awx = KD_MUL(t.w[h], t.x[h]);
     for (int i = h + 1; i <= e; ++i) {
       const double wi = t.w[i];
       if (kInt) aw = A::add(aw, A::from_w(wi));
-      awx = KD_ADD(awx, kd_wx(wi, t.x[i]));
+      awx = KD_ADD(awx, KD_MUL(wi, t.x[i]));
     }
     if (kInt) t.L[e] = A::store(aw);
     t.w[e] = awx;
@@ -508,7 +501,7 @@ __device__ int warp_compress(WarpTileSmall& t, int n, int scale, double compress
     const int h = t.headpos[sI];
     const double sw = A::to_d(A::load(t.L[e]));
     const double lo_v = t.x[h], hi_v = t.x[e];
-    double mean = kd_div(t.w[e], sw);
+    double mean = KD_DIV(t.w[e], sw);
     const uint64_t km = kd_order_key(mean);
     if (km < kd_order_key(lo_v)) mean = lo_v;
     else if (km > kd_order_key(hi_v)) mean = hi_v;
@@ -776,11 +769,11 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
         continue;
       }
       T aw = A::from_w(t.w[h]);
-      double awx = kd_wx(t.w[h], t.x[h]);
+      double awx = KD_MUL(t.w[h], t.x[h]);
       for (int i = h + 1; i <= e; ++i) {
         const double wi = t.w[i];
         if (kInt) aw = A::add(aw, A::from_w(wi));
-        awx = KD_ADD(awx, kd_wx(wi, t.x[i]));
+        awx = KD_ADD(awx, KD_MUL(wi, t.x[i]));
       }
       if (kInt) t.L[e] = A::store(aw);
       t.w[e] = awx;
@@ -815,7 +808,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
       for (int j = 0; j < cnt; ++j) {
         const int sp = slot(lo + j);
         const double wi = t.w[sp], xi = t.x[sp];
-        const double wx = kd_wx(wi, xi);
+        const double wx = KD_MUL(wi, xi);
         const bool hd = t.hf[sp];
         if (hd || j == 0) {
           if (kInt) aw = A::from_w(wi);
@@ -932,7 +925,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
     const int se = slot(e), sh = slot(h);
     const double sw = A::to_d(A::load(t.L[se]));
     const double lo_v = t.x[sh], hi_v = t.x[se];
-    double mean = kd_div(t.w[se], sw);
+    double mean = KD_DIV(t.w[se], sw);
     const uint64_t km = kd_order_key(mean);
     if (km < kd_order_key(lo_v)) mean = lo_v;
     else if (km > kd_order_key(hi_v)) mean = hi_v;
