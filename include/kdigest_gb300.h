@@ -177,8 +177,11 @@ KD_API int kd_store_ingest(kd_store* st, const uint32_t* keys, const double* val
  * *batches_done (may be NULL) receives its position (nbatch on success).
  * Device pointers (KD_PTR_DEVICE) are read in place; host memory (pinned or
  * pageable) is copied batch by batch into device staging buffers by the copy
- * engine while earlier batches compute.  No reference counterpart beyond the
- * add_batch loop it replaces. */
+ * engine while earlier batches compute.  Under a session memory budget with
+ * no room for the two extra ingest workspaces the batches run one
+ * kd_store_ingest each (same results); a budget with no room for the staging
+ * buffers of host inputs returns KD_ENOMEM before any batch runs.  No
+ * reference counterpart beyond the add_batch loop it replaces. */
 KD_API int kd_store_ingest_many(kd_store* st, int64_t nbatch, const uint32_t* const* keys,
                                 const double* const* values, const int64_t* n, int clock_mode,
                                 const double* timestamps, int flags, int64_t* batches_done);

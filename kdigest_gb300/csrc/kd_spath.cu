@@ -140,6 +140,7 @@ struct SpSh {
   long long tot_base;  // the stored total in units of tot_u
   int C, B, err, nc, mismatch, unsorted, exact, cut, renorm, pre_adv, integral, fast, filt;
   int longreach;  // a cluster start whose reach passed 64 candidates
+  int mm_first;   // first candidate whose speculated decision the exact test overturned
   int bfail;      // a bucket of the buffer merge was too large
   int nruns;      // runs of the exponent in the current buffer fill
   long long wsum[32];  // per-warp partial sums of block scans and reductions
@@ -582,6 +583,7 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
     sh.B = 0;
     sh.exact = 1;
     sh.mismatch = 0;
+    sh.mm_first = 0x7fffffff;
     sh.longreach = 0;
   }
   __syncthreads();
@@ -841,13 +843,18 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
       double cur_m = sm[s0];
 #pragma unroll 4
       for (int j = s0 + 1; j < e; ++j) cur_m = KD_ADD(cur_m, KD_MUL(KD_SUB(sm[j], cur_m), ratio[j]));
-      if (e < W && sm[e] == cur_m) sh.mismatch = 1;  // the reference coalesces an exact mean tie
+      if (e < W && sm[e] == cur_m) {  // the reference coalesces an exact mean tie
+        sh.mismatch = 1;
+        atomicMin(&sh.mm_first, e);
+      }
       m.cm[t] = cur_m;
     }
     __syncthreads();
   }
   // 7. non-integral weights: re-check every decision with the chain's exact sums
-  if (!exact && !sh.mismatch) {
+  //    (also after a mean tie in step 6, so that mm_first is the first
+  //    overturned decision of all)
+  if (!exact) {
     if (threadIdx.x == 0) {
       double acc = 0.0;
       for (int t = 0; t < nc; ++t) {
@@ -881,22 +888,39 @@ __device__ __noinline__ void sp_merge(const SpArgs& a, const SpMem& m, SpSh& sh,
         fits = KD_SUB(sp_k(scale, KD_DIV(num, st), nrm), sp_k(scale, KD_DIV(m.wsf[tt], st), nrm)) <=
                1.0;
       }
-      if (start) {
-        if (fits) sh.mismatch = 1;
-      } else if (!fits && !(sm[j] == sm[m.cst[tt]])) {
+      if (start ? fits : (!fits && !(sm[j] == sm[m.cst[tt]]))) {
         sh.mismatch = 1;
+        atomicMin(&sh.mm_first, j);
       }
     }
     __syncthreads();
   }
-  // 8. mismatch: the reference loop, one thread
+  // 8. mismatch: the reference loop, one thread.  With non-integral weights it
+  //    resumes at the first overturned candidate j0: every decision before j0
+  //    is the reference's, so the clusters before the one holding j0 - 1 are
+  //    final, and that cluster's state is rebuilt with the reference's own
+  //    operations (weights before it summed in order, its running mean from
+  //    the ratios step 6 left in kk, its running weight from rw).
   if (sh.mismatch) {
     if (threadIdx.x == 0) {
       double wsf = 0.0, cur_m = sm[0], cur_w = sw[0];
+      int k = 0, i0 = 1;
+      const int j0 = sh.mm_first;
+      if (!exact && j0 > 0 && j0 < W) {
+        const int t = m.cid[j0];
+        const int tt = m.cst[t] == j0 ? t - 1 : t;  // the cluster holding j0 - 1
+        for (int u = 0; u < tt; ++u) wsf = KD_ADD(wsf, m.cw[u]);
+        const int s0 = m.cst[tt];
+        const double* ratio = m.kk;
+        cur_m = sm[s0];
+        for (int j = s0 + 1; j < j0; ++j) cur_m = KD_ADD(cur_m, KD_MUL(KD_SUB(sm[j], cur_m), ratio[j]));
+        cur_w = m.rw[j0];
+        k = tt;
+        i0 = j0;
+      }
       double kq = sp_k(scale, KD_DIV(wsf, st), nrm);
-      int k = 0;
       bool overflow = false;
-      for (int i = 1; i < W; ++i) {
+      for (int i = i0; i < W; ++i) {
         const double qr = KD_DIV(KD_ADD(KD_ADD(wsf, cur_w), sw[i]), st);
         const double span = KD_SUB(sp_k(scale, qr, nrm), kq);
         if (sm[i] == cur_m || span <= 1.0) {

@@ -81,6 +81,28 @@ def test_count_decay_renormalise_and_prune(kd, oracle, half_life):
     _same_queries(d, od, xs=(0.1, 0.5, 1.0, 2.0, 10.0))
 
 
+@pytest.mark.parametrize("scale", [0, 1])
+def test_count_decay_unclamped_scales(kd, oracle, scale):
+    """K0 and K1 do not clamp q (scale.mojo:91-118): with decayed weights the
+    chain's sum can round above the stored total, so K1 meets asin just above
+    1 (NaN: the candidate does not fit) at the end of a merge pass, where the
+    parallel sweep's speculation assumed the end value; the pass then resumes
+    the reference loop at the overturned candidate.  Config 1's stream with a
+    10^5-sample half-life, a quarter of it."""
+    dec = kd.Decay.half_life(1e5)
+    d = kd.TDigest(100.0, scale, decay=dec)
+    od = oracle.Digest(scale, 100.0, dec.rate_lambda)
+    rng = np.random.default_rng(31 + scale)
+    vals = rng.standard_normal(250_000)
+    for b in range(0, len(vals), 4096):
+        d.add_batch(vals[b:b + 4096])
+        od.add_many(vals[b:b + 4096])
+        if b % (16 * 4096) == 0:
+            _same(d, od)
+    _same(d, od)
+    _same_queries(d, od)
+
+
 def test_add_at_weighted_and_time_decay(kd, oracle):
     dec = kd.Decay.half_life(10.0)
     d = kd.TDigest(100.0, kd.K3, decay=dec)
