@@ -161,6 +161,31 @@ def test_budget_backpressure_keeps_results(kd):
     _compare(kd, ga, ra, gb, rb)
 
 
+def test_retry_inside_a_window_group(kd):
+    """A window whose batch needs the full sort (more than 64 values of one key
+    that agree in every sorted bit, out of order) is retried by itself inside
+    its group; the later windows of the group run again, queries included, on
+    the retried store.  Every result is still the same as alone."""
+    rng = np.random.default_rng(15)
+    reqs = [("ingest", 0.0, np.arange(NK, dtype=np.uint32), rng.lognormal(0, 2, NK))]
+    for w in range(40):
+        t = 0.0021 + w * 1e-3
+        k = int(rng.integers(0, NK))
+        base = 1.0 + float(rng.integers(0, 1 << 20)) * 2.0 ** -20  # low 32 significand bits zero
+        tied = base + rng.permutation(100) * 2.0 ** -52              # differ in the lowest 7 bits
+        reqs.append(("ingest", t, np.full(100, k, np.uint32), tied))
+        reqs.append(("ingest", t + 1e-5, rng.integers(0, NK, 500).astype(np.uint32),
+                     rng.lognormal(0, 2, 500)))
+        reqs.append(("quantile", t + 2e-5, rng.integers(0, NK, 20).astype(np.uint32), rng.random(20)))
+        reqs.append(("cdf", t + 3e-5, rng.integers(0, NK, 20).astype(np.uint32),
+                     rng.lognormal(0, 2, 20)))
+    window = 1e-3
+    ga, ra, st = _serve(kd, reqs, window)
+    gb, rb = _alone(kd, reqs, window)
+    _compare(kd, ga, ra, gb, rb)
+    assert st["windows_grouped"] > 0  # full-sort windows keep the worker behind the client
+
+
 def test_concurrent_waiters(kd):
     """Waiters on other threads see their own results while the client submits."""
     reqs = _trace(14, 200, 2e-4)
