@@ -1112,6 +1112,7 @@ def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
         gc.enable()
     st = srv.stats()
     mem = srv.memory()
+    alloc = sess.alloc_stats()
     lat = np.empty(len(tickets))
     status = np.empty(len(tickets), np.int64)
     for i, tk in enumerate(tickets):
@@ -1150,6 +1151,10 @@ def run_serve(seconds: float, window: float, rate: float = SERVE_RATE) -> dict:
         "query_pairs_per_s": round(q_pairs / t_all, 1),
         "windows": st["windows"], "window_groups": st["groups"],
         "windows_in_overlapped_groups": st["windows_grouped"],
+        "longest_group_ms": round(st["max_group_s"] * 1e3, 3), "groups_over_10ms": st["slow_groups"],
+        "group_staging_s": round(st["stage_s"], 3),
+        "workspace_growths": alloc["workspace_growths"],
+        "workspace_growth_s": round(alloc["workspace_growth_s"], 3),
         "gpu_worker_busy_frac": round(st["busy_s"] / (t_all + (t_meas - t0)), 3),
         "client_max_lag_ms": round(lag * 1e3, 3), "submit_seconds": round(t_sub, 3),
         "status_counts": {str(int(k)): int(v) for k, v in zip(vals, cnts)},

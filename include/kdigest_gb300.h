@@ -86,7 +86,13 @@ KD_API void kd_session_destroy(kd_session* s);
 KD_API const char* kd_last_error(kd_session* s);
 KD_API int kd_session_sync(kd_session* s);
 KD_API int kd_session_set_option(kd_session* s, int option, int value);
-/* The CUDA stream (cudaStream_t) all work of this session is ordered on. */
+/* Ingest workspace (re)allocations of this session so far and the host seconds
+ * they took (each frees the old buffers, which waits for the device).  Either
+ * pointer may be NULL. */
+KD_API int kd_session_alloc_stats(kd_session* s, int64_t* grows, double* seconds);
+/* The CUDA stream (cudaStream_t) all work of this session is ordered on.  It
+ * is created at the device's highest stream priority, so work a caller
+ * enqueues on other streams yields SMs to it. */
 KD_API void* kd_session_stream(kd_session* s);
 /* Accumulated per-stage device milliseconds of ingests (prep, sort, plan, level0,
  * levels, commit; recorded when KD_OPT_STAGE_TIMING is on), kernels launched and
@@ -311,9 +317,12 @@ KD_API int kd_server_stats(kd_server* srv, double* lat3, int64_t* completed, int
 /* Windows that were closed together when the worker took them run as one
  * group through the pipelined ingest: one window's prep and sort on the device
  * beside the previous window's queries, compress and commit.  Groups run so
- * far, and the windows that ran in groups of two or more.  Either pointer may
- * be NULL. */
-KD_API int kd_server_groups(kd_server* srv, int64_t* groups, int64_t* windows_grouped);
+ * far, the windows that ran in groups of two or more, the longest group in
+ * seconds (queries, ingest and completion), the groups that took longer than
+ * 10 ms, and the seconds the worker spent packing groups and starting their
+ * copies (buffer growth included).  Any pointer may be NULL. */
+KD_API int kd_server_groups(kd_server* srv, int64_t* groups, int64_t* windows_grouped,
+                            double* max_group_s, int64_t* slow_groups, double* stage_s);
 KD_API void kd_server_destroy(kd_server* srv);
 
 /* Key dictionary.  No counterpart in the reference: GroupedTDigest.add_batch

@@ -39,6 +39,7 @@ EXPORTED = (
     "kd_store_add", "kd_store_flush", "kd_store_merge_into", "kd_store_ingest_many",
     "kd_store_query_batch", "kd_grouped_compress", "kd_quantile", "kd_cdf", "kd_merge",
     "kd_server_latency", "kd_server_memory", "kd_server_groups", "kd_selftest_fp64",
+    "kd_session_alloc_stats",
 )
 KD_REQ_INGEST, KD_REQ_QUANTILE, KD_REQ_CDF = 0, 1, 2
 
@@ -117,8 +118,10 @@ def load(path: str = LIB_PATH):
     L.kd_server_latency.argtypes = [_P, _I64, ctypes.POINTER(_D)]
     L.kd_server_memory.argtypes = [_P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t),
                                    ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
-    L.kd_server_groups.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]
+    L.kd_server_groups.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                                   ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_D)]
     L.kd_selftest_fp64.argtypes = [ctypes.c_int, _P, _P, _I64, _P]
+    L.kd_session_alloc_stats.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_D)]
     L.kd_compress_noalloc.argtypes = [ctypes.c_int, _D, _P, _P, _I64, ctypes.c_int, _P, _P, _I64,
                                       ctypes.POINTER(_I64), _P, ctypes.c_char_p, ctypes.c_int]
     L.kd_store_stats.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),

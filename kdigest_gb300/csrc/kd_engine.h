@@ -177,6 +177,8 @@ struct KdSession {
   cudaStream_t stream = nullptr;
   size_t mem_budget = 0;
   size_t mem_used = 0;
+  long long ws_grows = 0;   // ingest workspace (re)allocations
+  double ws_grow_s = 0.0;   // host seconds spent in them (frees synchronise the device)
   int num_sms = 0;
   int force_exact = 0;
   int max_levels = 32;
@@ -341,6 +343,14 @@ int kd_pipeline_merge(KdSession* s, KdStore* dst, KdStore* src, const long long*
                       const uint32_t* h_parts, long long ngroups);
 int kd_store_alloc(KdSession* s, KdStore* st);
 void kd_store_free(KdStore* st);
+// The batch capacity a workspace is sized for: its own when the batch fits,
+// else at least twice it.  Callers derive every other capacity from it, so a
+// run of ever larger batches reallocates once per doubling of the batch.
+inline long long kd_ws_batch_cap(long long n, long long cap_n) {
+  if (n <= cap_n) return cap_n;
+  const long long twice = cap_n < (1LL << 30) ? 2 * cap_n : (1LL << 31) - 1;
+  return n > twice ? n : twice;
+}
 int kd_ws_reserve(KdSession* s, long long n, long long keys, long long inter, long long work,
                   long long merged, long long tmap, KdWorkspace* wp = nullptr);
 // Batches folded in order as if by one kd_pipeline_ingest each (unit weights),

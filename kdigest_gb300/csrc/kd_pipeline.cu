@@ -2455,13 +2455,14 @@ int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const 
   }
   int rc = kd_pipeline_prepare_device(s);
   if (rc) return rc;
-  const long long keys_max = std::min<long long>(n, st->d.K);
-  long long want_inter = std::max<long long>(64, 2 * (n / KD_TILE) + 64);
-  long long want_work = 2 * keys_max + n / KD_TILE + 64;
-  long long want_merged = 2 * n + 64 * keys_max + 1024;
+  const long long ncap = kd_ws_batch_cap(n, s->ws.err ? s->ws.cap_n : 0);
+  const long long keys_max = std::min<long long>(ncap, st->d.K);
+  long long want_inter = std::max<long long>(64, 2 * (ncap / KD_TILE) + 64);
+  long long want_work = 2 * keys_max + ncap / KD_TILE + 64;
+  long long want_merged = 2 * ncap + 64 * keys_max + 1024;
   for (int attempt = 0; attempt < 4; ++attempt) {
     KdWorkspace& w0 = s->ws;
-    rc = kd_ws_reserve(s, n, keys_max, std::max(want_inter, w0.cap_inter),
+    rc = kd_ws_reserve(s, ncap, keys_max, std::max(want_inter, w0.cap_inter),
                        std::max(want_work, w0.cap_work), std::max(want_merged, w0.cap_merged), st->d.K);
     if (rc) return rc;
     rc = kd_pipeline_attempt(s, st, s->ws, d_keys, d_vals, d_wts, n, mode, timestamp, d_merge_min,
@@ -2515,7 +2516,6 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
   int rc = kd_pipeline_prepare_device(s);
   if (rc) return rc;
   const KdStoreDev sd = st->d;
-  const long long keys_max = std::min<long long>(nmax, sd.K);
   if (!s->ahead) {
     if (cudaStreamCreateWithFlags(&s->ahead, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->ahead2, cudaStreamNonBlocking) != cudaSuccess ||
@@ -2616,12 +2616,17 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
   for (int q = 1; q < KD_PIPE_WS; ++q) ws[q] = &s->ws_more[q - 1];
   long long base = 0;  // batches before it are committed
   while (base < nb) {
-    // Every workspace sized as the one-call path sizes its own for the
-    // largest batch, and at least as large as any already is (a retry on the
-    // one-call path may have grown the first).
-    long long ci = std::max(64LL, 2 * (nmax / KD_TILE) + 64);
-    long long cw = 2 * keys_max + nmax / KD_TILE + 64;
-    long long cm = 2 * nmax + 64 * keys_max + 1024;
+    // Every workspace sized as the one-call path sizes its own (from one batch
+    // capacity for the largest batch), and at least as large as any already
+    // is (a retry on the one-call path may have grown the first); all get the
+    // same request, so they grow together.
+    long long capn = 0;
+    for (KdWorkspace* wp : ws) capn = std::max(capn, wp->err ? wp->cap_n : 0LL);
+    const long long ncap = kd_ws_batch_cap(nmax, capn);
+    const long long kcap = std::min<long long>(ncap, sd.K);
+    long long ci = std::max(64LL, 2 * (ncap / KD_TILE) + 64);
+    long long cw = 2 * kcap + ncap / KD_TILE + 64;
+    long long cm = 2 * ncap + 64 * kcap + 1024;
     for (KdWorkspace* wp : ws) {
       ci = std::max(ci, wp->cap_inter);
       cw = std::max(cw, wp->cap_work);
@@ -2630,7 +2635,7 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
     bool room = true;
     for (long long i = base; i < std::min(nb, base + KD_PIPE_WS); ++i) {  // the workspaces in use
       KdWorkspace* wp = ws[i % KD_PIPE_WS];
-      rc = kd_ws_reserve(s, nmax, keys_max, ci, cw, cm, sd.K, wp);
+      rc = kd_ws_reserve(s, ncap, kcap, ci, cw, cm, sd.K, wp);
       if (rc == KD_ENOMEM && wp != &s->ws) {
         room = false;  // no memory for the extra workspaces: one call per batch
         break;

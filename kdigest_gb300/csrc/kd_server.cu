@@ -80,6 +80,11 @@ struct Buf {
 
 // Windows a worker takes at once (each is one batch of the pipelined ingest).
 #define KD_SRV_GROUP 4
+// A window with more ingest pairs than this runs alone through the one-call
+// ingest: the pipelined ingest sizes every workspace it uses for its largest
+// batch, so a large window inside a group would grow all three (gigabytes at a
+// million keys, each growth a device-wide synchronisation).
+#define KD_SRV_GROUP_BIG (1LL << 18)
 
 // One window of a staged group: its requests [r0, r1) of the group's list and
 // its place in the group's buffers.
@@ -179,6 +184,9 @@ struct kd_server {
   size_t dev_peak = 0;       // the largest dev_base + buffered_dev seen
   long long completed = 0, windows_done = 0;
   long long groups = 0, windows_grouped = 0;  // groups run; windows run in groups of two or more
+  double max_group_s = 0.0;  // the longest group, from its take to its completion
+  long long slow_groups = 0; // groups that took longer than 10 ms
+  double stage_s = 0.0;      // host packing and copy set-up of groups (allocation included)
   double busy_s = 0.0;
   int fatal = 0;
   char fatal_msg[256] = {0};
@@ -204,6 +212,12 @@ std::unique_ptr<Staged> take_group(kd_server* v, int bi) {
   auto sg = std::make_unique<Staged>();
   sg->buf = bi;
   while (sg->wins.size() < KD_SRV_GROUP && v->front_closed()) {
+    long long ing = 0;  // the front window's ingest pairs
+    for (const auto& r : v->pending) {
+      if (r->window != v->pending.front()->window) break;
+      if (r->kind == KD_REQ_INGEST) ing += (long long)r->vals.size();
+    }
+    if (!sg->wins.empty() && ing > KD_SRV_GROUP_BIG) break;  // a large window runs alone
     Win w;
     w.window = v->pending.front()->window;
     w.r0 = sg->reqs.size();
@@ -227,6 +241,7 @@ std::unique_ptr<Staged> take_group(kd_server* v, int bi) {
     sg->n_ing += w.n_ing;
     sg->n_q += w.n_qq + w.n_qc;
     sg->wins.push_back(w);
+    if (w.n_ing > KD_SRV_GROUP_BIG) break;  // and nothing joins it
   }
   return sg;
 }
@@ -299,7 +314,9 @@ void run_group(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>* 
     if (!*next && v->front_closed()) {
       *next = take_group(v, sg.buf ^ 1);
       lk.unlock();
+      const double ts0 = now_s();
       const int rc = stage_copy(v, **next);
+      v->stage_s += now_s() - ts0;  // the worker thread alone writes it
       if (rc) (*next)->buf = -rc - 1;  // remember the failure for its turn
     }
   }
@@ -372,6 +389,8 @@ void run_group(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>* 
   ++v->groups;
   if (nw > 1) v->windows_grouped += nw;
   v->busy_s += t1 - t0;
+  v->max_group_s = std::max(v->max_group_s, t1 - t0);
+  if (t1 - t0 > 0.010) ++v->slow_groups;
   v->cv.notify_all();
 }
 
@@ -386,7 +405,9 @@ void worker_main(kd_server* v) {
       if (v->pending.empty()) return;  // stopping
       cur = take_group(v, bi);
       lk.unlock();
+      const double ts0 = now_s();
       const int rc = stage_copy(v, *cur);
+      v->stage_s += now_s() - ts0;
       if (rc) cur->buf = -rc - 1;
     }
     int stage_rc = KD_OK;
@@ -592,11 +613,15 @@ KD_API int kd_server_stats(kd_server* v, double* lat3, int64_t* completed, int64
   return KD_OK;
 }
 
-KD_API int kd_server_groups(kd_server* v, int64_t* groups, int64_t* windows_grouped) {
+KD_API int kd_server_groups(kd_server* v, int64_t* groups, int64_t* windows_grouped,
+                            double* max_group_s, int64_t* slow_groups, double* stage_s) {
   if (!v) return KD_EINVAL;
   std::lock_guard<std::mutex> lk(v->mu);
   if (groups) *groups = v->groups;
   if (windows_grouped) *windows_grouped = v->windows_grouped;
+  if (max_group_s) *max_group_s = v->max_group_s;
+  if (slow_groups) *slow_groups = v->slow_groups;
+  if (stage_s) *stage_s = v->stage_s;
   return KD_OK;
 }
 

@@ -107,6 +107,13 @@ class GpuSession:
     def reset_stats(self):
         N.load().kd_session_reset_stats(self._h)
 
+    def alloc_stats(self) -> dict:
+        """Ingest workspace (re)allocations so far and the host seconds they took."""
+        grows = ctypes.c_int64(0)
+        sec = ctypes.c_double(0.0)
+        N.load().kd_session_alloc_stats(self._h, ctypes.byref(grows), ctypes.byref(sec))
+        return {"workspace_growths": grows.value, "workspace_growth_s": sec.value}
+
     @property
     def stream(self) -> int:
         return N.load().kd_session_stream(self._h) or 0
@@ -979,13 +986,18 @@ class Server:
         busy = ctypes.c_double(0.0)
         groups = ctypes.c_int64(0)
         grouped = ctypes.c_int64(0)
+        gmax = ctypes.c_double(0.0)
+        slow = ctypes.c_int64(0)
+        stage = ctypes.c_double(0.0)
         L = N.load()
         L.kd_server_stats(self._h, N.ptr(lat), ctypes.byref(done), ctypes.byref(wins),
                           ctypes.byref(busy))
-        L.kd_server_groups(self._h, ctypes.byref(groups), ctypes.byref(grouped))
+        L.kd_server_groups(self._h, ctypes.byref(groups), ctypes.byref(grouped), ctypes.byref(gmax),
+                           ctypes.byref(slow), ctypes.byref(stage))
         return {"p50_s": lat[0], "p99_s": lat[1], "p999_s": lat[2], "completed": done.value,
                 "windows": wins.value, "busy_s": busy.value, "groups": groups.value,
-                "windows_grouped": grouped.value}
+                "windows_grouped": grouped.value, "max_group_s": gmax.value,
+                "slow_groups": slow.value, "stage_s": stage.value}
 
     def close(self):
         if getattr(self, "_h", None):
