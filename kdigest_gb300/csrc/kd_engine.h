@@ -187,7 +187,7 @@ struct KdSession {
   // sent to the small-tile kernel, and resident blocks per SM of the two tile
   // kernels.  Defaults are the committed autotuner choice for GB300.
   int small_cap = 128;
-  int large_bps = 7;
+  int large_bps = 6;
   int small_bps = 8;
   // Run a level's two tile kernels on two streams (the second joins back
   // before anything reads their outputs).  Also a launch setting only.

@@ -12,11 +12,13 @@ The tuner builds a store in the steady state of a Zipf-keyed grouped ingest
 up), then runs a coordinate descent over
     small tile cap   in {32, 64, 96, 128}
     large blocks/SM  in {4, 5, 6, 7, 8}
-    small blocks/SM  in {4, 6, 8, 12, 16}
+    small blocks/SM  in {4, 6, 8, 10, 12, 16}
     concurrent tiles in {0, 1} (the two kernels of a level on two streams)
-timing each candidate as the median device time (CUDA events on the session
-stream) of several ingest steps, and writes the measurements and the choice to
-tuning/gb300.json.  GpuSession applies that file's choice; the library's
+timing each candidate on the headline's form of the step: the pipelined
+multi-batch ingest (add_batches, one batch's sort beside the previous batch's
+compress), per batch, median of three calls of 13 batches, CUDA events on the
+session stream (--objective per-call times one kd_store_ingest per batch
+instead).  It writes the measurements and the choice to tuning/gb300.json.  GpuSession applies that file's choice; the library's
 built-in defaults (KdSession in csrc/kd_engine.h) are set to it.
 
     python -m kdigest_gb300.tune [--out kdigest_gb300/tuning/gb300.json]
@@ -34,7 +36,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TUNING_FILE = os.path.join(HERE, "tuning", "gb300.json")
 PARAMS = (("small_tile_cap", 5, (32, 64, 96, 128)),
           ("large_blocks_per_sm", 6, (4, 5, 6, 7, 8)),
-          ("small_blocks_per_sm", 7, (4, 6, 8, 12, 16)),
+          ("small_blocks_per_sm", 7, (4, 6, 8, 10, 12, 16)),
           ("concurrent_tiles", 8, (0, 1)))
 # the starting point of the search (the launch shapes before tuning)
 DEFAULTS = {"small_tile_cap": 128, "large_blocks_per_sm": 6, "small_blocks_per_sm": 8,
@@ -76,6 +78,7 @@ def main(argv=None) -> int:
     ap.add_argument("--keys", type=int, default=65536)
     ap.add_argument("--batch", type=int, default=1 << 22)
     ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--objective", choices=["pipelined", "per-call"], default="pipelined")
     args = ap.parse_args(argv)
 
     import torch
@@ -105,7 +108,7 @@ def main(argv=None) -> int:
         step()
     torch.cuda.synchronize()
 
-    def measure(cfg: dict) -> float:
+    def measure_per_call(cfg: dict) -> float:
         apply_tuning(sess, cfg)
         step()  # first step of a new shape runs eagerly, the second captures
         step()
@@ -119,6 +122,22 @@ def main(argv=None) -> int:
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
         return statistics.median(times)
+
+    def measure_pipelined(cfg: dict) -> float:
+        apply_tuning(sess, cfg)
+        store.add_batches(d_batches[:3])  # captures this shape's graphs
+        times = []
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            store.add_batches(d_batches[3:])
+            e1.record(ext)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / (len(d_batches) - 3))
+        return statistics.median(times)
+
+    measure = measure_pipelined if args.objective == "pipelined" else measure_per_call
 
     cur = dict(DEFAULTS)
     log = []
@@ -158,7 +177,10 @@ def main(argv=None) -> int:
         "sms": torch.cuda.get_device_properties(0).multi_processor_count,
         "workload": f"grouped ingest, {args.keys} Zipf(1.1) K3 keys, compression 100, "
                     f"batches of {args.batch} in steady state",
-        "timing": f"median of {args.steps} steps, CUDA events on the session stream",
+        "timing": ("per batch, median of three pipelined add_batches calls of "
+                   f"{len(d_batches) - 3} batches" if args.objective == "pipelined"
+                   else f"median of {args.steps} one-call steps") + ", CUDA events on the session stream",
+        "objective": args.objective,
         "default": DEFAULTS, "default_ms": default_ms,
         "choice": cur, "choice_ms": chosen_ms, "results_identical": same,
         "measurements": log,
