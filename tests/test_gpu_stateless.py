@@ -233,3 +233,38 @@ def test_query_batch_one_launch_equals_two_calls(kd):
                                     co.data_ptr(), N.KD_PTR_DEVICE)
         assert rc == 0
         assert np.array_equal(qo.cpu().numpy(), eq) and np.array_equal(co.cpu().numpy(), ec), rep
+
+
+@pytest.mark.parametrize("nk,decay", [(1024, False), (300, True)])
+def test_query_batch_many_queries_per_digest(kd, nk, decay):
+    """A batch of hundreds of queries per digest in one launch gives the same
+    bits as the per-call queries, for interior points, both tails, q = 0 and 1,
+    x outside the range, ties and decayed (singleton-tested) digests."""
+    rng = np.random.default_rng(nk)
+    dec = kd.Decay.half_life(5e4) if decay else None
+    g = kd.GroupedTDigest(nk, 100.0, scale=kd.K2, decay=dec, session=kd.GpuSession())
+    for _ in range(3):
+        keys = rng.integers(0, nk, 200000).astype(np.uint32)
+        vals = np.round(rng.standard_normal(200000) * 4) / 4  # ties
+        g.add_batch(keys, vals)
+    g.add_batch(np.arange(nk, dtype=np.uint32), rng.standard_normal(nk) * 10)
+    n = 280000
+    qk = rng.integers(0, nk, n).astype(np.uint32)
+    qs = np.concatenate([rng.random(n - 6), [0.0, 1.0, 1e-12, 1 - 1e-12, 0.5, 5e-7]])
+    ck = rng.integers(0, nk, n).astype(np.uint32)
+    xs = np.concatenate([rng.standard_normal(n - 4) * 5, [-1e9, 1e9, 0.0, 0.25]])
+    hq, hc = g.query_batch(qk, qs, ck, xs)
+    eq, ec = g.quantiles(qk, qs), g.cdfs(ck, xs)
+    assert np.array_equal(hq.view(np.uint64), eq.view(np.uint64))
+    assert np.array_equal(hc.view(np.uint64), ec.view(np.uint64))
+
+
+def test_query_batch_empty_digest_reported(kd):
+    rng = np.random.default_rng(9)
+    g = kd.GroupedTDigest(512, 100.0, scale=kd.K1, session=kd.GpuSession())
+    g.add_batch(rng.integers(0, 511, 100000).astype(np.uint32), rng.standard_normal(100000))  # key 511 stays empty
+    n = 140000
+    qk = rng.integers(0, 511, n).astype(np.uint32)
+    qk[n // 2] = 511
+    with pytest.raises(ValueError, match="empty digest"):  # KD_EEMPTY, at the query that hit it
+        g.query_batch(qk, rng.random(n), qk[:0], np.zeros(0))
