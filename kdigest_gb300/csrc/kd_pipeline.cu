@@ -2096,8 +2096,22 @@ static KdSortBufs sort_bufs(const KdSession* s, KdWorkspace& w) {
 
 static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, const KdLevelDev& lv,
                           const double* dx, const double* dw, int id_last, KdStepView& v,
-                          const TileArgs* level0 = nullptr) {
+                          const TileArgs* level0 = nullptr, long long tiles_bound = -1) {
   cudaStream_t str = s->stream;
+  // The large-tile grid: the tuned blocks per SM, or one block per tile when
+  // the host's bound on the tiles fits the kernel's residency (a single
+  // digest's batch: its tiles then run in one wave instead of two).
+  if (s->large_resident == 0) {
+    int r = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_tiles_blk, KD_TILE_WARPS * 32, tile_smem()) !=
+        cudaSuccess)
+      r = 0;
+    cudaGetLastError();
+    s->large_resident = std::max(r, 1);
+  }
+  long long grid_large = (long long)s->num_sms * s->large_bps;
+  if (tiles_bound > grid_large && tiles_bound <= (long long)s->num_sms * s->large_resident)
+    grid_large = tiles_bound;
   TileArgs ta{sd, lv.Tl, lv.Ts, lv.I, lv, dx, dw, w.tkey, w.tbuf, w.st_count, w.scr_m,
               w.scr_w, w.tcount, w.cap_work, w.cap_inter, w.needs, s->force_exact, id_last,
               w.err};
@@ -2120,10 +2134,10 @@ static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, co
     v.note(cudaStreamWaitEvent(s->side, s->fork_ev, 0));
     k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * s->small_bps, 128, tile_smem_small(), s->side>>>(ta);
     v.note(cudaEventRecord(s->join_ev, s->side));
-    k_tiles_blk<<<s->num_sms * s->large_bps, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
+    k_tiles_blk<<<(int)grid_large, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
     v.note(cudaStreamWaitEvent(str, s->join_ev, 0));
   } else {
-    k_tiles_blk<<<s->num_sms * s->large_bps, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
+    k_tiles_blk<<<(int)grid_large, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
     k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * s->small_bps, 128, tile_smem_small(), str>>>(ta);
   }
   v.launches += 2;
@@ -2292,7 +2306,8 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   m0.tpscale = w.tpscale;
   m0.totals = w.totals;
   m0.n = n;
-  enqueue_tiles(s, w, sd, l0, nullptr, nullptr, id_last, v, &m0);
+  // level-0 tiles: each key's priors fill at most one tile, its samples n_k / 1024 + 1 more
+  enqueue_tiles(s, w, sd, l0, nullptr, nullptr, id_last, v, &m0, n / KD_TILE + 2 * keys_max + 1);
   stage_mark(s, 4);
   v.curA = a1;
   v.Iprev = l0.I;
