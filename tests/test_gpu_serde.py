@@ -129,3 +129,39 @@ def test_session_destroyed_before_its_store_and_server(kd):
         g.centroid_counts()
     srv.close()
     del g
+
+
+@pytest.mark.parametrize("clock", ["count", "time"])
+def test_export_equals_oracle_records_with_decay(kd, oracle, clock):
+    """Every record of a multi-key decayed store's batched export equals, byte
+    for byte, the oracle's to_bytes of that key's digest fed the same batches
+    (decayed weights, log-scale, clock and stored total in the header; keys
+    never ingested as empty records)."""
+    nk = 48
+    rng = np.random.default_rng(41 if clock == "count" else 42)
+    if clock == "count":
+        lam = oracle.log(2.0) / 5000.0
+        g = kd.GroupedTDigest(nk, 100.0, kd.Decay.rate(lam), scale=kd.K3)
+        refs = [oracle.Digest(oracle.K3, 100.0, lam) for _ in range(nk)]
+    else:
+        lam = oracle.log(2.0) / 60.0
+        g = kd.GroupedTDigest(nk, 200.0, kd.Decay.rate(lam), scale=kd.K2)
+        refs = [oracle.Digest(oracle.K2, 200.0, lam) for _ in range(nk)]
+    t = 0.0
+    for step in range(8):
+        n = int(rng.integers(2000, 30000))
+        keys = (rng.zipf(1.3, n) - 1) % (nk - 3)  # the last three keys stay empty
+        vals = rng.lognormal(0.0, 2.0, n)
+        if clock == "count":
+            g.add_batch(keys.astype(np.uint32), vals)
+            oracle.grouped_add_batch(refs, keys, vals)
+        else:
+            t += rng.exponential(30.0)
+            g.add_batch_at(keys.astype(np.uint32), vals, t)
+            for k in range(nk):
+                sel = vals[keys == k]
+                if len(sel):
+                    refs[k].add_batch_p_at(sel, t)
+    data, offs = g.export()
+    for k in range(nk):
+        assert data[offs[k]:offs[k + 1]] == refs[k].to_bytes(), k
