@@ -350,7 +350,13 @@ void run_group(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>* 
     if (rc == KD_OK) done = nw;
   }
   const double t1 = now_s();
-  std::lock_guard<std::mutex> lk(v->mu);
+  // Outside the lock: each request's status and query results (written to the
+  // caller's buffer before the status is published), and its consumed data
+  // moved out, to be freed after the lock is released (freeing a large
+  // request unmaps pages, which a submit waiting on the lock would wait for).
+  std::vector<int> status(sg.reqs.size(), KD_OK);
+  std::vector<std::vector<uint32_t>> dead_keys(sg.reqs.size());
+  std::vector<std::vector<double>> dead_vals(sg.reqs.size());
   for (long long i = 0; i < nw; ++i) {
     const Win& w = sg.wins[(size_t)i];
     // A failed window fails its requests and every later window's (whose
@@ -360,22 +366,27 @@ void run_group(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>* 
     for (size_t j = w.r0; j < w.r1; ++j) {
       Req& r = *sg.reqs[j];
       const size_t n = r.vals.size();
-      if (r.kind == KD_REQ_INGEST) {
-        r.status = wrc;
-      } else {
+      int stt = wrc;
+      if (r.kind != KD_REQ_INGEST) {
         long long& o = r.kind == KD_REQ_QUANTILE ? oq : oc;
-        int stt = wrc;
         if (wrc == KD_OK) {
           for (size_t k = 0; k < n; ++k)
             if (std::isnan(b.h_qo[o + (long long)k])) stt = KD_EEMPTY;  // inputs were validated
           if (r.out) memcpy(r.out, b.h_qo + o, n * 8);
         }
         o += (long long)n;
-        r.status = stt;
       }
+      status[j] = stt;
+      dead_keys[j].swap(r.keys);
+      dead_vals[j].swap(r.vals);
+    }
+  }
+  {
+    std::lock_guard<std::mutex> lk(v->mu);
+    for (size_t j = 0; j < sg.reqs.size(); ++j) {
+      Req& r = *sg.reqs[j];
+      r.status = status[j];
       r.t_done = t1;
-      std::vector<uint32_t>().swap(r.keys);  // the data is consumed: release it now
-      std::vector<double>().swap(r.vals);
       v->latencies.push_back(t1 - r.t_submit);
       v->buffered_dev -= std::min(v->buffered_dev, r.dev_bytes);
       auto wi = v->win_dev.find(r.window);
@@ -383,15 +394,15 @@ void run_group(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>* 
         v->win_dev.erase(wi);
       ++v->completed;
     }
+    v->dev_measured = v->s->mem_used + buf_dev_bytes(v->buf[0]) + buf_dev_bytes(v->buf[1]);
+    v->windows_done += nw;
+    ++v->groups;
+    if (nw > 1) v->windows_grouped += nw;
+    v->busy_s += t1 - t0;
+    v->max_group_s = std::max(v->max_group_s, t1 - t0);
+    if (t1 - t0 > 0.010) ++v->slow_groups;
+    v->cv.notify_all();
   }
-  v->dev_measured = v->s->mem_used + buf_dev_bytes(v->buf[0]) + buf_dev_bytes(v->buf[1]);
-  v->windows_done += nw;
-  ++v->groups;
-  if (nw > 1) v->windows_grouped += nw;
-  v->busy_s += t1 - t0;
-  v->max_group_s = std::max(v->max_group_s, t1 - t0);
-  if (t1 - t0 > 0.010) ++v->slow_groups;
-  v->cv.notify_all();
 }
 
 void worker_main(kd_server* v) {
