@@ -186,6 +186,50 @@ def test_retry_inside_a_window_group(kd):
     assert st["windows_grouped"] > 0  # full-sort windows keep the worker behind the client
 
 
+def test_failed_windows_report_and_the_server_recovers(kd):
+    """With every sort's look-back made to run out (the test-only session
+    option), each window's ingest fails with KD_ETIMEOUT: every request of
+    those windows completes with that status (none hangs), whether the
+    windows ran alone or grouped, and the store stays as the last good window
+    left it.  With the option cleared the server serves new windows, and the
+    store equals one that never saw the failed windows."""
+    from kdigest_gb300 import _native as N
+
+    rng = np.random.default_rng(21)
+    g = _store(kd)
+    sess = g.session
+    srv = kd.Server(g, window=1e-3)
+    first = rng.lognormal(0, 2, NK)
+    t0 = srv.submit_ingest(0.0, np.arange(NK, dtype=np.uint32), first)
+    srv.flush()
+    assert srv.wait(t0, 30.0)[0] == 0
+    sess.set_option(N.KD_OPT_TEST_WAIT, 2000)
+    tickets = []
+    for w in range(6):
+        t = 0.0105 + w * 1e-3
+        keys = rng.integers(0, NK, 20000).astype(np.uint32)  # several sort tiles
+        tickets.append(srv.submit_ingest(t, keys, rng.lognormal(0, 2, 20000)))
+        tickets.append(srv.submit_quantiles(t + 1e-4, keys[:10], rng.random(10)))
+    srv.flush()
+    assert [srv.wait(tk, 60.0)[0] for tk in tickets] == [N.KD_ETIMEOUT] * len(tickets)
+    sess.set_option(N.KD_OPT_TEST_WAIT, 0)
+    keys = rng.integers(0, NK, 20000).astype(np.uint32)
+    vals = rng.lognormal(0, 2, 20000)
+    t1 = srv.submit_ingest(0.05, keys, vals)
+    srv.flush()
+    assert srv.wait(t1, 30.0)[0] == 0
+    srv.close()
+    ref = _store(kd)
+    ref.add_batch_at(np.arange(NK, dtype=np.uint32), first, 0.0)
+    ref.add_batch_at(keys, vals, 0.05)
+    assert np.array_equal(g.centroid_counts(), ref.centroid_counts())
+    for k in range(0, NK, 5):
+        ma, wa = g.centroids(k)
+        mb, wb = ref.centroids(k)
+        assert np.array_equal(ma, mb) and np.array_equal(wa, wb), k
+        assert g.state(k) == ref.state(k)
+
+
 def test_concurrent_waiters(kd):
     """Waiters on other threads see their own results while the client submits."""
     reqs = _trace(14, 200, 2e-4)
