@@ -2470,8 +2470,8 @@ int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const 
   }
   int rc = kd_pipeline_prepare_device(s);
   if (rc) return rc;
-  const long long ncap = kd_ws_batch_cap(n, s->ws.err ? s->ws.cap_n : 0);
-  const long long keys_max = std::min<long long>(ncap, st->d.K);
+  long long ncap = kd_ws_batch_cap(n, s->ws.err ? s->ws.cap_n : 0);
+  long long keys_max = std::min<long long>(ncap, st->d.K);
   long long want_inter = std::max<long long>(64, 2 * (ncap / KD_TILE) + 64);
   long long want_work = 2 * keys_max + ncap / KD_TILE + 64;
   long long want_merged = 2 * ncap + 64 * keys_max + 1024;
@@ -2479,6 +2479,15 @@ int kd_pipeline_ingest(KdSession* s, KdStore* st, const uint32_t* d_keys, const 
     KdWorkspace& w0 = s->ws;
     rc = kd_ws_reserve(s, ncap, keys_max, std::max(want_inter, w0.cap_inter),
                        std::max(want_work, w0.cap_work), std::max(want_merged, w0.cap_merged), st->d.K);
+    if (rc == KD_ENOMEM && ncap > n) {  // no room for the doubled capacity: the batch's own
+      ncap = n;
+      keys_max = std::min<long long>(n, st->d.K);
+      want_inter = std::max<long long>(64, 2 * (n / KD_TILE) + 64);
+      want_work = 2 * keys_max + n / KD_TILE + 64;
+      want_merged = 2 * n + 64 * keys_max + 1024;
+      rc = kd_ws_reserve(s, ncap, keys_max, std::max(want_inter, w0.cap_inter),
+                         std::max(want_work, w0.cap_work), std::max(want_merged, w0.cap_merged), st->d.K);
+    }
     if (rc) return rc;
     rc = kd_pipeline_attempt(s, st, s->ws, d_keys, d_vals, d_wts, n, mode, timestamp, d_merge_min,
                              d_merge_max, d_merge_clock, carry, d_carry_mm);
@@ -2637,20 +2646,30 @@ int kd_pipeline_ingest_many(KdSession* s, KdStore* st, long long nb, const uint3
     // same request, so they grow together.
     long long capn = 0;
     for (KdWorkspace* wp : ws) capn = std::max(capn, wp->err ? wp->cap_n : 0LL);
-    const long long ncap = kd_ws_batch_cap(nmax, capn);
-    const long long kcap = std::min<long long>(ncap, sd.K);
-    long long ci = std::max(64LL, 2 * (ncap / KD_TILE) + 64);
-    long long cw = 2 * kcap + ncap / KD_TILE + 64;
-    long long cm = 2 * ncap + 64 * kcap + 1024;
-    for (KdWorkspace* wp : ws) {
-      ci = std::max(ci, wp->cap_inter);
-      cw = std::max(cw, wp->cap_work);
-      cm = std::max(cm, wp->cap_merged);
-    }
+    bool exact = false;  // sized for the largest batch itself (no room for the doubled capacity)
+    long long ncap = 0, kcap = 0, ci = 0, cw = 0, cm = 0;
+    auto size_for = [&](long long nc) {
+      ncap = nc;
+      kcap = std::min<long long>(ncap, sd.K);
+      ci = std::max(64LL, 2 * (ncap / KD_TILE) + 64);
+      cw = 2 * kcap + ncap / KD_TILE + 64;
+      cm = 2 * ncap + 64 * kcap + 1024;
+      for (KdWorkspace* wp : ws) {
+        ci = std::max(ci, wp->cap_inter);
+        cw = std::max(cw, wp->cap_work);
+        cm = std::max(cm, wp->cap_merged);
+      }
+    };
+    size_for(kd_ws_batch_cap(nmax, capn));
     bool room = true;
     for (long long i = base; i < std::min(nb, base + KD_PIPE_WS); ++i) {  // the workspaces in use
       KdWorkspace* wp = ws[i % KD_PIPE_WS];
       rc = kd_ws_reserve(s, ncap, kcap, ci, cw, cm, sd.K, wp);
+      if (rc == KD_ENOMEM && !exact && ncap > nmax) {
+        exact = true;
+        size_for(nmax);
+        rc = kd_ws_reserve(s, ncap, kcap, ci, cw, cm, sd.K, wp);
+      }
       if (rc == KD_ENOMEM && wp != &s->ws) {
         room = false;  // no memory for the extra workspaces: one call per batch
         break;
