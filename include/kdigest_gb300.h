@@ -284,7 +284,10 @@ KD_API int kd_store_import(kd_store* st, const uint32_t* keys, int64_t nkeys, co
  * buffered or in-flight request (its staging, and about 100 bytes of ingest
  * workspace per ingest pair) must stay within it; submit blocks until there is
  * room, and returns KD_ENOMEM for a request that could not fit alone.  The
- * store's session belongs to the server until it is destroyed.  Query outputs are written to `out` (n doubles, kept valid until
+ * server also holds two staging buffer sets, pinned host and device memory for
+ * groups of 2^22 ingest and 2^20 query pairs (about 68 MB each, allocated at
+ * creation; grown for larger groups).  The store's session belongs to the
+ * server until it is destroyed.  Query outputs are written to `out` (n doubles, kept valid until
  * the request is waited for); a query of an empty digest completes with
  * KD_EEMPTY and NaN. */
 #define KD_REQ_INGEST 0

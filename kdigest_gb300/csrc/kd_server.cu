@@ -463,6 +463,12 @@ KD_API int kd_server_create(kd_store* store, double window_s, size_t budget_byte
   if (rc == KD_OK) rc = kd_spath_flush(s, &store->st);
   if (rc == KD_OK && cudaStreamCreateWithFlags(&v->copy_stream, cudaStreamNonBlocking) != cudaSuccess) rc = KD_ECUDA;
   if (rc == KD_OK && cudaMalloc(&v->d_qerr, sizeof(KdErrHost)) != cudaSuccess) rc = KD_ECUDA;
+  // Staging for groups of up to 2^22 ingest and 2^20 query pairs, pinned now:
+  // pinning or unpinning tens of megabytes while serving holds the process's
+  // memory map and stalls every thread, clients included.  Larger groups
+  // still grow the buffers (geometrically); a failure here only defers that.
+  if (rc == KD_OK)
+    for (Buf& b : v->buf) grow_buf(b, (size_t)1 << 22, (size_t)1 << 20);
   if (rc == KD_OK && cudaMemset(v->d_qerr, 0, sizeof(KdErrHost)) != cudaSuccess) rc = KD_ECUDA;
   if (rc) {
     cudaGetLastError();
