@@ -5,8 +5,8 @@ the seeded inputs of tests/golden/gen.py).
 - In the reference association the oracle reproduces every fixture bit for
   bit (ids, counts, centroids, states, quantiles, cdf).
 - In the kernels' association (the default) ids, counts, weights and states
-  are identical and means, quantiles and cdf agree within the benchmark spec's bounds
-  for summation order: 1e-12 relative for centroids, 1e-9 for queries.
+  are identical and means, quantiles and cdf agree within the bounds set for
+  summation order: 1e-12 relative for centroids, 1e-9 for queries.
 - With the C library's log / asin in place of the shared FP64 functions, the
   bucket ids do not change on these cases.
 """

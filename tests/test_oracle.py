@@ -362,8 +362,8 @@ def test_tile_compress_equals_reference_lane_loops():
 def test_build_sums_differ_from_reference_in_means_only():
     """The kernels' association of sum(w*x) changes the means by rounding only:
     bucket ids, centroid counts and weights are identical to the reference's,
-    and every mean agrees within 1e-12 relative (the benchmark spec's bound for
-    summation order)."""
+    and every mean agrees within 1e-12 relative (the bound set for summation
+    order)."""
     rng = np.random.default_rng(77)
     worst = 0.0
     for scale, comp, x, w in _tile_cases(rng, 600):
