@@ -314,7 +314,10 @@ KD_API int kd_server_memory(kd_server* srv, size_t* in_use, size_t* peak, size_t
 /* Closes every open window and waits until all submitted requests completed. */
 KD_API int kd_server_flush(kd_server* srv);
 /* Submit-to-completion latency percentiles in seconds (p50, p99, p999), requests
- * completed, windows served and seconds the worker spent serving windows. */
+ * completed, windows served and seconds the worker spent serving windows.  The
+ * percentiles are exact over the first 2^20 completed requests; after that they
+ * are taken over a uniform sample of 2^20 of all completed requests (reservoir
+ * sampling, seeded: the same completions give the same sample). */
 KD_API int kd_server_stats(kd_server* srv, double* lat3, int64_t* completed, int64_t* windows,
                            double* busy_s);
 /* Windows that were closed together when the worker took them run as one

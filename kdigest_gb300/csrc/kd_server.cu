@@ -85,6 +85,19 @@ struct Buf {
 // batch, so a large window inside a group would grow all three (gigabytes at a
 // million keys, each growth a device-wide synchronisation).
 #define KD_SRV_GROUP_BIG (1LL << 18)
+// Latencies kept for the percentiles: every one up to this many completions,
+// then a uniform sample of this size (reservoir sampling, Algorithm R of
+// Vitter, "Random sampling with a reservoir", ACM TOMS 11(1), 1985), so a
+// long-running server holds a fixed 8 MB for them.
+#define KD_SRV_LAT_CAP ((size_t)1 << 20)
+
+// splitmix64: the reservoir's replacement indices (seeded, so repeatable).
+uint64_t srv_rand(uint64_t& x) {
+  uint64_t z = (x += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
 
 // One window of a staged group: its requests [r0, r1) of the group's list and
 // its place in the group's buffers.
@@ -175,7 +188,18 @@ struct kd_server {
   double clock_ts = -std::numeric_limits<double>::infinity();
   long long newest_window = std::numeric_limits<long long>::min();
   bool flushing = false, stop = false;
-  std::vector<double> latencies;
+  std::vector<double> latencies;  // all, or a uniform sample of KD_SRV_LAT_CAP
+  unsigned long long lat_seen = 0;
+  uint64_t lat_rng = 0x6b64696765737400ull;
+  void record_latency(double x) {
+    if (latencies.size() < KD_SRV_LAT_CAP) {
+      latencies.push_back(x);
+    } else {
+      const uint64_t j = srv_rand(lat_rng) % (lat_seen + 1);
+      if (j < KD_SRV_LAT_CAP) latencies[(size_t)j] = x;
+    }
+    ++lat_seen;
+  }
   size_t buffered_dev = 0;   // device footprint of submitted, not yet completed requests
   std::map<long long, size_t> win_dev;  // the same, per window
   unsigned long long next_seq = 0, admit_seq = 0;  // admission in submit order
@@ -387,7 +411,7 @@ void run_group(kd_server* v, Staged& sg, int stage_rc, std::unique_ptr<Staged>* 
       Req& r = *sg.reqs[j];
       r.status = status[j];
       r.t_done = t1;
-      v->latencies.push_back(t1 - r.t_submit);
+      v->record_latency(t1 - r.t_submit);
       v->buffered_dev -= std::min(v->buffered_dev, r.dev_bytes);
       auto wi = v->win_dev.find(r.window);
       if (wi != v->win_dev.end() && (wi->second -= std::min(wi->second, r.dev_bytes)) == 0)
@@ -610,9 +634,15 @@ KD_API int kd_server_flush(kd_server* v) {
 KD_API int kd_server_stats(kd_server* v, double* lat3, int64_t* completed, int64_t* windows,
                            double* busy_s) {
   if (!v) return KD_EINVAL;
-  std::lock_guard<std::mutex> lk(v->mu);
-  if (lat3) {
-    std::vector<double> l = v->latencies;
+  std::vector<double> l;
+  {
+    std::lock_guard<std::mutex> lk(v->mu);
+    if (lat3) l = v->latencies;
+    if (completed) *completed = v->completed;
+    if (windows) *windows = v->windows_done;
+    if (busy_s) *busy_s = v->busy_s;
+  }
+  if (lat3) {  // sorted outside the lock: the worker publishes results meanwhile
     std::sort(l.begin(), l.end());
     const double ps[3] = {0.50, 0.99, 0.999};
     for (int i = 0; i < 3; ++i) {
@@ -624,9 +654,6 @@ KD_API int kd_server_stats(kd_server* v, double* lat3, int64_t* completed, int64
       lat3[i] = l[std::min(l.size() - 1, k == 0 ? 0 : k - 1)];
     }
   }
-  if (completed) *completed = v->completed;
-  if (windows) *windows = v->windows_done;
-  if (busy_s) *busy_s = v->busy_s;
   return KD_OK;
 }
 
