@@ -690,7 +690,7 @@ def config2_line(args) -> dict:
                      "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(c2_gbs / peaks["hbm_gbs"], 5), "traffic": None,
                      "compulsory_bytes_per_step": c2_bytes,
-                     "note": "one digest per batch: about 30 dependent launches over 1024 tiles, "
+                     "note": "one digest per batch: 28 dependent launches over 1024 tiles, "
                              "bound by launch latency and FP64 arithmetic, not by HBM"},
     }
     return line

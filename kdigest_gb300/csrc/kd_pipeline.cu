@@ -2258,16 +2258,17 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   const uint32_t* sidx = with_idx ? w.idx[r] : nullptr;
   // scans with one entry per key: one item per thread when the partials fit
   const bool key_items1 = kd_scan_partials_needed(std::max<long long>(sd.K, keys_max), 1) <= w.cap_partials;
+  int scan_launches = 0;
   if (key_level && key_items1)
-    kd_scan<1>(KeyTouchedSrc{w.kstamp, w.kepoch},
+    scan_launches += kd_scan<1>(KeyTouchedSrc{w.kstamp, w.kepoch},
                KeyTouchedDst{w.kfirst, w.tkey, w.tstart, w.tmap, w.cap_keys}, sd.K, w.partials,
                &w.totals[0], str);
   else if (key_level)
-    kd_scan(KeyTouchedSrc{w.kstamp, w.kepoch},
-            KeyTouchedDst{w.kfirst, w.tkey, w.tstart, w.tmap, w.cap_keys}, sd.K, w.partials,
-            &w.totals[0], str);
+    scan_launches += kd_scan(KeyTouchedSrc{w.kstamp, w.kepoch},
+                             KeyTouchedDst{w.kfirst, w.tkey, w.tstart, w.tmap, w.cap_keys}, sd.K,
+                             w.partials, &w.totals[0], str);
   else
-    kd_scan(TouchedSrc{skey}, TouchedDst{skey, w.tkey, w.tstart, w.tmap, w.cap_keys, sd.K}, n,
+    scan_launches += kd_scan(TouchedSrc{skey}, TouchedDst{skey, w.tkey, w.tstart, w.tmap, w.cap_keys, sd.K}, n,
             w.partials, &w.totals[0], str);
   {
     PrepareArgs pa{sd, n, k64, w.tkey, w.tstart, w.totals, mode, w.d_call, w.tm, w.tprior,
@@ -2283,18 +2284,18 @@ static KdStepView enqueue_step(KdSession* s, KdStore* st, KdWorkspace& w, long l
   l0.I = (int*)&w.totals[2] + 0;
   int* a1 = (int*)&w.totals[1] + 2;
   if (key_items1)
-    kd_scan<1>(Plan0Src{w.totals, w.tm, s->small_cap},
+    scan_launches += kd_scan<1>(Plan0Src{w.totals, w.tm, s->small_cap},
                Plan0Dst{w.totals, w.tm, l0, w.lv[1], w.cap_work, w.cap_keys, s->small_cap}, keys_max,
                w.partials, &w.totals[1], str);
   else
-    kd_scan(Plan0Src{w.totals, w.tm, s->small_cap},
+    scan_launches += kd_scan(Plan0Src{w.totals, w.tm, s->small_cap},
             Plan0Dst{w.totals, w.tm, l0, w.lv[1], w.cap_work, w.cap_keys, s->small_cap}, keys_max,
             w.partials, &w.totals[1], str);
   {
     InterArgs ia{a1, l0, w.lv[1], l0.I, w.cap_inter, w.needs, w.err};
     k_inter0<<<1, 1024, 0, str>>>(ia);
   }
-  v.launches += 3 + 1 + 3 + 1;
+  v.launches += scan_launches + 2;
   stage_mark(s, 3);
   TileArgs m0{};
   m0.k64 = k64;

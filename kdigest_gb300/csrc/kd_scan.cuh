@@ -109,21 +109,56 @@ __global__ void __launch_bounds__(KD_SCAN_THREADS) kd_scan_apply(Src src, Dst ds
   }
 }
 
-// Host launcher.  `partials` must hold ceil(n_max / (KD_SCAN_THREADS * ITEMS))
-// int4s.  Fewer items per thread give more blocks: for short scans (one entry
-// per key) that spreads them over the GPU instead of a few blocks.
+// A scan that fits one block (n <= KD_SCAN_THREADS * ITEMS) in one launch: the
+// same values as reduce / partials / apply (the block's exclusive prefix is the
+// global one), the total written before any element is handed to dst.
+template <class Src, class Dst, int ITEMS = KD_SCAN_ITEMS>
+__global__ void __launch_bounds__(KD_SCAN_THREADS) kd_scan_single(Src src, Dst dst, long long n,
+                                                                  int4* total) {
+  __shared__ int4 sw[32];
+  const long long base = (long long)threadIdx.x * ITEMS;
+  int4 vals[ITEMS];
+  int4 acc = make_int4(0, 0, 0, 0);
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const long long i = base + k;
+    vals[k] = i < n ? src(i) : make_int4(0, 0, 0, 0);
+    acc = i4add(acc, vals[k]);
+  }
+  int4 tot;
+  const int4 incl = block_scan_incl(acc, sw, &tot);
+  if (threadIdx.x == 0 && total) *total = tot;
+  __syncthreads();
+  int4 run = make_int4(incl.x - acc.x, incl.y - acc.y, incl.z - acc.z, incl.w - acc.w);
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const long long i = base + k;
+    if (i < n) dst(i, run, vals[k]);
+    run = i4add(run, vals[k]);
+  }
+}
+
+// Host launcher; returns the kernels it launched.  `partials` must hold
+// ceil(n_max / (KD_SCAN_THREADS * ITEMS)) int4s.  Fewer items per thread give
+// more blocks: for short scans (one entry per key) that spreads them over the
+// GPU instead of a few blocks.  A scan of one block is one launch.
 template <int ITEMS = KD_SCAN_ITEMS, class Src, class Dst>
-static inline void kd_scan(Src src, Dst dst, long long n_max, int4* partials, int4* total,
-                           cudaStream_t st) {
+static inline int kd_scan(Src src, Dst dst, long long n_max, int4* partials, int4* total,
+                          cudaStream_t st) {
   if (n_max <= 0) {
     if (total) cudaMemsetAsync(total, 0, sizeof(int4), st);
-    return;
+    return 0;
   }
   constexpr long long tile = (long long)KD_SCAN_THREADS * ITEMS;
   int nb = (int)((n_max + tile - 1) / tile);
+  if (nb == 1) {
+    kd_scan_single<Src, Dst, ITEMS><<<1, KD_SCAN_THREADS, 0, st>>>(src, dst, n_max, total);
+    return 1;
+  }
   kd_scan_reduce<Src, ITEMS><<<nb, KD_SCAN_THREADS, 0, st>>>(src, n_max, partials);
   kd_scan_partials<<<1, 1024, 0, st>>>(partials, nb, total);
   kd_scan_apply<Src, Dst, ITEMS><<<nb, KD_SCAN_THREADS, 0, st>>>(src, dst, n_max, partials);
+  return 3;
 }
 
 static inline long long kd_scan_partials_needed(long long n_max, int items = KD_SCAN_ITEMS) {

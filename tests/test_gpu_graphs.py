@@ -116,7 +116,9 @@ def test_replays_with_stage_timing(kd):
         g.add_batch(keys, vals)
         e.add_batch(keys, vals)
     st = sess.stats()
-    assert st["ingests"] == 6 and st["launches"] > 6 * 20
+    # every ingest: prep, histogram, the radix passes, unpack, repair, two
+    # one-block scans, prepare, level plan, tiles and commit
+    assert st["ingests"] == 6 and st["launches"] >= 6 * 15
     assert all(v > 0.0 for v in st["stage_ms"].values()), st
     _same(g, e, nk)
 
