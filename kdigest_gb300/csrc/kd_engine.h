@@ -188,7 +188,9 @@ struct KdSession {
   // kernels.  Defaults are the committed autotuner choice for GB300.
   int small_cap = 128;
   int large_bps = 6;
-  int large_resident = 0;  // resident blocks per SM of the large-tile kernel (0: not queried yet)
+  // resident blocks per SM of the large-tile kernel, narrow and wide blocks
+  // (0: not queried yet)
+  int large_resident[2] = {0, 0};
   int small_bps = 8;
   // Run a level's two tile kernels on two streams (the second joins back
   // before anything reads their outputs).  Also a launch setting only.

@@ -513,31 +513,42 @@ __device__ int warp_compress(WarpTileSmall& t, int n, int scale, double compress
 
 // ---------------------------------------------------------------------------
 // Block-cooperative compress of one tile above the small-tile cap: the same
-// values as warp_compress, every stage spread over the block's KD_TILE_WARPS
-// warps (the tile in the chunk slot layout).
+// values as warp_compress, every stage spread over the block's W warps (the
+// tile in the chunk slot layout).  Stores of many keys use blocks of
+// KD_TILE_WARPS warps (many tiles per SM: more, smaller blocks); stores of at
+// most one key per SM use KD_TILE_WARPS_WIDE, since their upper levels hold a
+// few tiles each and wait for one tile's latency.
 // ---------------------------------------------------------------------------
 #define KD_TILE_WARPS 4
+#define KD_TILE_WARPS_WIDE 8
+// Chunks of the large-tile sum(w * x): the association the oracle restates
+// (128 chunks of ceil(n / 128) elements, carried across groups of 32), held
+// by threads 0..127 whatever the block size; the other threads hold none.
+#define KD_WX_CHUNKS 128
+static_assert(KD_TILE_WARPS * 32 >= KD_WX_CHUNKS && KD_TILE_WARPS_WIDE >= KD_TILE_WARPS,
+              "a thread per sum(w * x) chunk");
+template <int W>
 struct BlockScr {
   double totb;          // tile total (int64 bits in the integral path)
   double totd;
   KFilterTile ft;
   int nneed, ndiv, nout, stop, maxlen;
   unsigned nz;          // rounds of 32 that hold a head
-  long long wsum[KD_TILE_WARPS];
-  double cwx[KD_TILE_WARPS];  // per warp: segmented sum(w * x) carried out of its last chunk
-  double cw[KD_TILE_WARPS];   // the same for sum(w) (int64 bits, integral path)
-  int cf[KD_TILE_WARPS];      // whether the warp's chunks hold a head
+  long long wsum[W];
+  double cwx[W];  // per warp: segmented sum(w * x) carried out of its last chunk
+  double cw[W];   // the same for sum(w) (int64 bits, integral path)
+  int cf[W];      // whether the warp's chunks hold a head
   int rc[32];           // heads per round of 32 elements (then their offsets)
   unsigned hb[32];      // head ballot per round
 };
 
-template <bool kInt>
-__device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, double compression,
+template <bool kInt, int W>
+__device__ int block_compress(WarpTile& t, BlockScr<W>& bs, int n, int scale, double compression,
                               int force_exact, int32_t id_last, double* __restrict__ om,
                               double* __restrict__ ow) {
   typedef TileAcc<kInt> A;
   typedef typename A::T T;
-  constexpr int NT = KD_TILE_WARPS * 32;
+  constexpr int NT = W * 32;
   constexpr int PER = KD_TILE / NT;  // positions per thread
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const SlotMap slot(n);
@@ -549,7 +560,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
   if (kInt) {
     // exact int64 sums: each warp scans a contiguous range of rounds, then
     // adds the totals of the warps before it
-    const int per = (rounds + KD_TILE_WARPS - 1) / KD_TILE_WARPS;
+    const int per = (rounds + W - 1) / W;
     const int rb = warp * per, re = min(rounds, rb + per);
     T carry = 0;
     for (int r = rb; r < re; ++r) {
@@ -568,7 +579,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
     __syncthreads();
     T off = 0, all = 0;
 #pragma unroll
-    for (int w2 = 0; w2 < KD_TILE_WARPS; ++w2) {
+    for (int w2 = 0; w2 < W; ++w2) {
       const T s2 = (T)bs.wsum[w2];
       if (w2 < warp) off = A::add(off, s2);
       all = A::add(all, s2);
@@ -634,7 +645,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
   const double totd = bs.totd;
   const KFilterTile ft = bs.ft;
 
-  // 3a. Bucket ids; warp w takes rounds w, w + KD_TILE_WARPS, ...
+  // 3a. Bucket ids; warp w takes rounds w, w + W, ...
   int* const ids = t.ids();
   unsigned short* const plist = t.poslist();
   for (int r0 = warp * 32; r0 < n; r0 += NT) {
@@ -681,7 +692,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
   __syncthreads();
   // 3c. Heads: flags per round, offsets by a scan over the rounds, then the
   //     positions (the ids are all read before any position is written).
-  for (int r = warp; r < rounds; r += KD_TILE_WARPS) {
+  for (int r = warp; r < rounds; r += W) {
     const int p = r * 32 + lane;
     const bool act = p < n;
     const int32_t id = act ? ids[p] : 0;
@@ -710,7 +721,7 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
     }
   }
   __syncthreads();
-  for (int r = warp; r < rounds; r += KD_TILE_WARPS) {
+  for (int r = warp; r < rounds; r += W) {
     const unsigned hbits = bs.hb[r];
     if ((hbits >> lane) & 1u) t.headpos[bs.rc[r] + __popc(hbits & lt_mask)] = (unsigned short)(r * 32 + lane);
   }
@@ -795,9 +806,9 @@ __device__ int block_compress(WarpTile& t, BlockScr& bs, int n, int scale, doubl
     __syncthreads();
     {  // one chunk per thread: serial pieces, a segmented carry across each
        // warp's 32 chunks, then across the warps in order
-      const int E4 = (n + NT - 1) / NT;
+      const int E4 = (n + KD_WX_CHUNKS - 1) / KD_WX_CHUNKS;
       const int lo = tid * E4;
-      const int cnt = max(0, min(E4, n - lo));
+      const int cnt = max(0, min(E4, n - lo));  // none for tid >= KD_WX_CHUNKS
       T aw = 0;
       double awx = 0.0;
       bool head_seen = false;
@@ -1548,10 +1559,11 @@ __global__ void __launch_bounds__(32 * (CAP == KD_TILE ? 1 : 4)) k_tiles(TileArg
 
 // One block of KD_TILE_WARPS warps per tile above the small-tile cap (the large
 // work list): coalesced load into the slot layout, then block_compress.
-__global__ void __launch_bounds__(KD_TILE_WARPS * 32) k_tiles_blk(TileArgs a) {
+template <int W>
+__global__ void __launch_bounds__(W * 32) k_tiles_blk(TileArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpTile& t = *reinterpret_cast<WarpTile*>(smem_raw);
-  __shared__ BlockScr bs;
+  __shared__ BlockScr<W> bs;
   if (threadIdx.x == 0) bs.stop = kd_err_get(a.err);  // one read, so the block exits as one
   __syncthreads();
   if (bs.stop) return;
@@ -1589,9 +1601,9 @@ __global__ void __launch_bounds__(KD_TILE_WARPS * 32) k_tiles_blk(TileArgs a) {
     integral = __syncthreads_and(integral);
     const TileOut o = tile_out(a, ai, lt, j, m);
     const int c = integral
-                      ? block_compress<true>(t, bs, n, s.scale, s.compression, a.force_exact,
+                      ? block_compress<true, W>(t, bs, n, s.scale, s.compression, a.force_exact,
                                              a.id_last, o.m, o.w)
-                      : block_compress<false>(t, bs, n, s.scale, s.compression, a.force_exact,
+                      : block_compress<false, W>(t, bs, n, s.scale, s.compression, a.force_exact,
                                               a.id_last, o.m, o.w);
     if (threadIdx.x == 0) *o.count = c;
   }
@@ -2047,7 +2059,10 @@ int kd_pipeline_prepare_device(KdSession* s) {
   static std::atomic<bool> done[64];
   std::atomic<bool>* flag = (s->device >= 0 && s->device < 64) ? &done[s->device] : nullptr;
   if (flag && flag->load(std::memory_order_acquire)) return KD_OK;
-  KD_CK(cudaFuncSetAttribute(k_tiles_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem()));
+  KD_CK(cudaFuncSetAttribute(k_tiles_blk<KD_TILE_WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tile_smem()));
+  KD_CK(cudaFuncSetAttribute(k_tiles_blk<KD_TILE_WARPS_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tile_smem()));
   KD_CK(cudaFuncSetAttribute(kd_rs_onesweep<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kd_rs_smem(true)));
   KD_CK(cudaFuncSetAttribute(kd_rs_onesweep<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2098,19 +2113,27 @@ static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, co
                           const double* dx, const double* dw, int id_last, KdStepView& v,
                           const TileArgs* level0 = nullptr, long long tiles_bound = -1) {
   cudaStream_t str = s->stream;
+  // Wide blocks for stores of at most one key per SM (their levels above 0
+  // hold few tiles, each waiting for one tile's latency), narrow ones else.
+  const bool wide = sd.K <= (long long)s->num_sms;
+  const int nt_large = (wide ? KD_TILE_WARPS_WIDE : KD_TILE_WARPS) * 32;
   // The large-tile grid: the tuned blocks per SM, or one block per tile when
   // the host's bound on the tiles fits the kernel's residency (a single
   // digest's batch: its tiles then run in one wave instead of two).
-  if (s->large_resident == 0) {
+  int& resident = s->large_resident[wide ? 1 : 0];
+  if (resident == 0) {
     int r = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_tiles_blk, KD_TILE_WARPS * 32, tile_smem()) !=
-        cudaSuccess)
-      r = 0;
+    const cudaError_t e =
+        wide ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_tiles_blk<KD_TILE_WARPS_WIDE>, nt_large,
+                                                             tile_smem())
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_tiles_blk<KD_TILE_WARPS>, nt_large,
+                                                             tile_smem());
+    if (e != cudaSuccess) r = 0;
     cudaGetLastError();
-    s->large_resident = std::max(r, 1);
+    resident = std::max(r, 1);
   }
   long long grid_large = (long long)s->num_sms * s->large_bps;
-  if (tiles_bound > grid_large && tiles_bound <= (long long)s->num_sms * s->large_resident)
+  if (tiles_bound > grid_large && tiles_bound <= (long long)s->num_sms * resident)
     grid_large = tiles_bound;
   TileArgs ta{sd, lv.Tl, lv.Ts, lv.I, lv, dx, dw, w.tkey, w.tbuf, w.st_count, w.scr_m,
               w.scr_w, w.tcount, w.cap_work, w.cap_inter, w.needs, s->force_exact, id_last,
@@ -2127,6 +2150,12 @@ static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, co
     ta.totals = level0->totals;
     ta.n = level0->n;
   }
+  auto launch_large = [&]() {
+    if (wide)
+      k_tiles_blk<KD_TILE_WARPS_WIDE><<<(int)grid_large, nt_large, tile_smem(), str>>>(ta);
+    else
+      k_tiles_blk<KD_TILE_WARPS><<<(int)grid_large, nt_large, tile_smem(), str>>>(ta);
+  };
   if (s->concurrent_tiles && s->side) {
     // fork: the small-tile kernel on the side stream, joined back before the
     // next launch on the session stream (inside a capture: a graph branch)
@@ -2134,10 +2163,10 @@ static void enqueue_tiles(KdSession* s, KdWorkspace& w, const KdStoreDev& sd, co
     v.note(cudaStreamWaitEvent(s->side, s->fork_ev, 0));
     k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * s->small_bps, 128, tile_smem_small(), s->side>>>(ta);
     v.note(cudaEventRecord(s->join_ev, s->side));
-    k_tiles_blk<<<(int)grid_large, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
+    launch_large();
     v.note(cudaStreamWaitEvent(str, s->join_ev, 0));
   } else {
-    k_tiles_blk<<<(int)grid_large, KD_TILE_WARPS * 32, tile_smem(), str>>>(ta);
+    launch_large();
     k_tiles<KD_SERIAL_TILE_MAX><<<s->num_sms * s->small_bps, 128, tile_smem_small(), str>>>(ta);
   }
   v.launches += 2;
